@@ -1,0 +1,329 @@
+"""Benchmark of the FOM rank-2 FP64 velocity-stress leapfrog (DOF-updates/s).
+
+Workload (one GPU): staggered axisymmetric grid of 1000 theta x 2000 r vertices,
+theta in [0, 180] deg, r in [3480, 6371] km; radially layered material with
+density 3.3->5.6 g/cm^3 and shear speed 4.4->7.3 km/s increasing with depth;
+M = 256 forcings (Gaussian-derivative signals, depths U[200,700] km, periods
+U[30,90] s, delay 180 s, seeded); dt from CFL 0.25; receivers every 1 degree at
+the surface (seismogram every step).  A "step" is one leapfrog step (velocity
+half-step + stress half-step) of all 256 columns: 5,997,000 x 256 DOF-updates.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's CRS leapfrog
+(oracle/, Kokkos-Kernels CRS row semantics, OpenMP over all host threads) on a
+bounded sample of the same workload.  Under torchrun every rank runs its own
+256 forcing columns (the columns are independent: weak scaling, no collective
+in the time loop); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NTH, NR, M = 1000, 2000, 256
+MATERIAL = [3300.0, 2300.0 / 2891000.0, 0.0, 4400.0, 2900.0 / 2891000.0, 0.0]
+SEED = 20261203
+METRIC = "FOM DOF-updates/s (rank-2 FP64 leapfrog)"
+WORKLOAD = "FOM rank-2 FP64, 1000 theta x 2000 r grid, M=256 forcings"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def workload_inputs(np, mesh):
+    rng = np.random.default_rng(SEED)
+    depths = rng.uniform(200.0, 700.0, M)
+    periods = rng.uniform(30.0, 90.0, M)
+    gids = [mesh.map_source(float(d), 0.0) for d in depths]
+    rcv = [mesh.map_receiver(float(a)) for a in range(0, 181)]
+    dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
+    return gids, periods, rcv, dt
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(np, budget_s=20.0):
+    """The oracle's CRS leapfrog on a bounded sample of the same workload, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    import shaw_gb300 as shaw
+    oracle_lib.build()
+    mesh = shaw.Mesh.generate(NTH, NR)
+    with tempfile.TemporaryDirectory() as d:
+        mesh.write(d)
+        om = oracle_lib.OracleMesh(d)
+    om.set_material("unilayer", [(MATERIAL[0:3], MATERIAL[3:6])])
+    threads = oracle_lib.lib().orc_num_threads(0)
+    ms = 16  # forcing columns in the sample
+    xv = np.zeros((om.nvp, ms))
+    xs = np.random.default_rng(1).standard_normal((om.nsp, ms))
+    dt = 0.01
+    om.fom_advance(xv, xs, 1, dt)  # first touch
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and steps < 200:
+        om.fom_advance(xv, xs, 1, dt)
+        steps += 1
+    el = time.perf_counter() - t0
+    units = (om.nvp + om.nsp) * ms * steps
+    return dict(value=units / el, unit="DOF-updates/s", cores=threads, kind="port",
+                sample="%d leapfrog steps of %d of the 256 forcing columns on the 1000x2000 grid (%.1f s)"
+                       % (steps, ms, el), seconds=el, steps=steps)
+
+
+def run_reference(args):
+    import numpy as np
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    per_step_budget = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    import shaw_gb300 as shaw
+    oracle_lib.build()
+    shaw.build()
+    mesh = shaw.Mesh.generate(NTH, NR)
+    with tempfile.TemporaryDirectory() as d:
+        mesh.write(d)
+        om = oracle_lib.OracleMesh(d)
+    om.set_material("unilayer", [(MATERIAL[0:3], MATERIAL[3:6])])
+    threads = oracle_lib.lib().orc_num_threads(0)
+    ms = 16
+    xv = np.zeros((om.nvp, ms))
+    xs = np.random.default_rng(1).standard_normal((om.nsp, ms))
+    for _ in range(args.warmup):
+        om.fom_advance(xv, xs, 1, 0.01)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        om.fom_advance(xv, xs, 1, 0.01)
+    el = time.perf_counter() - t0
+    value = (om.nvp + om.nsp) * ms * args.steps / el
+    sample = "each step: one leapfrog step of %d of the 256 forcing columns on the 1000x2000 grid" % ms
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3 * (M / ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings": M, "sample_forcings": ms,
+                       "l2": "inputs larger than L2 (state 12 GB)"},
+            "cpu_baseline": {"value": value, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "host": platform.machine(), "cpu_threads": threads}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+    import torch
+    import shaw_gb300 as shaw
+    shaw.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(0)
+
+    mesh = shaw.Mesh.generate(NTH, NR)
+    mesh.set_material("unilayer", MATERIAL)
+    gids, periods, rcv, dt = workload_inputs(np, mesh)
+    dofs = (mesh.nvp + mesh.nsp) * M
+    total_steps = args.warmup + args.steps
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # ---- device-resident throughput -------------------------------------------------
+    f = shaw.Fom(mesh, 2, M)
+    f.set_sources(gids, "gaussDer", periods, 180.0)
+    f.set_receivers(rcv, 1, total_steps)
+    f.reset()
+    stream = torch.cuda.ExternalStream(f.stream)
+    f.advance(dt, args.warmup)
+    f.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = f.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        f.advance(dt, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    f.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = f.kernel_launches - launches0
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * dofs * args.steps / (ms / 1e3)
+
+    # ---- per-kernel durations (CUDA events on the launching stream) -----------------
+    kv, ks = [], []
+    for _ in range(6):
+        a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        a.record(stream)
+        f.update_velocity(dt, total_steps)
+        b.record(stream)
+        f.update_stress(dt)
+        c.record(stream)
+        c.synchronize()
+        kv.append(a.elapsed_time(b))
+        ks.append(b.elapsed_time(c))
+    kv, ks = sorted(kv)[1:-1], sorted(ks)[1:-1]
+    t_v, t_s = sum(kv) / len(kv) / 1e3, sum(ks) / len(ks) / 1e3
+    f.close()
+
+    # ---- end to end through the C ABI from host buffers -------------------------------
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    g = shaw.Fom(mesh, 2, M)                      # operators H2D from the host mesh arrays
+    g.set_sources(gids, "gaussDer", periods, 180.0)
+    g.set_receivers(rcv, 1, args.steps)
+    g.run(dt, args.steps)
+    seis = g.seismogram()                         # D2H of the result
+    e2e_s = time.perf_counter() - t0
+    g.close()
+    barrier()
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * dofs * args.steps / e2e_s
+    h2d = (mesh.nvp * (5 * 8 + 2 * 8 + 8 + 4 * 8 + 8) + mesh.nsp * (3 * 8 + 4 + 2 * 8 + 8 + 8)  # desc arrays
+           + M * (8 + 4 + 8 + 8) + len(rcv) * 8)
+    d2h = seis.nbytes
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    hbm, peak_kind = measured_peaks()
+    # dominant kernel: the stress half-step (nsp ~ 2 nvp).  Algorithmic bytes per launch:
+    # read + write every sp value, read every vp value once: (2*nsp + nvp) * M * 8.
+    bytes_s = (2 * mesh.nsp + mesh.nvp) * M * 8
+    bytes_v = (2 * mesh.nvp + mesh.nsp) * M * 8
+    ach = bytes_s / t_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings_per_gpu": M, "dt": dt,
+                   "receivers": len(rcv), "seismogram_freq": 1,
+                   "l2": "inputs larger than L2 (state 12.3 GB per GPU), no flush needed",
+                   "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": "fom_stress_kernel", "achieved": ach, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "algorithmic_bytes_per_launch": bytes_s, "launch_ms": t_s * 1e3,
+                     "velocity_kernel": {"launch_ms": t_v * 1e3, "achieved": bytes_v / t_v / 1e9,
+                                         "frac": bytes_v / t_v / 1e9 / hbm},
+                     "fp64_flops_per_step": (8 * (mesh.nvp - 2 * mesh.nr) + 4 * mesh.nsp) * M},
+        "e2e": {"value": e2e_value, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if world == 1:
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(np).items() if k in
+                                ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

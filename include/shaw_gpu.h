@@ -1,0 +1,205 @@
+/*
+ * shaw_gpu.h -- C ABI of the GB300 (sm_103a) implementation of SHAW's two
+ * data-parallel hot paths:
+ *   (a) the full-order (FOM) velocity-stress leapfrog on the staggered
+ *       axisymmetric (r, theta) grid, rank-1 (one forcing) and rank-2 (M forcings);
+ *   (b) the Galerkin ROM leapfrog on the reduced operators.
+ *
+ * Conventions (the same for every entry point):
+ *   - every function returns an int status (SHAW_OK == 0); no exception crosses
+ *     the ABI.  shaw_last_error() gives a one-line message for the calling thread.
+ *     The status codes mirror the reference's throw sites.
+ *   - caller-owned host arrays are copied in; the library owns all device memory.
+ *   - one CUDA stream per handle (shaw_*_stream); a handle is not thread-safe.
+ *   - gids follow the reference's mesh files: vp gid = j*nth + i (theta fastest),
+ *     sp gids interleaved per cell (srp, then stp), see meshing/helpers/full_mesh_utils.py.
+ *   - multi-column host arrays are column-major ("LayoutLeft"), as the
+ *     reference's host views are when written to file.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   ShWavePP ctor + fillVpJacobian/fillSpJacobian  src/kokkos/shwavepp.hpp:100-148,319-466
+ *   updateVelocity / updateStress                  src/kokkos/fom_update_kernels.hpp:60-181
+ *   runFom                                         src/kokkos/fom_run.hpp:66-161
+ *   RankOneForcing / RankTwoForcing                src/kokkos/forcing_rank_one.hpp:56-179,
+ *                                                  src/kokkos/forcing_rank_two.hpp:56-173
+ *   Seismogram                                     src/kokkos/seismogram.hpp:82-233
+ *   StateObserver                                  src/kokkos/state_observer.hpp:81-231
+ *   computeRomOperatorsUsingFomJacsWithMatProp     src/kokkos/rom_compute_jacobians.hpp:59-109
+ *   runRomRankOneForcing                           src/kokkos/rom_run_rank_one.hpp:91-162
+ *   runRomRankTwoForcing                           src/kokkos/torevise/run_rom_rank_two_forcing.hpp:119-201
+ *   reconstructSeismogram (ROM seismogram)         src/tools/main_reconstruct_seismo.cc:147-190
+ *   computeThinSVD (POD)                           src/tools/main_eigen_svd.cc:113-197
+ */
+#ifndef SHAW_GPU_H_
+#define SHAW_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SHAW_OK                 0
+#define SHAW_ERR_INVALID_ARG    1  /* bad pointer / size / enum value                        */
+#define SHAW_ERR_CUDA           2  /* a CUDA runtime call failed                              */
+#define SHAW_ERR_MESH           3  /* mesh files missing/malformed, or not a full structured mesh */
+#define SHAW_ERR_FREQ_DIVISOR   4  /* sampling freq does not divide the step count
+                                      (seismogram.hpp:163-169, state_observer.hpp:130-143)   */
+#define SHAW_ERR_CFL            5  /* check_cfl.hpp:66-73                                     */
+#define SHAW_ERR_DISPERSION     6  /* check_dispersion_criterion.hpp:68-81                    */
+#define SHAW_ERR_FORCING_SETS   7  /* realizations not divisible by forcingSize
+                                      (fom_problem_rank_two.hpp:136-139)                      */
+#define SHAW_ERR_NONFINITE      8  /* NaN/Inf seen in a sampled state                         */
+#define SHAW_ERR_IO             9  /* file could not be opened / written                      */
+#define SHAW_ERR_PARSE         10  /* input file invalid (throw sites of src/shared/parser/)  */
+#define SHAW_ERR_UNSUPPORTED   11  /* valid input outside what this build implements          */
+#define SHAW_ERR_OUT_OF_MEMORY 12
+#define SHAW_ERR_STATE         13  /* call order violated (e.g. run before set_sources)      */
+
+/* ---- signal kinds (src/shared/enums/supported_signal_enums.hpp) --------- */
+#define SHAW_SIGNAL_RICKER    0
+#define SHAW_SIGNAL_SINUSOID  1
+#define SHAW_SIGNAL_GAUSS_DER 2
+
+/* ---- arithmetic of a run ------------------------------------------------ */
+#define SHAW_FP64             0  /* plain FP64 (the oracle-parity path)                     */
+#define SHAW_MIXED_TF32X3     1  /* ROM: split TF32x3 products, FP32 accumulate, Kahan state */
+#define SHAW_MIXED_BF16X3     2  /* ROM: split BF16x3 products, FP32 accumulate, Kahan state */
+#define SHAW_MIXED_FP32       3  /* FP32 products, Kahan-compensated FP32 state             */
+
+const char* shaw_last_error(void);
+const char* shaw_version(void);
+
+/* ======================================================================== *
+ *  FOM                                                                      *
+ * ======================================================================== */
+
+/* What ShWavePP reads from the mesh directory and the material model
+ * (src/kokkos/shwavepp.hpp:100-146).  Arrays are indexed by gid. */
+typedef struct {
+  uint64_t nth, nr;             /* grid points along theta / r (mesh_info.dat)          */
+  uint64_t nvp, nsp;            /* numPtsVp, numPtsSp                                    */
+  double dth_inv;               /* 1/dth  [1/rad]                                        */
+  double drr_inv;               /* 1/dr   [1/m]                                          */
+  const int64_t* graph_vp;      /* nvp x 5 row-major: gid, W, N, E, S  (graph_vp.dat)    */
+  const int64_t* graph_sp;      /* nsp x 3 row-major: gid, first, second (graph_sp.dat)  */
+  const int32_t* labels_sp;     /* nsp: 1 = srp (sigma_r,phi), 2 = stp (sigma_theta,phi) */
+  const double* coords_vp;      /* nvp x 2: theta [rad], 1/r [1/m]                       */
+  const double* coords_sp;      /* nsp x 2                                               */
+  const double* cot_vp;         /* nvp: cot(theta), 0 on the symmetry axis               */
+  const double* cot_sp;         /* nsp                                                   */
+  const double* coeff_vp;       /* nvp x 4: boundary factors c0..c3 (coeff_vp.dat)       */
+  const double* rho_inv_vp;     /* nvp: 1/density                                        */
+  const double* shear_mod_sp;   /* nsp: density * vs^2                                   */
+} shaw_fom_operator_desc;
+
+typedef struct shaw_fom_s* shaw_fom_t;
+
+/* ShWavePP ctor + state allocation of FomProblemRank{One,Two}Forcing.
+ * rank 1: one forcing, vector state, source added as KokkosBlas::mult does;
+ * rank 2: num_forcings columns, source added as AddForcingRank2 does.
+ * precision: SHAW_FP64. */
+int shaw_fom_create(const shaw_fom_operator_desc* desc, int rank, uint32_t num_forcings, int precision,
+                    shaw_fom_t* out);
+void shaw_fom_destroy(shaw_fom_t h);
+
+/* RankOneForcing / RankTwoForcing: one source per column (vp gid from the
+ * reference's point-source mapper) and its signal.  The signal is evaluated
+ * on the device at t = (n-1)*dt at step n, as the reference does. */
+int shaw_fom_set_sources(shaw_fom_t h, const uint64_t* vp_gid, const int32_t* kind,
+                         const double* period, const double* delay);
+
+/* Seismogram: receivers' vp gids; every `freq` steps x_vp[gid_r, :] is stored.
+ * nsteps % freq must be 0.  R == 0 disables. */
+int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* vp_gid, uint32_t num_receivers,
+                           uint64_t freq, uint64_t nsteps);
+
+/* StateObserver: snapshot matrices written straight into caller host arrays,
+ * vp: nvp x (nsteps/freq_vp) x M, sp: nsp x (nsteps/freq_sp) x M (LayoutLeft).
+ * The arrays must stay valid until the handle is destroyed or snapshots are
+ * disabled (freq 0).  They are page-locked by the library while registered. */
+int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t freq_vp, uint64_t freq_sp, uint64_t nsteps,
+                           double* host_vp, double* host_sp);
+
+/* runFom: zero the states, then nsteps leapfrog steps (blocking). */
+int shaw_fom_run(shaw_fom_t h, double dt, uint64_t nsteps);
+/* Zero states and counters (the start of runFom). */
+int shaw_fom_reset(shaw_fom_t h);
+/* Enqueue nsteps more leapfrog steps on the handle's stream (non-blocking). */
+int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps);
+/* updateVelocity for step `step` (1-based; forcing at t=(step-1)*dt) and
+ * updateStress: one half-step each, on the handle's stream. */
+int shaw_fom_update_velocity(shaw_fom_t h, double dt, uint64_t step);
+int shaw_fom_update_stress(shaw_fom_t h, double dt);
+int shaw_fom_synchronize(shaw_fom_t h);
+
+/* Copy out the seismogram, R x (nsteps/freq) x M (LayoutLeft). */
+int shaw_fom_get_seismogram(shaw_fom_t h, double* out);
+/* Copy the states out / in: vp nvp x M, sp nsp x M (LayoutLeft). */
+int shaw_fom_get_state(shaw_fom_t h, double* vp, double* sp);
+int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
+/* The handle's cudaStream_t, for callers that time with CUDA events. */
+void* shaw_fom_stream(shaw_fom_t h);
+/* Kernels this handle has launched since creation (graph replays count each node). */
+uint64_t shaw_fom_kernel_launches(shaw_fom_t h);
+
+/* ======================================================================== *
+ *  Host-side setup (the reference's main.cc + MeshInfo + material + mappers) *
+ * ======================================================================== */
+
+typedef struct shaw_mesh_s* shaw_mesh_t;
+
+/* MeshInfo + readFullMeshGraphFile + readFullMeshCoeffFile
+ * (src/shared/mesh_helpers/mesh_info.hpp:116-214, read_graph_file.hpp:54-124,
+ *  read_vpcoeff_file.hpp:52-81). */
+int shaw_mesh_load(const char* mesh_dir, shaw_mesh_t* out);
+/* The full-mesh generator (meshing/create_single_mesh.py -> helpers/full_mesh_utils.py,
+ * build_graph_impl.py), in memory. Angles in degrees, radii in km. */
+int shaw_mesh_generate(uint64_t nth, uint64_t nr, double th_left_deg, double th_right_deg,
+                       double r_cmb_km, double r_surf_km, shaw_mesh_t* out);
+/* Write mesh_info.dat, graph_vp.dat, graph_sp.dat, coeff_vp.dat into dir
+ * (meshing/helpers/write_files.py formats). */
+int shaw_mesh_write(shaw_mesh_t m, const char* dir);
+/* out[14]: thL, thR [deg], rCmb, rSurf [m], dth [rad], dr [m], 1/dth, 1/dr,
+ * nvp, nsp, nth, nr, minArc, maxArc [m]. */
+int shaw_mesh_info(shaw_mesh_t m, double* out);
+/* Material models (src/shared/material_models/material_model_{unilayer,bilayer,prem}.hpp):
+ *   SHAW_MATERIAL_UNILAYER params: rho[3], vs[3]           (depth in metres)
+ *   SHAW_MATERIAL_BILAYER  params: rho1[3], vs1[3], disc_km, rho2[3], vs2[3]
+ *   SHAW_MATERIAL_PREM     params: none
+ * Fills 1/rho at vp points and rho*vs^2 at sp points (shwavepp.hpp:246-286). */
+#define SHAW_MATERIAL_UNILAYER 0
+#define SHAW_MATERIAL_BILAYER  1
+#define SHAW_MATERIAL_PREM     2
+int shaw_mesh_set_material(shaw_mesh_t m, int kind, const double* params, uint32_t nparams);
+/* Caller-computed material (the reference's "custom" kind): per-point arrays. */
+int shaw_mesh_set_material_arrays(shaw_mesh_t m, const double* rho_inv_vp, const double* shear_mod_sp);
+/* min/max shear velocity seen while setting the material (for the checkers). */
+int shaw_mesh_min_max_vs(shaw_mesh_t m, double* minmax);
+/* Views into the mesh's arrays, valid while the mesh lives. */
+int shaw_mesh_operator_desc(shaw_mesh_t m, shaw_fom_operator_desc* out);
+/* mapPointSourceToGridPoint / mapNominalLocationToVelocityGridPoint. */
+int shaw_mesh_map_source(shaw_mesh_t m, double depth_km, double angle_deg, uint64_t* gid);
+int shaw_mesh_map_receiver(shaw_mesh_t m, double angle_deg, uint64_t* gid);
+/* checkCfl (returns SHAW_ERR_CFL on violation) and checkDispersionCriterion
+ * (SHAW_ERR_DISPERSION); *value receives the cfl number. */
+int shaw_mesh_check_cfl(shaw_mesh_t m, double dt, double* value);
+int shaw_mesh_check_dispersion(shaw_mesh_t m, double max_freq);
+void shaw_mesh_destroy(shaw_mesh_t m);
+
+/* shawExe <input.yaml>: parse the YAML input, run the FOM (rank-1 single or
+ * multi-forcing, rank-2 sets) or the ROM, and write the reference's output
+ * files into the current directory. */
+int shaw_run_input_file(const char* yaml_path);
+/* InputParser (src/shared/parser/input_parser.hpp:52-70): parse and validate an
+ * input file without running it; writes "key=value" lines (one per parsed
+ * field, the reference's getter names) into out[cap].  Returns SHAW_ERR_PARSE
+ * with the reference's message on invalid input. */
+int shaw_parse_input(const char* yaml_path, char* out, size_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SHAW_GPU_H_ */

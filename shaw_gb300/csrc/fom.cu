@@ -1,0 +1,780 @@
+// fom.cu -- matrix-free FOM velocity-stress leapfrog for sm_103a.
+//
+// The reference assembles two CRS Jacobians (src/kokkos/shwavepp.hpp:319-466) and
+// advances with two Kokkos-Kernels SpMV/SpMM calls per step
+// (src/kokkos/fom_update_kernels.hpp:60-181).  Here the sparsity is implicit: the
+// library checks once that the mesh is the mesher's structured full grid and then
+// computes neighbour gids from (j, i).  Only the stencil values are stored, one
+// coefficient array per neighbour slot (SoA), with dt folded in:
+//   vp point p:  v[p] = v[p] + cN*s[N] + cS*s[S] + cW*s[W] + cE*s[E]  (+ forcing)
+//   sp point q:  s[q] = s[q] + cA*v[A] + cB*v[B]
+// which is the reference's y + dt*(J x) re-associated to four (two) FMAs per
+// entry: on GB300 the FP64 pipe, not HBM, is the tighter roof for this update.
+//
+// State layout in HBM: row-major [gid][M] (M = number of forcings, m fastest),
+// i.e. gid order of the reference, so snapshots need no permutation.  Each thread
+// owns VEC consecutive columns of one point (16-byte vector loads when M is even).
+// Source injection (RankOneForcing / AddForcingRank2) is fused into the velocity
+// kernel: the one thread that owns (src_gid[m], m) evaluates the signal on device.
+// The seismogram receiver gather is fused into the stress launch as extra blocks
+// (they read the velocity of the same step, which that launch does not modify).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "shaw_internal.h"
+
+namespace shaw {
+
+namespace {
+thread_local std::string t_err;
+}
+
+void set_error(const std::string& msg) { t_err = msg; }
+int fail(int code, const std::string& msg) {
+  t_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  t_err = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? SHAW_ERR_OUT_OF_MEMORY : SHAW_ERR_CUDA;
+}
+
+}  // namespace shaw
+
+extern "C" const char* shaw_last_error(void) { return shaw::t_err.c_str(); }
+extern "C" const char* shaw_version(void) { return "shaw_gb300 0.1 (sm_103a)"; }
+
+using shaw::FastDiv;
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kGraphChunk = 64;  // leapfrog steps per captured CUDA graph
+
+struct FomCtl {
+  unsigned long long step_base;  // steps completed before the current chunk
+  unsigned int nonfinite;        // set when a gathered receiver value is NaN/Inf
+  unsigned int pad;
+};
+
+// Arguments shared by both half-step kernels (passed by value, < 4 KB).
+struct FomArgs {
+  double* xv;          // [nvp][M]
+  double* xs;          // [nsp][M]
+  const double* cvp;   // 4 planes of nvp: N, S, W, E (dt folded)
+  const double* csp;   // 2 planes of nsp: A, B (dt folded)
+  const double* rho_inv;
+  const unsigned long long* src;  // [M] source vp gid per column
+  const int* kind;
+  const double* period;
+  const double* delay;
+  const unsigned long long* rcv;  // [R]
+  double* seis;                   // [R x T x M] LayoutLeft
+  FomCtl* ctl;
+  double dt;
+  uint32_t nth, nr, M, chunks;    // chunks = M / VEC
+  uint32_t vp_items, sp_items;    // nvp*chunks, nsp*chunks
+  uint32_t sp_row;                // 2*nth - 1
+  uint32_t R, seis_freq, seis_T;
+  uint32_t sp_blocks;             // blocks of the stress part of the stress launch
+  int rank2;
+  FastDiv chunks_div, nth_div, sprow_div;
+};
+
+template <int VEC>
+struct VecT;
+template <>
+struct VecT<1> {
+  using type = double;
+  __device__ static double ld(const double* p) { return *p; }
+  __device__ static void st(double* p, double v) { *p = v; }
+};
+template <>
+struct VecT<2> {
+  using type = double2;
+  __device__ static double2 ld(const double* p) { return *reinterpret_cast<const double2*>(p); }
+  __device__ static void st(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
+};
+
+__device__ __forceinline__ void fma_into(double& acc, double c, double x) { acc = fma(c, x, acc); }
+__device__ __forceinline__ void fma_into(double2& acc, double c, double2 x) {
+  acc.x = fma(c, x.x, acc.x);
+  acc.y = fma(c, x.y, acc.y);
+}
+__device__ __forceinline__ double& lane(double& v, int) { return v; }
+__device__ __forceinline__ double& lane(double2& v, int e) { return e == 0 ? v.x : v.y; }
+
+// sp gid of the stp point of cell (j, i): interleaved numbering of the mesher.
+__device__ __forceinline__ uint32_t stp_gid(uint32_t j, uint32_t i, const FomArgs& a) {
+  return (j + 1 < a.nr) ? j * a.sp_row + 2 * i + 1 : j * a.sp_row + i;
+}
+
+// updateVelocity (fom_update_kernels.hpp:60-90 rank-1, :132-167 rank-2) for one step.
+template <int VEC>
+__global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint32_t k_local,
+                                                                unsigned long long host_step) {
+  using V = VecT<VEC>;
+  const uint32_t item = blockIdx.x * kThreads + threadIdx.x;
+  if (item >= a.vp_items) return;
+  const uint32_t p = shaw::fast_div(item, a.chunks_div);
+  const uint32_t c = item - p * a.chunks;
+  const uint32_t j = shaw::fast_div(p, a.nth_div);
+  const uint32_t i = p - j * a.nth;
+  double* xp = a.xv + (size_t)p * a.M + c * VEC;
+  typename V::type v = V::ld(xp);
+  if (i != 0 && i + 1 != a.nth) {
+    // interior theta: N/S are srp points, W/E stp points.  At the CMB (j == 0)
+    // and the surface (j == nr-1) N and S are the same srp (merged coefficient in cN).
+    const uint32_t rowN = (j + 1 < a.nr) ? j : j - 1;
+    const uint32_t rowS = (j > 0) ? j - 1 : 0;
+    const uint32_t gN = rowN * a.sp_row + 2 * i;
+    const uint32_t gS = rowS * a.sp_row + 2 * i;
+    const uint32_t gW = stp_gid(j, i - 1, a);
+    const uint32_t gE = stp_gid(j, i, a);
+    const size_t nvp = (size_t)a.nth * a.nr;
+    const double cN = __ldg(a.cvp + p);
+    const double cS = __ldg(a.cvp + nvp + p);
+    const double cW = __ldg(a.cvp + 2 * nvp + p);
+    const double cE = __ldg(a.cvp + 3 * nvp + p);
+    const size_t off = (size_t)c * VEC;
+    fma_into(v, cN, V::ld(a.xs + (size_t)gN * a.M + off));
+    fma_into(v, cS, V::ld(a.xs + (size_t)gS * a.M + off));
+    fma_into(v, cW, V::ld(a.xs + (size_t)gW * a.M + off));
+    fma_into(v, cE, V::ld(a.xs + (size_t)gE * a.M + off));
+  }
+  // forcing: the thread owning (src[m], m) adds it, evaluating the signal at t_{n-1}
+  const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
+#pragma unroll
+  for (int e = 0; e < VEC; ++e) {
+    const uint32_t m = c * VEC + e;
+    if (a.src[m] == p) {
+      const double t = (double)(n - 1) * a.dt;
+      const double f = shaw::signal_value(a.kind[m], a.delay[m], a.period[m], t);
+      const double ri = a.rho_inv[p];
+      double& x = lane(v, e);
+      // explicit roundings: no FMA contraction, as the reference's host kernels
+      if (a.rank2)
+        x = __dadd_rn(x, __dmul_rn(__dmul_rn(ri, f), a.dt));  // AddForcingRank2: x += rhoInv*f*dt
+      else
+        x = __dadd_rn(x, __dmul_rn(__dmul_rn(a.dt, ri), f));  // KokkosBlas::mult(1, x, dt, rhoInv, f)
+    }
+  }
+  V::st(xp, v);
+}
+
+// updateStress (fom_update_kernels.hpp:93-104, :170-181) + fused receiver gather.
+template <int VEC>
+__global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_t k_local,
+                                                              unsigned long long host_step) {
+  using V = VecT<VEC>;
+  if (blockIdx.x >= a.sp_blocks) {
+    // Seismogram::storeVelocitySignalAtReceivers (seismogram.hpp:193-214)
+    const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
+    if (a.seis_freq == 0 || n % a.seis_freq != 0) return;
+    const uint32_t idx = (blockIdx.x - a.sp_blocks) * kThreads + threadIdx.x;
+    if (idx >= a.R * a.M) return;
+    const uint32_t r = idx % a.R, m = idx / a.R;
+    const unsigned long long cnt = n / a.seis_freq - 1;
+    const double val = a.xv[(size_t)a.rcv[r] * a.M + m];
+    a.seis[r + (size_t)a.R * (cnt + (size_t)a.seis_T * m)] = val;
+    if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
+    return;
+  }
+  const uint32_t item = blockIdx.x * kThreads + threadIdx.x;
+  if (item >= a.sp_items) return;
+  const uint32_t q = shaw::fast_div(item, a.chunks_div);
+  const uint32_t c = item - q * a.chunks;
+  const uint32_t j = shaw::fast_div(q, a.sprow_div);
+  const uint32_t rem = q - j * a.sp_row;
+  uint32_t gA, gB;
+  if (j + 1 < a.nr && (rem & 1u) == 0) {
+    // srp of cell (j, i): north vp (j+1, i), south vp (j, i)
+    const uint32_t i = rem >> 1;
+    gA = (j + 1) * a.nth + i;
+    gB = j * a.nth + i;
+  } else {
+    // stp of cell (j, i): west vp (j, i), east vp (j, i+1)
+    const uint32_t i = (j + 1 < a.nr) ? (rem >> 1) : rem;
+    gA = j * a.nth + i;
+    gB = gA + 1;
+  }
+  const size_t nsp = (size_t)(a.nr - 1) * a.nth + (size_t)a.nr * (a.nth - 1);
+  const double cA = __ldg(a.csp + q);
+  const double cB = __ldg(a.csp + nsp + q);
+  double* sp = a.xs + (size_t)q * a.M + c * VEC;
+  typename V::type s = V::ld(sp);
+  const size_t off = (size_t)c * VEC;
+  fma_into(s, cA, V::ld(a.xv + (size_t)gA * a.M + off));
+  fma_into(s, cB, V::ld(a.xv + (size_t)gB * a.M + off));
+  V::st(sp, s);
+}
+
+__global__ void fom_fold_kernel(const double* raw, double* folded, double dt, size_t n) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
+    folded[k] = dt * raw[k];
+}
+
+__global__ void fom_advance_base_kernel(FomCtl* ctl, unsigned int by) { ctl->step_base += by; }
+__global__ void fom_set_base_kernel(FomCtl* ctl, unsigned long long v) { ctl->step_base = v; }
+
+// [N][M] -> [M][N] for the LayoutLeft snapshot copy.
+__global__ void fom_transpose_kernel(const double* in, double* out, uint32_t N, uint32_t M) {
+  __shared__ double tile[32][33];
+  const uint32_t n0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
+  for (uint32_t r = threadIdx.y; r < 32; r += 8) {
+    const uint32_t n = n0 + r, m = m0 + threadIdx.x;
+    if (n < N && m < M) tile[r][threadIdx.x] = in[(size_t)n * M + m];
+  }
+  __syncthreads();
+  for (uint32_t r = threadIdx.y; r < 32; r += 8) {
+    const uint32_t m = m0 + r, n = n0 + threadIdx.x;
+    if (n < N && m < M) out[(size_t)m * N + n] = tile[threadIdx.x][r];
+  }
+}
+
+}  // namespace
+
+struct shaw_fom_s {
+  uint64_t nth = 0, nr = 0, nvp = 0, nsp = 0;
+  uint32_t M = 1;
+  int rank = 1;
+  int precision = SHAW_FP64;
+  cudaStream_t stream = nullptr;
+  // device buffers
+  double* xv = nullptr;
+  double* xs = nullptr;
+  double* cvp_raw = nullptr;
+  double* csp_raw = nullptr;
+  double* cvp = nullptr;
+  double* csp = nullptr;
+  double* rho_inv = nullptr;
+  unsigned long long* src = nullptr;
+  int* kind = nullptr;
+  double* period = nullptr;
+  double* delay = nullptr;
+  unsigned long long* rcv = nullptr;
+  double* seis = nullptr;
+  double* staging = nullptr;
+  FomCtl* ctl = nullptr;
+  bool sources_set = false;
+  // receivers / snapshots
+  uint32_t R = 0;
+  uint64_t seis_freq = 0, seis_T = 0, seis_nsteps = 0;
+  uint64_t snap_fvp = 0, snap_fsp = 0, snap_nsteps = 0, snap_cvp = 0, snap_csp = 0;
+  double* host_vp = nullptr;
+  double* host_sp = nullptr;
+  // run state
+  double folded_dt = std::nan("");
+  uint64_t step = 0;  // completed steps since reset
+  uint64_t launches = 0;
+  // graph cache
+  cudaGraphExec_t graph = nullptr;
+  double graph_dt = std::nan("");
+};
+
+namespace {
+
+using H = shaw_fom_s;
+
+FomArgs make_args(const H* h, double dt) {
+  FomArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.xv = h->xv;
+  a.xs = h->xs;
+  a.cvp = h->cvp;
+  a.csp = h->csp;
+  a.rho_inv = h->rho_inv;
+  a.src = h->src;
+  a.kind = h->kind;
+  a.period = h->period;
+  a.delay = h->delay;
+  a.rcv = h->rcv;
+  a.seis = h->seis;
+  a.ctl = h->ctl;
+  a.dt = dt;
+  a.nth = (uint32_t)h->nth;
+  a.nr = (uint32_t)h->nr;
+  a.M = h->M;
+  const int vec = (h->M % 2 == 0) ? 2 : 1;
+  a.chunks = h->M / vec;
+  a.vp_items = (uint32_t)(h->nvp * a.chunks);
+  a.sp_items = (uint32_t)(h->nsp * a.chunks);
+  a.sp_row = (uint32_t)(2 * h->nth - 1);
+  a.R = h->R;
+  a.seis_freq = (uint32_t)h->seis_freq;
+  a.seis_T = (uint32_t)h->seis_T;
+  a.sp_blocks = (a.sp_items + kThreads - 1) / kThreads;
+  a.rank2 = h->rank == 2 ? 1 : 0;
+  a.chunks_div = shaw::make_fastdiv(a.chunks);
+  a.nth_div = shaw::make_fastdiv(a.nth);
+  a.sprow_div = shaw::make_fastdiv(a.sp_row);
+  return a;
+}
+
+int launch_velocity(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
+  const uint32_t blocks = (a.vp_items + kThreads - 1) / kThreads;
+  if (a.chunks * 2 == h->M)
+    fom_velocity_kernel<2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  else
+    fom_velocity_kernel<1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  return SHAW_OK;
+}
+
+int launch_stress(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
+  uint32_t blocks = a.sp_blocks;
+  if (a.R && a.seis_freq) blocks += (a.R * a.M + kThreads - 1) / kThreads;
+  if (a.chunks * 2 == h->M)
+    fom_stress_kernel<2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  else
+    fom_stress_kernel<1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  return SHAW_OK;
+}
+
+int ensure_folded(H* h, double dt) {
+  if (h->folded_dt == dt) return SHAW_OK;
+  fom_fold_kernel<<<1024, 256, 0, h->stream>>>(h->cvp_raw, h->cvp, dt, 4 * h->nvp);
+  fom_fold_kernel<<<1024, 256, 0, h->stream>>>(h->csp_raw, h->csp, dt, 2 * h->nsp);
+  h->launches += 2;
+  SHAW_CUDA(cudaGetLastError());
+  h->folded_dt = dt;
+  return SHAW_OK;
+}
+
+// Copy the current vp (dof 0) or sp (dof 1) state into column `col` of the host snapshot matrix.
+int snapshot_copy(H* h, int dof, uint64_t col) {
+  const uint64_t N = dof == 0 ? h->nvp : h->nsp;
+  const uint64_t T = h->snap_nsteps / (dof == 0 ? h->snap_fvp : h->snap_fsp);
+  double* host = dof == 0 ? h->host_vp : h->host_sp;
+  const double* dev = dof == 0 ? h->xv : h->xs;
+  if (h->M == 1) {
+    SHAW_CUDA(cudaMemcpyAsync(host + N * col, dev, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return SHAW_OK;
+  }
+  dim3 grid((unsigned)((N + 31) / 32), (h->M + 31) / 32);
+  fom_transpose_kernel<<<grid, dim3(32, 8), 0, h->stream>>>(dev, h->staging, (uint32_t)N, h->M);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  SHAW_CUDA(cudaMemcpy2DAsync(host + N * col, N * T * sizeof(double), h->staging, N * sizeof(double),
+                              N * sizeof(double), h->M, cudaMemcpyDeviceToHost, h->stream));
+  return SHAW_OK;
+}
+
+int check_ready(H* h, double dt) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
+  if (!h->sources_set) return shaw::fail(SHAW_ERR_STATE, "shaw_fom_set_sources must be called before stepping");
+  return SHAW_OK;
+}
+
+// Build (once per dt) a graph of kGraphChunk steps that reads its step numbers
+// from the device-side step_base and advances it at the end.
+int ensure_graph(H* h, double dt) {
+  if (h->graph && h->graph_dt == dt) return SHAW_OK;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  const FomArgs a = make_args(h, dt);
+  cudaGraph_t g = nullptr;
+  SHAW_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const uint64_t before = h->launches;
+  int rc = SHAW_OK;
+  for (uint32_t k = 0; k < kGraphChunk && rc == SHAW_OK; ++k) {
+    rc = launch_velocity(h, a, k, 0);
+    if (rc == SHAW_OK) rc = launch_stress(h, a, k, 0);
+  }
+  if (rc == SHAW_OK) {
+    fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, kGraphChunk);
+  }
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  h->launches = before;  // captured launches are counted when the graph is replayed
+  if (rc != SHAW_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGraphInstantiate");
+  h->graph_dt = dt;
+  return SHAW_OK;
+}
+
+int set_step_base(H* h) {
+  fom_set_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, (unsigned long long)h->step);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  return SHAW_OK;
+}
+
+bool valid_structured_mesh(const shaw_fom_operator_desc* d, std::string& why) {
+  const uint64_t nth = d->nth, nr = d->nr;
+  if (nth < 2 || nr < 2) { why = "nth and nr must be >= 2"; return false; }
+  if (d->nvp != nth * nr) { why = "numPtsVp != nth*nr"; return false; }
+  if (d->nsp != (nr - 1) * nth + nr * (nth - 1)) { why = "numPtsSp != (nr-1)*nth + nr*(nth-1)"; return false; }
+  if (d->nvp * 4 >= (1ull << 32) || d->nsp * 2 >= (1ull << 32)) { why = "mesh too large for 32-bit indexing"; return false; }
+  const uint64_t row = 2 * nth - 1;
+  auto srp = [&](uint64_t j, uint64_t i) { return j * row + 2 * i; };
+  auto stp = [&](uint64_t j, uint64_t i) { return (j + 1 < nr) ? j * row + 2 * i + 1 : j * row + i; };
+  for (uint64_t p = 0; p < d->nvp; ++p) {
+    const uint64_t j = p / nth, i = p % nth;
+    const int64_t* g = d->graph_vp + p * 5;
+    const int64_t eW = (i >= 1) ? (int64_t)stp(j, i - 1) : (int64_t)stp(j, i);
+    const int64_t eE = (i + 1 < nth) ? (int64_t)stp(j, i) : (int64_t)stp(j, i - 1);
+    const int64_t eN = (j + 1 < nr) ? (int64_t)srp(j, i) : (int64_t)srp(j - 1, i);
+    const int64_t eS = (j >= 1) ? (int64_t)srp(j - 1, i) : (int64_t)srp(j, i);
+    if (g[0] != (int64_t)p || g[1] != eW || g[2] != eN || g[3] != eE || g[4] != eS) {
+      why = "graph_vp row " + std::to_string(p) + " does not match the structured full mesh";
+      return false;
+    }
+  }
+  for (uint64_t q = 0; q < d->nsp; ++q) {
+    const uint64_t j = q / row, rem = q % row;
+    const int64_t* g = d->graph_sp + q * 3;
+    int64_t eA, eB;
+    int lab;
+    if (j + 1 < nr && rem % 2 == 0) {
+      const uint64_t i = rem / 2;
+      lab = 1; eA = (int64_t)((j + 1) * nth + i); eB = (int64_t)(j * nth + i);
+    } else {
+      const uint64_t i = (j + 1 < nr) ? rem / 2 : rem;
+      lab = 2; eA = (int64_t)(j * nth + i); eB = eA + 1;
+    }
+    if (g[0] != (int64_t)q || g[1] != eA || g[2] != eB || d->labels_sp[q] != lab) {
+      why = "graph_sp row " + std::to_string(q) + " does not match the structured full mesh";
+      return false;
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int precision, shaw_fom_t* out) {
+  if (!d || !out) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (M == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "num_forcings must be >= 1");
+  if (rank != 1 && rank != 2) return shaw::fail(SHAW_ERR_INVALID_ARG, "rank must be 1 or 2");
+  if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
+  if (precision != SHAW_FP64) return shaw::fail(SHAW_ERR_UNSUPPORTED, "FOM precision must be SHAW_FP64");
+  if (!d->graph_vp || !d->graph_sp || !d->labels_sp || !d->coords_vp || !d->coords_sp || !d->cot_vp ||
+      !d->cot_sp || !d->coeff_vp || !d->rho_inv_vp || !d->shear_mod_sp)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "operator descriptor has a null array");
+  std::string why;
+  if (!valid_structured_mesh(d, why)) return shaw::fail(SHAW_ERR_MESH, why);
+  if ((uint64_t)d->nsp * M >= (1ull << 32) || (uint64_t)d->nvp * M >= (1ull << 32))
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "mesh points x forcings must stay below 2^32");
+
+  // Stencil values in the reference's expression order (shwavepp.hpp:361-364, 441-454).
+  const uint64_t nvp = d->nvp, nsp = d->nsp;
+  std::vector<double> cv(4 * nvp, 0.0), cs(2 * nsp, 0.0);
+  const double three = 3.0, oneHalf = 1.0 / 2.0;
+  for (uint64_t p = 0; p < nvp; ++p) {
+    const int64_t* g = d->graph_vp + p * 5;
+    const double rInv = d->coords_vp[p * 2 + 1];
+    const double cot = d->cot_vp[p];
+    const double rhoInv = d->rho_inv_vp[p];
+    const double* c = d->coeff_vp + p * 4;
+    const double cW = (-rInv * d->dth_inv + rInv * cot) * c[0] * rhoInv;
+    const double cN = (d->drr_inv + three * oneHalf * rInv) * c[1] * rhoInv;
+    const double cE = (rInv * d->dth_inv + rInv * cot) * c[2] * rhoInv;
+    const double cS = (-d->drr_inv + three * oneHalf * rInv) * c[3] * rhoInv;
+    if (g[2] == g[4]) { cv[p] = cN + cS; cv[nvp + p] = 0.0; }
+    else { cv[p] = cN; cv[nvp + p] = cS; }
+    if (g[1] == g[3]) { cv[2 * nvp + p] = cW + cE; cv[3 * nvp + p] = 0.0; }
+    else { cv[2 * nvp + p] = cW; cv[3 * nvp + p] = cE; }
+  }
+  for (uint64_t q = 0; q < nsp; ++q) {
+    const double rInv = d->coords_sp[q * 2 + 1];
+    const double G = d->shear_mod_sp[q];
+    if (d->labels_sp[q] == 1) {
+      cs[q] = (d->drr_inv - rInv * oneHalf) * G;
+      cs[nsp + q] = (-d->drr_inv - rInv * oneHalf) * G;
+    } else {
+      cs[q] = (-d->dth_inv - oneHalf * d->cot_sp[q]) * rInv * G;
+      cs[nsp + q] = (d->dth_inv - oneHalf * d->cot_sp[q]) * rInv * G;
+    }
+  }
+
+  H* h = new H();
+  h->nth = d->nth; h->nr = d->nr; h->nvp = nvp; h->nsp = nsp; h->M = M; h->rank = rank;
+  h->precision = precision;
+  auto bail = [&](int rc) { shaw_fom_destroy(h); return rc; };
+  cudaError_t e;
+#define SHAW_TRY(call) do { e = (call); if (e != cudaSuccess) return bail(shaw::cuda_fail(e, #call)); } while (0)
+  SHAW_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  SHAW_TRY(cudaMalloc(&h->xv, nvp * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->xs, nsp * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->cvp_raw, 4 * nvp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->csp_raw, 2 * nsp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->cvp, 4 * nvp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->csp, 2 * nsp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->rho_inv, nvp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->src, M * sizeof(unsigned long long)));
+  SHAW_TRY(cudaMalloc(&h->kind, M * sizeof(int)));
+  SHAW_TRY(cudaMalloc(&h->period, M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->delay, M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->ctl, sizeof(FomCtl)));
+  SHAW_TRY(cudaMemcpyAsync(h->cvp_raw, cv.data(), cv.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->csp_raw, cs.data(), cs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->rho_inv, d->rho_inv_vp, nvp * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xv, 0, nvp * M * sizeof(double), h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xs, 0, nsp * M * sizeof(double), h->stream));
+  SHAW_TRY(cudaStreamSynchronize(h->stream));
+#undef SHAW_TRY
+  *out = h;
+  return SHAW_OK;
+}
+
+void shaw_fom_destroy(shaw_fom_t h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->host_vp) cudaHostUnregister(h->host_vp);
+  if (h->host_sp) cudaHostUnregister(h->host_sp);
+  void* bufs[] = {h->xv, h->xs, h->cvp_raw, h->csp_raw, h->cvp, h->csp, h->rho_inv, h->src, h->kind,
+                  h->period, h->delay, h->rcv, h->seis, h->staging, h->ctl};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int shaw_fom_set_sources(shaw_fom_t h, const uint64_t* gid, const int32_t* kind, const double* period,
+                         const double* delay) {
+  if (!h || !gid || !kind || !period || !delay) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  for (uint32_t m = 0; m < h->M; ++m) {
+    if (gid[m] >= h->nvp) return shaw::fail(SHAW_ERR_INVALID_ARG, "source gid out of range");
+    if (kind[m] < SHAW_SIGNAL_RICKER || kind[m] > SHAW_SIGNAL_GAUSS_DER)
+      return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown signal kind");
+    if (!(period[m] > 0.0)) return shaw::fail(SHAW_ERR_INVALID_ARG, "Period for signal must be positive.");
+    if (!(delay[m] >= 0.0)) return shaw::fail(SHAW_ERR_INVALID_ARG, "Delay time of the signal must be >=0");
+  }
+  static_assert(sizeof(unsigned long long) == sizeof(uint64_t), "gid width");
+  SHAW_CUDA(cudaMemcpyAsync(h->src, gid, h->M * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemcpyAsync(h->kind, kind, h->M * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemcpyAsync(h->period, period, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemcpyAsync(h->delay, delay, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->sources_set = true;
+  return SHAW_OK;
+}
+
+int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* gid, uint32_t R, uint64_t freq, uint64_t nsteps) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->rcv) { cudaFree(h->rcv); h->rcv = nullptr; }
+  if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
+  h->R = 0; h->seis_freq = 0; h->seis_T = 0; h->seis_nsteps = 0;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (R == 0) return SHAW_OK;
+  if (!gid) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver gids");
+  if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
+  if (nsteps % freq != 0)
+    return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Seismogram sampling frequency not a divisor of steps");
+  for (uint32_t r = 0; r < R; ++r)
+    if (gid[r] >= h->nvp) return shaw::fail(SHAW_ERR_INVALID_ARG, "receiver gid out of range");
+  const uint64_t T = nsteps / freq;
+  if ((uint64_t)R * h->M >= (1ull << 31) || T >= (1ull << 32))
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "seismogram too large");
+  SHAW_CUDA(cudaMalloc(&h->rcv, R * sizeof(unsigned long long)));
+  SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
+  SHAW_CUDA(cudaMemcpyAsync(h->rcv, gid, R * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->R = R; h->seis_freq = freq; h->seis_T = T; h->seis_nsteps = nsteps;
+  return SHAW_OK;
+}
+
+int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t fvp, uint64_t fsp, uint64_t nsteps, double* host_vp,
+                           double* host_sp) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->host_vp) cudaHostUnregister(h->host_vp);
+  if (h->host_sp) cudaHostUnregister(h->host_sp);
+  h->host_vp = h->host_sp = nullptr;
+  h->snap_fvp = h->snap_fsp = h->snap_nsteps = 0;
+  if (fvp == 0 && fsp == 0) return SHAW_OK;
+  if (fvp == 0 || fsp == 0 || !host_vp || !host_sp)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "snapshot frequencies and arrays are required for both dofs");
+  if (nsteps % fvp != 0) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Snapshot Vp frequency not a divisor of steps");
+  if (nsteps % fsp != 0) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Snapshot Sp frequency not a divisor of steps");
+  const size_t bvp = h->nvp * (nsteps / fvp) * h->M * sizeof(double);
+  const size_t bsp = h->nsp * (nsteps / fsp) * h->M * sizeof(double);
+  SHAW_CUDA(cudaHostRegister(host_vp, bvp, cudaHostRegisterDefault));
+  cudaError_t e = cudaHostRegister(host_sp, bsp, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    cudaHostUnregister(host_vp);
+    return shaw::cuda_fail(e, "cudaHostRegister(host_sp)");
+  }
+  if (h->M > 1 && !h->staging) {
+    e = cudaMalloc(&h->staging, std::max(h->nvp, h->nsp) * h->M * sizeof(double));
+    if (e != cudaSuccess) {
+      cudaHostUnregister(host_vp);
+      cudaHostUnregister(host_sp);
+      return shaw::cuda_fail(e, "cudaMalloc(staging)");
+    }
+  }
+  h->host_vp = host_vp; h->host_sp = host_sp;
+  h->snap_fvp = fvp; h->snap_fsp = fsp; h->snap_nsteps = nsteps;
+  return SHAW_OK;
+}
+
+int shaw_fom_reset(shaw_fom_t h) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->nvp * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->nsp * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
+  if (h->seis)
+    SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
+  h->step = 0;
+  h->snap_cvp = h->snap_csp = 0;
+  return SHAW_OK;
+}
+
+int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
+  int rc = check_ready(h, dt);
+  if (rc) return rc;
+  if (h->seis_freq && h->step + nsteps > h->seis_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the seismogram was sized for");
+  if (h->snap_fvp && h->step + nsteps > h->snap_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
+  if ((rc = ensure_folded(h, dt))) return rc;
+  const bool snaps = h->snap_fvp != 0;
+  uint64_t done = 0;
+  if (!snaps && nsteps >= kGraphChunk) {
+    // Graph replay: the graph reads its step numbers from ctl->step_base.
+    if ((rc = ensure_graph(h, dt))) return rc;
+    if ((rc = set_step_base(h))) return rc;
+    const uint64_t per = 2 * kGraphChunk + 1;
+    while (nsteps - done >= kGraphChunk) {
+      SHAW_CUDA(cudaGraphLaunch(h->graph, h->stream));
+      h->launches += per;
+      done += kGraphChunk;
+      h->step += kGraphChunk;
+    }
+  }
+  const FomArgs a = make_args(h, dt);
+  for (; done < nsteps; ++done) {
+    const unsigned long long n = h->step + 1;
+    if ((rc = launch_velocity(h, a, 0, n))) return rc;
+    if (snaps && n % h->snap_fvp == 0) {
+      if ((rc = snapshot_copy(h, 0, h->snap_cvp))) return rc;
+      h->snap_cvp++;
+    }
+    if ((rc = launch_stress(h, a, 0, n))) return rc;
+    if (snaps && n % h->snap_fsp == 0) {
+      if ((rc = snapshot_copy(h, 1, h->snap_csp))) return rc;
+      h->snap_csp++;
+    }
+    h->step++;
+  }
+  return SHAW_OK;
+}
+
+int shaw_fom_synchronize(shaw_fom_t h) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  FomCtl c;
+  SHAW_CUDA(cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c.nonfinite) return shaw::fail(SHAW_ERR_NONFINITE, "NaN/Inf in a sampled velocity (seismogram)");
+  return SHAW_OK;
+}
+
+int shaw_fom_run(shaw_fom_t h, double dt, uint64_t nsteps) {
+  int rc = check_ready(h, dt);
+  if (rc) return rc;
+  if (h->seis_freq && nsteps != h->seis_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "nsteps differs from the seismogram's step count");
+  if (h->snap_fvp && nsteps != h->snap_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "nsteps differs from the snapshots' step count");
+  if ((rc = shaw_fom_reset(h))) return rc;
+  if ((rc = shaw_fom_advance(h, dt, nsteps))) return rc;
+  return shaw_fom_synchronize(h);
+}
+
+int shaw_fom_update_velocity(shaw_fom_t h, double dt, uint64_t step) {
+  int rc = check_ready(h, dt);
+  if (rc) return rc;
+  if (step == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "steps are 1-based");
+  if ((rc = ensure_folded(h, dt))) return rc;
+  const FomArgs a = make_args(h, dt);
+  return launch_velocity(h, a, 0, step);
+}
+
+int shaw_fom_update_stress(shaw_fom_t h, double dt) {
+  int rc = check_ready(h, dt);
+  if (rc) return rc;
+  if ((rc = ensure_folded(h, dt))) return rc;
+  FomArgs a = make_args(h, dt);
+  a.seis_freq = 0;  // a bare half-step records no seismogram
+  return launch_stress(h, a, 0, 1);
+}
+
+int shaw_fom_get_seismogram(shaw_fom_t h, double* out) {
+  if (!h || !out) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (!h->seis) return shaw::fail(SHAW_ERR_STATE, "no receivers set");
+  SHAW_CUDA(cudaMemcpyAsync(out, h->seis, (size_t)h->R * h->seis_T * h->M * sizeof(double),
+                            cudaMemcpyDeviceToHost, h->stream));
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  return SHAW_OK;
+}
+
+static int copy_state(shaw_fom_t h, double* host, const double* chost, uint64_t N, double* dev, bool to_host) {
+  if (h->M == 1) {
+    if (to_host) SHAW_CUDA(cudaMemcpyAsync(host, dev, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    else SHAW_CUDA(cudaMemcpyAsync(dev, chost, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+    return SHAW_OK;
+  }
+  // host LayoutLeft [N x M] <-> device row-major [N][M]: transpose on the host side
+  std::vector<double> tmp(N * h->M);
+  if (to_host) {
+    SHAW_CUDA(cudaMemcpyAsync(tmp.data(), dev, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+    for (uint64_t n = 0; n < N; ++n)
+      for (uint32_t m = 0; m < h->M; ++m) host[n + N * m] = tmp[n * h->M + m];
+  } else {
+    for (uint64_t n = 0; n < N; ++n)
+      for (uint32_t m = 0; m < h->M; ++m) tmp[n * h->M + m] = chost[n + N * m];
+    SHAW_CUDA(cudaMemcpyAsync(dev, tmp.data(), tmp.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return SHAW_OK;
+}
+
+int shaw_fom_get_state(shaw_fom_t h, double* vp, double* sp) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  int rc = SHAW_OK;
+  if (vp && (rc = copy_state(h, vp, nullptr, h->nvp, h->xv, true))) return rc;
+  if (sp && (rc = copy_state(h, sp, nullptr, h->nsp, h->xs, true))) return rc;
+  return SHAW_OK;
+}
+
+int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  int rc = SHAW_OK;
+  if (vp && (rc = copy_state(h, nullptr, vp, h->nvp, h->xv, false))) return rc;
+  if (sp && (rc = copy_state(h, nullptr, sp, h->nsp, h->xs, false))) return rc;
+  return SHAW_OK;
+}
+
+void* shaw_fom_stream(shaw_fom_t h) { return h ? (void*)h->stream : nullptr; }
+uint64_t shaw_fom_kernel_launches(shaw_fom_t h) { return h ? h->launches : 0; }
+
+}  // extern "C"
