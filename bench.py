@@ -42,6 +42,9 @@ def parse():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    # smaller cases for profiling captures (the default is the benchmark workload)
+    p.add_argument("--forcings", type=int, default=M)
+    p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
 
@@ -112,6 +115,29 @@ class ClockSampler:
         sm.sort()
         med = sm[len(sm) // 2] if sm else None
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# DRAM bytes (read + write) of one fom_stress_kernel launch per forcing column, from the
+# ncu capture summarised in profiles/fom_kernels_rank2_1000x2000.md (M = 16, scaled by M).
+TRAFFIC_STRESS_PER_FORCING = (831.617024e6 + 461.196032e6) / 16
+
+
+def dgemm_tflops(torch):
+    """FP64 peak proxy: cuBLAS DGEMM 8192^3, best of 3 (CUDA events)."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * 8192 ** 3 / (best / 1e3) / 1e12
 
 
 def measured_peaks():
@@ -285,6 +311,7 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     hbm, peak_kind = measured_peaks()
+    fp64_peak = dgemm_tflops(torch)
     # dominant kernel: the stress half-step (nsp ~ 2 nvp).  Algorithmic bytes per launch:
     # read + write every sp value, read every vp value once: (2*nsp + nvp) * M * 8.
     bytes_s = (2 * mesh.nsp + mesh.nvp) * M * 8
@@ -299,17 +326,22 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (state 12.3 GB per GPU), no flush needed",
                    "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": "fom_stress_kernel", "achieved": ach, "peak": hbm,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": TRAFFIC_STRESS_PER_FORCING * M,
                      "algorithmic_bytes_per_launch": bytes_s, "launch_ms": t_s * 1e3,
                      "velocity_kernel": {"launch_ms": t_v * 1e3, "achieved": bytes_v / t_v / 1e9,
                                          "frac": bytes_v / t_v / 1e9 / hbm},
+                     # GB300's FP64 rate is the tighter roof: 2 FMAs per sp update, 4 per interior vp update
+                     "fp64": {"achieved_tflops": 4.0 * mesh.nsp * M / t_s / 1e12,
+                              "peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM 8192^3)",
+                              "frac": 4.0 * mesh.nsp * M / t_s / 1e12 / fp64_peak},
                      "fp64_flops_per_step": (8 * (mesh.nvp - 2 * mesh.nr) + 4 * mesh.nsp) * M},
         "e2e": {"value": e2e_value, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if world == 1:
+    if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(np).items() if k in
                                 ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line), flush=True)
@@ -318,7 +350,11 @@ def run_ours(args):
 
 
 def main():
+    global M, WORKLOAD
     args = parse()
+    if args.forcings != M:
+        M = args.forcings
+        WORKLOAD = "FOM rank-2 FP64, 1000 theta x 2000 r grid, M=%d forcings" % M
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -146,6 +146,52 @@ void* shaw_fom_stream(shaw_fom_t h);
 uint64_t shaw_fom_kernel_launches(shaw_fom_t h);
 
 /* ======================================================================== *
+ *  ROM                                                                      *
+ * ======================================================================== */
+
+typedef struct shaw_rom_s* shaw_rom_t;
+
+/* computeRomOperatorsUsingFomJacsWithMatProp (rom_compute_jacobians.hpp:83-102)
+ * in FP64 on the GPU with the FOM handle's operators:
+ *   rom_jvp (kv x ks, row-major) = PhiVp^T (Jvp PhiSp)
+ *   rom_jsp (ks x kv, row-major) = PhiSp^T (Jsp PhiVp)
+ * phi_vp: nvp x kv, phi_sp: nsp x ks, both LayoutLeft (the lsv_* file layout). */
+int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const double* phi_sp, uint64_t ks,
+                     double* rom_jvp, double* rom_jsp);
+
+/* The reduced system of runRomRankOneForcing (rank 1, M == 1) and
+ * runRomRankTwoForcing (rank 2, M columns):
+ *   xv += dt Av xs ;  xv[:,j] += (f_j(t_{n-1}) dt) b[:,j] ;  xs += dt As xv
+ * rom_jvp kv x ks and rom_jsp ks x kv row-major; b kv x M LayoutLeft with
+ * b[:,j] = rhoInv[src_j] * PhiVp[src_j, :] (rom_problem_rank_one.hpp:137-147).
+ * precision: SHAW_FP64, or SHAW_MIXED_FP32 (rank 1: FP32 hi+lo operators and
+ * state, error-free products and compensated sums). */
+int shaw_rom_create(uint64_t kv, uint64_t ks, const double* rom_jvp, const double* rom_jsp, int rank,
+                    uint32_t num_forcings, const double* b, int precision, shaw_rom_t* out);
+void shaw_rom_destroy(shaw_rom_t h);
+/* Signal of each column (kind, period, delay); evaluated on the device. */
+int shaw_rom_set_signals(shaw_rom_t h, const int32_t* kind, const double* period, const double* delay);
+/* Reduced-state snapshots (the ROM's StateObserver): kv x (nsteps/freq_vp) x M and
+ * ks x (nsteps/freq_sp) x M, LayoutLeft, filled by shaw_rom_run / _synchronize. */
+int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t freq_vp, uint64_t freq_sp, uint64_t nsteps, double* host_vp,
+                           double* host_sp);
+/* In-loop ROM seismogram S(r, t, j) = PhiVp[gid_r, :] . xv(:, j) at every freq
+ * steps (reconstructSeismogram, main_reconstruct_seismo.cc:157-185); phi_rows is
+ * R x kv row-major (the basis rows of the receivers' vp gids). */
+int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t num_receivers, uint64_t freq,
+                           uint64_t nsteps);
+int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps);
+int shaw_rom_reset(shaw_rom_t h);
+int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps);
+int shaw_rom_synchronize(shaw_rom_t h);
+/* States out: xv kv x M, xs ks x M (LayoutLeft). */
+int shaw_rom_get_state(shaw_rom_t h, double* xv, double* xs);
+/* Seismogram out: R x (nsteps/freq) x M (LayoutLeft). */
+int shaw_rom_get_seismogram(shaw_rom_t h, double* out);
+void* shaw_rom_stream(shaw_rom_t h);
+uint64_t shaw_rom_kernel_launches(shaw_rom_t h);
+
+/* ======================================================================== *
  *  Host-side setup (the reference's main.cc + MeshInfo + material + mappers) *
  * ======================================================================== */
 

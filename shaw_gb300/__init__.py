@@ -88,6 +88,21 @@ SIGNATURES = [
     ("shaw_fom_set_state", ctypes.c_int, [_vp, _dp, _dp]),
     ("shaw_fom_stream", _vp, [_vp]),
     ("shaw_fom_kernel_launches", ctypes.c_uint64, [_vp]),
+    ("shaw_rom_project", ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _dp, ctypes.c_uint64, _dp, _dp]),
+    ("shaw_rom_create", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _dp, _dp, ctypes.c_int, ctypes.c_uint32,
+                                       _dp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("shaw_rom_destroy", None, [_vp]),
+    ("shaw_rom_set_signals", ctypes.c_int, [_vp, _i32p, _dp, _dp]),
+    ("shaw_rom_set_snapshots", ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _dp, _dp]),
+    ("shaw_rom_set_receivers", ctypes.c_int, [_vp, _dp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64]),
+    ("shaw_rom_run", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
+    ("shaw_rom_reset", ctypes.c_int, [_vp]),
+    ("shaw_rom_advance", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
+    ("shaw_rom_synchronize", ctypes.c_int, [_vp]),
+    ("shaw_rom_get_state", ctypes.c_int, [_vp, _dp, _dp]),
+    ("shaw_rom_get_seismogram", ctypes.c_int, [_vp, _dp]),
+    ("shaw_rom_stream", _vp, [_vp]),
+    ("shaw_rom_kernel_launches", ctypes.c_uint64, [_vp]),
     ("shaw_mesh_load", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_vp)]),
     ("shaw_mesh_generate", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)]),
@@ -315,6 +330,98 @@ class Fom:
     @property
     def kernel_launches(self):
         return lib().shaw_fom_kernel_launches(self.h)
+
+
+def rom_project(fom, phi_vp, phi_sp):
+    """(romJvp, romJsp) = (PhiVp^T Jvp PhiSp, PhiSp^T Jsp PhiVp), FP64 on the GPU."""
+    pv = np.asfortranarray(phi_vp, np.float64)
+    ps = np.asfortranarray(phi_sp, np.float64)
+    kv, ks = pv.shape[1], ps.shape[1]
+    av = np.zeros((kv, ks))
+    as_ = np.zeros((ks, kv))
+    _check(lib().shaw_rom_project(fom.h, _p(pv, _dp), kv, _p(ps, _dp), ks, _p(av, _dp), _p(as_, _dp)))
+    return av, as_
+
+
+class Rom:
+    """Reduced-order leapfrog on the GPU (rank 1 or 2)."""
+
+    def __init__(self, rom_jvp, rom_jsp, b, rank=1, precision=FP64):
+        av = np.ascontiguousarray(rom_jvp, np.float64)
+        as_ = np.ascontiguousarray(rom_jsp, np.float64)
+        b = np.asfortranarray(np.asarray(b, np.float64).reshape(av.shape[0], -1, order="F"))
+        self.kv, self.ks = av.shape
+        self.M = b.shape[1]
+        h = _vp()
+        _check(lib().shaw_rom_create(self.kv, self.ks, _p(av, _dp), _p(as_, _dp), rank, self.M, _p(b, _dp),
+                                     precision, ctypes.byref(h)))
+        self.h = h
+        self._snaps = None
+        self.R = self.T = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().shaw_rom_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_signals(self, kinds, periods, delays):
+        M = self.M
+        k = np.ascontiguousarray(np.broadcast_to(np.asarray([SIGNAL.get(x, x) for x in np.atleast_1d(kinds)],
+                                                            np.int32), (M,)))
+        p = np.ascontiguousarray(np.broadcast_to(np.asarray(periods, np.float64), (M,)))
+        d = np.ascontiguousarray(np.broadcast_to(np.asarray(delays, np.float64), (M,)))
+        _check(lib().shaw_rom_set_signals(self.h, _p(k, _i32p), _p(p, _dp), _p(d, _dp)))
+
+    def set_snapshots(self, freq_vp, freq_sp, nsteps):
+        if freq_vp == 0:
+            _check(lib().shaw_rom_set_snapshots(self.h, 0, 0, 0, None, None))
+            self._snaps = None
+            return
+        svp = np.zeros((self.kv, nsteps // freq_vp, self.M), order="F")
+        ssp = np.zeros((self.ks, nsteps // freq_sp, self.M), order="F")
+        _check(lib().shaw_rom_set_snapshots(self.h, freq_vp, freq_sp, nsteps, _p(svp, _dp), _p(ssp, _dp)))
+        self._snaps = (svp, ssp)
+
+    def snapshots(self):
+        return self._snaps
+
+    def set_receivers(self, phi_rows, freq, nsteps):
+        pr = np.ascontiguousarray(phi_rows, np.float64)
+        _check(lib().shaw_rom_set_receivers(self.h, _p(pr, _dp), pr.shape[0], freq, nsteps))
+        self.R, self.T = pr.shape[0], nsteps // freq
+
+    def run(self, dt, nsteps):
+        _check(lib().shaw_rom_run(self.h, dt, nsteps))
+
+    def reset(self):
+        _check(lib().shaw_rom_reset(self.h))
+
+    def advance(self, dt, nsteps):
+        _check(lib().shaw_rom_advance(self.h, dt, nsteps))
+
+    def synchronize(self):
+        _check(lib().shaw_rom_synchronize(self.h))
+
+    def get_state(self):
+        xv = np.zeros((self.kv, self.M), order="F")
+        xs = np.zeros((self.ks, self.M), order="F")
+        _check(lib().shaw_rom_get_state(self.h, _p(xv, _dp), _p(xs, _dp)))
+        return xv, xs
+
+    def seismogram(self):
+        out = np.zeros((self.R, self.T, self.M), order="F")
+        _check(lib().shaw_rom_get_seismogram(self.h, _p(out, _dp)))
+        return out
+
+    @property
+    def stream(self):
+        return lib().shaw_rom_stream(self.h)
+
+    @property
+    def kernel_launches(self):
+        return lib().shaw_rom_kernel_launches(self.h)
 
 
 def parse_input(path):

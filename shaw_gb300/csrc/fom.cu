@@ -115,6 +115,19 @@ __device__ __forceinline__ uint32_t stp_gid(uint32_t j, uint32_t i, const FomArg
   return (j + 1 < a.nr) ? j * a.sp_row + 2 * i + 1 : j * a.sp_row + i;
 }
 
+// Source term of column m at vp point p for step n (1-based), signal at t = (n-1)*dt.
+// Out of line: only the one thread that owns (src[m], m) ever calls it.
+__device__ __noinline__ double add_forcing(double x, const FomArgs& a, uint32_t m, uint32_t p, uint32_t k_local,
+                                           unsigned long long host_step) {
+  const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
+  const double t = (double)(n - 1) * a.dt;
+  const double f = shaw::signal_value(a.kind[m], a.delay[m], a.period[m], t);
+  const double ri = a.rho_inv[p];
+  // explicit roundings (no FMA contraction), as in the reference's host kernels
+  if (a.rank2) return __dadd_rn(x, __dmul_rn(__dmul_rn(ri, f), a.dt));  // AddForcingRank2: x += rhoInv*f*dt
+  return __dadd_rn(x, __dmul_rn(__dmul_rn(a.dt, ri), f));              // KokkosBlas::mult(1, x, dt, rhoInv, f)
+}
+
 // updateVelocity (fom_update_kernels.hpp:60-90 rank-1, :132-167 rank-2) for one step.
 template <int VEC>
 __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint32_t k_local,
@@ -149,21 +162,12 @@ __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint3
     fma_into(v, cE, V::ld(a.xs + (size_t)gE * a.M + off));
   }
   // forcing: the thread owning (src[m], m) adds it, evaluating the signal at t_{n-1}
-  const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
-#pragma unroll
-  for (int e = 0; e < VEC; ++e) {
-    const uint32_t m = c * VEC + e;
-    if (a.src[m] == p) {
-      const double t = (double)(n - 1) * a.dt;
-      const double f = shaw::signal_value(a.kind[m], a.delay[m], a.period[m], t);
-      const double ri = a.rho_inv[p];
-      double& x = lane(v, e);
-      // explicit roundings: no FMA contraction, as the reference's host kernels
-      if (a.rank2)
-        x = __dadd_rn(x, __dmul_rn(__dmul_rn(ri, f), a.dt));  // AddForcingRank2: x += rhoInv*f*dt
-      else
-        x = __dadd_rn(x, __dmul_rn(__dmul_rn(a.dt, ri), f));  // KokkosBlas::mult(1, x, dt, rhoInv, f)
-    }
+  if (VEC == 1) {
+    if (a.src[c] == p) lane(v, 0) = add_forcing(lane(v, 0), a, c, p, k_local, host_step);
+  } else {
+    const ulonglong2 s2 = __ldg(reinterpret_cast<const ulonglong2*>(a.src) + c);
+    if (s2.x == p) lane(v, 0) = add_forcing(lane(v, 0), a, 2 * c, p, k_local, host_step);
+    if (s2.y == p) lane(v, 1) = add_forcing(lane(v, 1), a, 2 * c + 1, p, k_local, host_step);
   }
   V::st(xp, v);
 }
@@ -213,6 +217,53 @@ __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_
   fma_into(s, cA, V::ld(a.xv + (size_t)gA * a.M + off));
   fma_into(s, cB, V::ld(a.xv + (size_t)gB * a.M + off));
   V::st(sp, s);
+}
+
+// y = Jvp x (Jvp: nvp x nsp) or y = Jsp x (nsp x nvp) on column-major multivectors
+// (one column per blockIdx.y), with the unfolded stencil values: the multivector
+// SpMV of computeRomOperatorsUsingFomJacsWithMatProp (rom_compute_jacobians.hpp:88-101).
+// Per row the products are summed in the CRS entry order (N, S, W, E / A, B).
+__global__ void fom_apply_vp_kernel(const double* __restrict__ craw, const double* __restrict__ x,
+                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nvp = (size_t)nth * nr;
+  if (p >= nvp) return;
+  const double* xc = x + (size_t)blockIdx.y * nsp;
+  const uint32_t j = p / nth, i = p - j * nth;
+  double sum = 0.0;
+  if (i != 0 && i + 1 != nth) {
+    const uint32_t row = 2 * nth - 1;
+    const uint32_t gN = ((j + 1 < nr) ? j : j - 1) * row + 2 * i;
+    const uint32_t gS = ((j > 0) ? j - 1 : 0) * row + 2 * i;
+    const uint32_t gW = (j + 1 < nr) ? j * row + 2 * (i - 1) + 1 : j * row + i - 1;
+    const uint32_t gE = (j + 1 < nr) ? j * row + 2 * i + 1 : j * row + i;
+    sum = __dadd_rn(sum, __dmul_rn(craw[p], xc[gN]));
+    if (gS != gN) sum = __dadd_rn(sum, __dmul_rn(craw[nvp + p], xc[gS]));
+    sum = __dadd_rn(sum, __dmul_rn(craw[2 * nvp + p], xc[gW]));
+    sum = __dadd_rn(sum, __dmul_rn(craw[3 * nvp + p], xc[gE]));
+  }
+  y[(size_t)blockIdx.y * nvp + p] = sum;
+}
+
+__global__ void fom_apply_sp_kernel(const double* __restrict__ craw, const double* __restrict__ x,
+                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nsp) return;
+  const size_t nvp = (size_t)nth * nr;
+  const double* xc = x + (size_t)blockIdx.y * nvp;
+  const uint32_t row = 2 * nth - 1;
+  const uint32_t j = q / row, rem = q - j * row;
+  uint32_t gA, gB;
+  if (j + 1 < nr && (rem & 1u) == 0) {
+    gA = (j + 1) * nth + (rem >> 1);
+    gB = j * nth + (rem >> 1);
+  } else {
+    gA = j * nth + ((j + 1 < nr) ? (rem >> 1) : rem);
+    gB = gA + 1;
+  }
+  double sum = __dmul_rn(craw[q], xc[gA]);
+  sum = __dadd_rn(sum, __dmul_rn(craw[nsp + q], xc[gB]));
+  y[(size_t)blockIdx.y * nsp + q] = sum;
 }
 
 __global__ void fom_fold_kernel(const double* raw, double* folded, double dt, size_t n) {
@@ -778,3 +829,29 @@ void* shaw_fom_stream(shaw_fom_t h) { return h ? (void*)h->stream : nullptr; }
 uint64_t shaw_fom_kernel_launches(shaw_fom_t h) { return h ? h->launches : 0; }
 
 }  // extern "C"
+
+namespace shaw {
+
+// Column-major multivector products with the FOM operators (no dt, no forcing):
+// dof 0: y (nvp x ncols) = Jvp x (nsp x ncols); dof 1: y (nsp x ncols) = Jsp x (nvp x ncols).
+int fom_apply(shaw_fom_t h, int dof, const double* x, double* y, uint32_t ncols, cudaStream_t s) {
+  if (!h || !x || !y) return fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (ncols == 0) return SHAW_OK;
+  if (ncols > 65535) return fail(SHAW_ERR_UNSUPPORTED, "at most 65535 columns per operator product");
+  const uint32_t rows = (uint32_t)(dof == 0 ? h->nvp : h->nsp);
+  dim3 grid((rows + 255) / 256, ncols);
+  if (dof == 0)
+    fom_apply_vp_kernel<<<grid, 256, 0, s>>>(h->cvp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp);
+  else
+    fom_apply_sp_kernel<<<grid, 256, 0, s>>>(h->csp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  return SHAW_OK;
+}
+
+void fom_sizes(shaw_fom_t h, uint64_t* nvp, uint64_t* nsp) {
+  *nvp = h->nvp;
+  *nsp = h->nsp;
+}
+
+}  // namespace shaw

@@ -1,0 +1,649 @@
+// rom.cu -- Galerkin ROM leapfrog on the reduced operators, for sm_103a.
+//
+// Reference: runRomRankOneForcing (src/kokkos/rom_run_rank_one.hpp:112-151) and the
+// rank-2 form runRomRankTwoForcing (src/kokkos/torevise/run_rom_rank_two_forcing.hpp:149-188):
+//   xv += dt * Av xs ;  xv[:,j] += (f_j(t_{n-1}) * dt) * b[:,j] ;  xs += dt * As xv
+// with Av = PhiVp^T Jvp PhiSp (kv x ks), As = PhiSp^T Jsp PhiVp (ks x kv).
+//
+// Rank 1 (one forcing) is 2 x 20000 dependent GEMVs on a few hundred modes: latency
+// bound.  It runs as ONE persistent launch on a thread-block cluster: each CTA
+// keeps its slice of operator rows in shared memory and a full copy of both
+// reduced states; after each half-step every CTA pushes its new rows into all
+// CTAs' copies through distributed shared memory and the cluster barrier
+// (barrier.cluster, hardware) orders the exchange.  Two arithmetics:
+//   SHAW_FP64        FP64 products and state (the oracle-parity path);
+//   SHAW_MIXED_FP32  "double-float": operators and states split into FP32 hi+lo,
+//                    error-free products (FMA) with compensated FP32 sums
+//                    (Ogita-Rump-Oishi Dot2) and a compensated (Kahan-style)
+//                    state update, so every flop runs on the FP32 pipe.
+// Rank 2 (M forcings) in FP64 is two cuBLAS DGEMMs per step plus a fused forcing
+// kernel that evaluates the M signals on the device.
+#include <cooperative_groups.h>
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "shaw_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int kRomThreads = 256;
+constexpr int kRomWarps = kRomThreads / 32;
+
+// ---- double-float (hi + lo FP32) arithmetic ------------------------------------
+struct df {
+  float h, l;
+};
+
+__device__ __forceinline__ df df_split(double x) {
+  df r;
+  r.h = (float)x;
+  r.l = (float)(x - (double)r.h);
+  return r;
+}
+__device__ __forceinline__ double df_val(df a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float z = s - a;
+  return {s, (a - (s - z)) + (b - z)};
+}
+__device__ __forceinline__ df df_norm(float s, float c) { return two_sum(s, c); }
+// a + b in double-float
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.h, b.h);
+  s.l += a.l + b.l;
+  return df_norm(s.h, s.l);
+}
+// a * b in double-float (error-free product of the hi parts + cross terms)
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_norm(p, e);
+}
+// accumulate a*x into (s, c): Dot2 with cross terms
+__device__ __forceinline__ void df_dot_acc(float& s, float& c, df a, df x) {
+  const float p = a.h * x.h;
+  const float e = fmaf(a.h, x.h, -p);
+  const df t = two_sum(s, p);
+  s = t.h;
+  c += t.l + e;
+  c = fmaf(a.h, x.l, c);
+  c = fmaf(a.l, x.h, c);
+}
+
+struct RomArgs {
+  const double* Av;   // kv x ks row-major
+  const double* As;   // ks x kv row-major
+  const double* b;    // kv (rank-1 forcing vector)
+  double* xv;         // kv  (initial state in, final state out)
+  double* xs;         // ks
+  int kind;
+  double period, delay, dt;
+  uint32_t kv, ks, rows_v, rows_s;  // rows per CTA
+  unsigned long long step0, nsteps;
+  uint32_t fvp, fsp;
+  double* snap_vp;  // kv x Tvp (device)
+  double* snap_sp;  // ks x Tsp
+  unsigned long long Tvp, Tsp;
+  uint32_t R, fseis;
+  const double* phi_rcv;  // R x kv row-major (PhiVp[gid_r, :])
+  double* seis;           // R x Tseis
+  unsigned long long Tseis;
+};
+
+// Dynamic shared memory of the rank-1 kernel, in elements of T (double or df):
+//   xv_full[kv] | xs_full[ks] | Av rows [rows_v x ks] | As rows [rows_s x kv] | b rows [rows_v]
+template <typename T>
+size_t rank1_smem_bytes(uint32_t kv, uint32_t ks, uint32_t rv, uint32_t rs) {
+  return sizeof(T) * ((size_t)kv + ks + (size_t)rv * ks + (size_t)rs * kv + rv);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ void warp_sum_df(float& s, float& c) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+    const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+    const df t = two_sum(s, s2);
+    s = t.h;
+    c = c + c2 + t.l;
+  }
+}
+
+template <bool MIXED>
+struct Arith;
+
+template <>
+struct Arith<false> {
+  using T = double;
+  __device__ static T load(double x) { return x; }
+  __device__ static double value(T x) { return x; }
+  // warp dot product of row[0:n] with vec[0:n]
+  __device__ static T dot(const T* row, const T* vec, uint32_t n, int lane) {
+    double acc = 0.0;
+    for (uint32_t k = lane; k < n; k += 32) acc = fma(row[k], vec[k], acc);
+    return warp_sum(acc);
+  }
+  // x + dt*y, then + fdt*b when b != null: KokkosBlas::gemv then axpy roundings
+  __device__ static T update(T x, T y, double dt) { return __dadd_rn(x, __dmul_rn(dt, y)); }
+  __device__ static T axpy(T x, double a, T b) { return __dadd_rn(x, __dmul_rn(a, b)); }
+};
+
+template <>
+struct Arith<true> {
+  using T = df;
+  __device__ static T load(double x) { return df_split(x); }
+  __device__ static double value(T x) { return df_val(x); }
+  __device__ static T dot(const T* row, const T* vec, uint32_t n, int lane) {
+    float s = 0.f, c = 0.f;
+    for (uint32_t k = lane; k < n; k += 32) df_dot_acc(s, c, row[k], vec[k]);
+    warp_sum_df(s, c);
+    return df_norm(s, c);
+  }
+  __device__ static T update(T x, T y, double dt) { return df_add(x, df_mul(df_split(dt), y)); }
+  __device__ static T axpy(T x, double a, T b) { return df_add(x, df_mul(df_split(a), b)); }
+};
+
+// One persistent launch for nsteps ROM rank-1 leapfrog steps (one cluster).
+template <bool MIXED>
+__global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs a) {
+  using A = Arith<MIXED>;
+  using T = typename A::T;
+  cg::cluster_group cluster = cg::this_cluster();
+  const uint32_t crank = cluster.block_rank();
+  const uint32_t csize = cluster.num_blocks();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* xv = reinterpret_cast<T*>(smem_raw);
+  T* xs = xv + a.kv;
+  T* Av = xs + a.ks;
+  T* As = Av + (size_t)a.rows_v * a.ks;
+  T* bv = As + (size_t)a.rows_s * a.kv;
+  // row slices of this CTA (empty for trailing ranks when the rows do not divide evenly)
+  const uint32_t v0 = min(a.kv, crank * a.rows_v), v1 = min(a.kv, v0 + a.rows_v);
+  const uint32_t s0 = min(a.ks, crank * a.rows_s), s1 = min(a.ks, s0 + a.rows_s);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (uint32_t k = threadIdx.x; k < a.kv; k += kRomThreads) xv[k] = A::load(a.xv[k]);
+  for (uint32_t k = threadIdx.x; k < a.ks; k += kRomThreads) xs[k] = A::load(a.xs[k]);
+  for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kRomThreads)
+    Av[e] = A::load(a.Av[(size_t)v0 * a.ks + e]);
+  for (size_t e = threadIdx.x; e < (size_t)(s1 - s0) * a.kv; e += kRomThreads)
+    As[e] = A::load(a.As[(size_t)s0 * a.kv + e]);
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) bv[r - v0] = A::load(a.b[r]);
+  cluster.sync();
+
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    const unsigned long long n = a.step0 + it + 1;
+    // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt
+    const double fdt = shaw::signal_value(a.kind, a.delay, a.period, (double)(n - 1) * a.dt) * a.dt;
+    // 1. velocity rows of this CTA
+    for (uint32_t r = v0 + warp; r < v1; r += kRomWarps) {
+      const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
+      const T xold = xv[r];
+      __syncwarp();  // every lane has read the old row before one of them overwrites the local copy
+      if (lane < (int)csize) {
+        T x = A::update(xold, y, a.dt);
+        x = A::axpy(x, fdt, bv[r - v0]);
+        T* dst = cluster.map_shared_rank(xv + r, lane);
+        *dst = x;
+        if (lane == 0 && a.fvp && n % a.fvp == 0)
+          a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
+      }
+    }
+    cluster.sync();
+    // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185)
+    if (a.fseis && n % a.fseis == 0) {
+      for (uint32_t r = crank * kRomWarps + warp; r < a.R; r += csize * kRomWarps) {
+        const double* prow = a.phi_rcv + (size_t)r * a.kv;
+        double acc = 0.0;
+        for (uint32_t k = lane; k < a.kv; k += 32) acc = fma(prow[k], A::value(xv[k]), acc);
+        acc = warp_sum(acc);
+        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = acc;
+      }
+    }
+    // 2. stress rows of this CTA
+    for (uint32_t r = s0 + warp; r < s1; r += kRomWarps) {
+      const T y = A::dot(As + (size_t)(r - s0) * a.kv, xv, a.kv, lane);
+      const T xold = xs[r];
+      __syncwarp();
+      if (lane < (int)csize) {
+        const T x = A::update(xold, y, a.dt);
+        T* dst = cluster.map_shared_rank(xs + r, lane);
+        *dst = x;
+        if (lane == 0 && a.fsp && n % a.fsp == 0)
+          a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
+      }
+    }
+    cluster.sync();
+  }
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) a.xv[r] = A::value(xv[r]);
+  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kRomThreads) a.xs[r] = A::value(xs[r]);
+}
+
+// Rank-2 forcing: XV[:, j] += (f_j(t_{n-1}) * dt) * b[:, j]   (one block per column)
+__global__ void rom_forcing_rank2_kernel(double* xv, const double* b, const int* kind, const double* period,
+                                         const double* delay, double dt, unsigned long long n, uint32_t kv) {
+  __shared__ double fdt;
+  const uint32_t j = blockIdx.x;
+  if (threadIdx.x == 0) fdt = shaw::signal_value(kind[j], delay[j], period[j], (double)(n - 1) * dt) * dt;
+  __syncthreads();
+  double* col = xv + (size_t)j * kv;
+  const double* bc = b + (size_t)j * kv;
+  for (uint32_t i = threadIdx.x; i < kv; i += blockDim.x) col[i] = __dadd_rn(col[i], __dmul_rn(fdt, bc[i]));
+}
+
+}  // namespace
+
+struct shaw_rom_s {
+  uint64_t kv = 0, ks = 0;
+  uint32_t M = 1;
+  int rank = 1, precision = SHAW_FP64;
+  cudaStream_t stream = nullptr;
+  cublasHandle_t blas = nullptr;
+  double *Av = nullptr, *As = nullptr, *b = nullptr, *xv = nullptr, *xs = nullptr;
+  int* kind = nullptr;
+  double *period = nullptr, *delay = nullptr;
+  std::vector<int> h_kind;
+  std::vector<double> h_period, h_delay;
+  bool signals_set = false;
+  // observers
+  uint64_t fvp = 0, fsp = 0, snap_nsteps = 0;
+  double *snap_vp = nullptr, *snap_sp = nullptr;  // device
+  double *host_vp = nullptr, *host_sp = nullptr;  // caller arrays
+  uint32_t R = 0;
+  uint64_t fseis = 0, seis_T = 0, seis_nsteps = 0;
+  double *phi_rcv = nullptr, *seis = nullptr;
+  // rank-1 cluster launch shape
+  uint32_t cluster = 1, rows_v = 0, rows_s = 0;
+  size_t smem = 0;
+  uint64_t step = 0;
+  uint64_t launches = 0;
+};
+
+namespace {
+
+using RH = shaw_rom_s;
+
+template <bool MIXED>
+int rank1_configure(RH* h) {
+  using T = typename Arith<MIXED>::T;
+  int dev = 0, maxOptin = 0;
+  SHAW_CUDA(cudaGetDevice(&dev));
+  SHAW_CUDA(cudaDeviceGetAttribute(&maxOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t budget = (size_t)maxOptin;
+  for (uint32_t c : {1u, 2u, 4u, 8u, 16u}) {
+    const uint32_t rv = (uint32_t)((h->kv + c - 1) / c), rs = (uint32_t)((h->ks + c - 1) / c);
+    const size_t bytes = rank1_smem_bytes<T>((uint32_t)h->kv, (uint32_t)h->ks, rv, rs);
+    if (bytes <= budget) {
+      // prefer the smallest cluster whose per-CTA row slice keeps the warps busy
+      if (rv > 64 && c < 16) continue;
+      h->cluster = c; h->rows_v = rv; h->rows_s = rs; h->smem = bytes;
+      return SHAW_OK;
+    }
+  }
+  return shaw::fail(SHAW_ERR_UNSUPPORTED, "reduced operators too large for the on-chip rank-1 ROM kernel");
+}
+
+template <bool MIXED>
+int rank1_launch(RH* h, double dt, uint64_t nsteps) {
+  RomArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.Av = h->Av; a.As = h->As; a.b = h->b; a.xv = h->xv; a.xs = h->xs;
+  a.kind = h->h_kind[0]; a.period = h->h_period[0]; a.delay = h->h_delay[0]; a.dt = dt;
+  a.kv = (uint32_t)h->kv; a.ks = (uint32_t)h->ks; a.rows_v = h->rows_v; a.rows_s = h->rows_s;
+  a.step0 = h->step; a.nsteps = nsteps;
+  a.fvp = (uint32_t)h->fvp; a.fsp = (uint32_t)h->fsp; a.snap_vp = h->snap_vp; a.snap_sp = h->snap_sp;
+  a.R = h->R; a.fseis = (uint32_t)h->fseis; a.phi_rcv = h->phi_rcv; a.seis = h->seis; a.Tseis = h->seis_T;
+  auto kern = rom_rank1_cluster_kernel<MIXED>;
+  SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
+  if (h->cluster > 8) SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(h->cluster);
+  cfg.blockDim = dim3(kRomThreads);
+  cfg.dynamicSmemBytes = h->smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = h->cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  h->launches++;
+  return SHAW_OK;
+}
+
+int rank2_step(RH* h, double dt, uint64_t n) {
+  const double one = 1.0;
+  // xv = xv + dt * Av xs  (Av row-major kv x ks == column-major ks x kv -> op T)
+  if (cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)h->kv, (int)h->M, (int)h->ks, &dt, h->Av, (int)h->ks,
+                  h->xs, (int)h->ks, &one, h->xv, (int)h->kv) != CUBLAS_STATUS_SUCCESS)
+    return shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (velocity) failed");
+  rom_forcing_rank2_kernel<<<h->M, 128, 0, h->stream>>>(h->xv, h->b, h->kind, h->period, h->delay, dt, n,
+                                                        (uint32_t)h->kv);
+  h->launches += 2;
+  SHAW_CUDA(cudaGetLastError());
+  if (h->fvp && n % h->fvp == 0) {
+    const uint64_t T = h->snap_nsteps / h->fvp;
+    SHAW_CUDA(cudaMemcpy2DAsync(h->host_vp + h->kv * (n / h->fvp - 1), h->kv * T * sizeof(double), h->xv,
+                                h->kv * sizeof(double), h->kv * sizeof(double), h->M, cudaMemcpyDeviceToHost,
+                                h->stream));
+  }
+  if (h->fseis && n % h->fseis == 0) {
+    const double zero = 0.0;
+    // S(:, t, :) = PhiRcv (R x kv) * XV (kv x M) into the R x T x M seismogram
+    if (cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)h->R, (int)h->M, (int)h->kv, &one, h->phi_rcv,
+                    (int)h->kv, h->xv, (int)h->kv, &zero, h->seis + (size_t)h->R * (n / h->fseis - 1),
+                    (int)(h->R * h->seis_T)) != CUBLAS_STATUS_SUCCESS)
+      return shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (seismogram) failed");
+    h->launches++;
+  }
+  // xs = xs + dt * As xv
+  if (cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)h->ks, (int)h->M, (int)h->kv, &dt, h->As, (int)h->kv,
+                  h->xv, (int)h->kv, &one, h->xs, (int)h->ks) != CUBLAS_STATUS_SUCCESS)
+    return shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (stress) failed");
+  h->launches++;
+  if (h->fsp && n % h->fsp == 0) {
+    const uint64_t T = h->snap_nsteps / h->fsp;
+    SHAW_CUDA(cudaMemcpy2DAsync(h->host_sp + h->ks * (n / h->fsp - 1), h->ks * T * sizeof(double), h->xs,
+                                h->ks * sizeof(double), h->ks * sizeof(double), h->M, cudaMemcpyDeviceToHost,
+                                h->stream));
+  }
+  return SHAW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As, int rank, uint32_t M,
+                    const double* b, int precision, shaw_rom_t* out) {
+  if (!out || !Av || !As || !b) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (kv == 0 || ks == 0 || M == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "sizes must be positive");
+  if (kv > 65535 || ks > 65535) return shaw::fail(SHAW_ERR_UNSUPPORTED, "at most 65535 modes");
+  if (rank != 1 && rank != 2) return shaw::fail(SHAW_ERR_INVALID_ARG, "rank must be 1 or 2");
+  if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
+  if (rank == 1 && precision != SHAW_FP64 && precision != SHAW_MIXED_FP32)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-1 ROM precision must be SHAW_FP64 or SHAW_MIXED_FP32");
+  if (rank == 2 && precision != SHAW_FP64)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "this rank-2 ROM precision is not available");
+  RH* h = new RH();
+  h->kv = kv; h->ks = ks; h->M = M; h->rank = rank; h->precision = precision;
+  auto bail = [&](int rc) { shaw_rom_destroy(h); return rc; };
+  cudaError_t e;
+#define SHAW_TRY(call) do { e = (call); if (e != cudaSuccess) return bail(shaw::cuda_fail(e, #call)); } while (0)
+  SHAW_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  SHAW_TRY(cudaMalloc(&h->Av, kv * ks * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->As, kv * ks * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->b, kv * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->xv, kv * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->xs, ks * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->kind, M * sizeof(int)));
+  SHAW_TRY(cudaMalloc(&h->period, M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->delay, M * sizeof(double)));
+  SHAW_TRY(cudaMemcpyAsync(h->Av, Av, kv * ks * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->As, As, kv * ks * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->b, b, kv * M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xv, 0, kv * M * sizeof(double), h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xs, 0, ks * M * sizeof(double), h->stream));
+  SHAW_TRY(cudaStreamSynchronize(h->stream));
+#undef SHAW_TRY
+  int rc = SHAW_OK;
+  if (rank == 1) {
+    rc = precision == SHAW_FP64 ? rank1_configure<false>(h) : rank1_configure<true>(h);
+  } else {
+    if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) rc = shaw::fail(SHAW_ERR_CUDA, "cublasCreate failed");
+    else if (cublasSetStream(h->blas, h->stream) != CUBLAS_STATUS_SUCCESS)
+      rc = shaw::fail(SHAW_ERR_CUDA, "cublasSetStream failed");
+  }
+  if (rc) return bail(rc);
+  *out = h;
+  return SHAW_OK;
+}
+
+void shaw_rom_destroy(shaw_rom_t h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->blas) cublasDestroy(h->blas);
+  if (h->rank == 2) {
+    if (h->host_vp) cudaHostUnregister(h->host_vp);
+    if (h->host_sp) cudaHostUnregister(h->host_sp);
+  }
+  void* bufs[] = {h->Av, h->As, h->b, h->xv, h->xs, h->kind, h->period, h->delay,
+                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int shaw_rom_set_signals(shaw_rom_t h, const int32_t* kind, const double* period, const double* delay) {
+  if (!h || !kind || !period || !delay) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  for (uint32_t j = 0; j < h->M; ++j) {
+    if (kind[j] < SHAW_SIGNAL_RICKER || kind[j] > SHAW_SIGNAL_GAUSS_DER)
+      return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown signal kind");
+    if (!(period[j] > 0.0)) return shaw::fail(SHAW_ERR_INVALID_ARG, "Period for signal must be positive. ");
+    if (!(delay[j] >= 0.0)) return shaw::fail(SHAW_ERR_INVALID_ARG, "Delay time of the signal must be >=0");
+  }
+  h->h_kind.assign(kind, kind + h->M);
+  h->h_period.assign(period, period + h->M);
+  h->h_delay.assign(delay, delay + h->M);
+  SHAW_CUDA(cudaMemcpyAsync(h->kind, h->h_kind.data(), h->M * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemcpyAsync(h->period, period, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaMemcpyAsync(h->delay, delay, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->signals_set = true;
+  return SHAW_OK;
+}
+
+int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t fvp, uint64_t fsp, uint64_t nsteps, double* host_vp,
+                           double* host_sp) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->rank == 2) {
+    if (h->host_vp) cudaHostUnregister(h->host_vp);
+    if (h->host_sp) cudaHostUnregister(h->host_sp);
+  }
+  if (h->snap_vp) { cudaFree(h->snap_vp); h->snap_vp = nullptr; }
+  if (h->snap_sp) { cudaFree(h->snap_sp); h->snap_sp = nullptr; }
+  h->host_vp = h->host_sp = nullptr;
+  h->fvp = h->fsp = h->snap_nsteps = 0;
+  if (fvp == 0 && fsp == 0) return SHAW_OK;
+  if (fvp == 0 || fsp == 0 || !host_vp || !host_sp)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "snapshot frequencies and arrays are required for both dofs");
+  if (nsteps % fvp) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Snapshot Vp frequency not a divisor of steps");
+  if (nsteps % fsp) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Snapshot Sp frequency not a divisor of steps");
+  const size_t bvp = h->kv * (nsteps / fvp) * h->M * sizeof(double);
+  const size_t bsp = h->ks * (nsteps / fsp) * h->M * sizeof(double);
+  if (h->rank == 1) {
+    SHAW_CUDA(cudaMalloc(&h->snap_vp, bvp));
+    SHAW_CUDA(cudaMalloc(&h->snap_sp, bsp));
+  } else {
+    SHAW_CUDA(cudaHostRegister(host_vp, bvp, cudaHostRegisterDefault));
+    const cudaError_t e = cudaHostRegister(host_sp, bsp, cudaHostRegisterDefault);
+    if (e != cudaSuccess) {
+      cudaHostUnregister(host_vp);
+      return shaw::cuda_fail(e, "cudaHostRegister");
+    }
+  }
+  h->host_vp = host_vp; h->host_sp = host_sp;
+  h->fvp = fvp; h->fsp = fsp; h->snap_nsteps = nsteps;
+  return SHAW_OK;
+}
+
+int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uint64_t freq, uint64_t nsteps) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->phi_rcv) { cudaFree(h->phi_rcv); h->phi_rcv = nullptr; }
+  if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
+  h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
+  if (R == 0) return SHAW_OK;
+  if (!phi_rows) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver rows");
+  if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
+  if (nsteps % freq) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Seismogram sampling frequency not a divisor of steps");
+  const uint64_t T = nsteps / freq;
+  SHAW_CUDA(cudaMalloc(&h->phi_rcv, (size_t)R * h->kv * sizeof(double)));
+  SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
+  SHAW_CUDA(cudaMemcpyAsync(h->phi_rcv, phi_rows, (size_t)R * h->kv * sizeof(double), cudaMemcpyHostToDevice,
+                            h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->R = R; h->fseis = freq; h->seis_T = T; h->seis_nsteps = nsteps;
+  return SHAW_OK;
+}
+
+int shaw_rom_reset(shaw_rom_t h) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->kv * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->ks * h->M * sizeof(double), h->stream));
+  if (h->seis) SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
+  h->step = 0;
+  return SHAW_OK;
+}
+
+int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
+  if (!h->signals_set) return shaw::fail(SHAW_ERR_STATE, "shaw_rom_set_signals must be called before stepping");
+  if (h->fseis && h->step + nsteps > h->seis_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the seismogram was sized for");
+  if (h->fvp && h->step + nsteps > h->snap_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
+  if (nsteps == 0) return SHAW_OK;
+  int rc = SHAW_OK;
+  if (h->rank == 1) {
+    rc = h->precision == SHAW_FP64 ? rank1_launch<false>(h, dt, nsteps) : rank1_launch<true>(h, dt, nsteps);
+    if (rc) return rc;
+    h->step += nsteps;
+    return SHAW_OK;
+  }
+  for (uint64_t s = 0; s < nsteps; ++s) {
+    if ((rc = rank2_step(h, dt, h->step + 1))) return rc;
+    h->step++;
+  }
+  return SHAW_OK;
+}
+
+int shaw_rom_synchronize(shaw_rom_t h) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->rank == 1 && h->fvp) {
+    // rank-1 snapshots are collected on the device; copy what the run produced
+    const uint64_t Tv = std::min<uint64_t>(h->step / h->fvp, h->snap_nsteps / h->fvp);
+    const uint64_t Ts = std::min<uint64_t>(h->step / h->fsp, h->snap_nsteps / h->fsp);
+    SHAW_CUDA(cudaMemcpy(h->host_vp, h->snap_vp, h->kv * Tv * sizeof(double), cudaMemcpyDeviceToHost));
+    SHAW_CUDA(cudaMemcpy(h->host_sp, h->snap_sp, h->ks * Ts * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return SHAW_OK;
+}
+
+int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (h->fseis && nsteps != h->seis_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "nsteps differs from the seismogram's step count");
+  if (h->fvp && nsteps != h->snap_nsteps)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "nsteps differs from the snapshots' step count");
+  int rc = shaw_rom_reset(h);
+  if (rc) return rc;
+  if ((rc = shaw_rom_advance(h, dt, nsteps))) return rc;
+  return shaw_rom_synchronize(h);
+}
+
+int shaw_rom_get_state(shaw_rom_t h, double* xv, double* xs) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (xv) SHAW_CUDA(cudaMemcpy(xv, h->xv, h->kv * h->M * sizeof(double), cudaMemcpyDeviceToHost));
+  if (xs) SHAW_CUDA(cudaMemcpy(xs, h->xs, h->ks * h->M * sizeof(double), cudaMemcpyDeviceToHost));
+  return SHAW_OK;
+}
+
+int shaw_rom_get_seismogram(shaw_rom_t h, double* out) {
+  if (!h || !out) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (!h->seis) return shaw::fail(SHAW_ERR_STATE, "no receivers set");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  SHAW_CUDA(cudaMemcpy(out, h->seis, (size_t)h->R * h->seis_T * h->M * sizeof(double), cudaMemcpyDeviceToHost));
+  return SHAW_OK;
+}
+
+void* shaw_rom_stream(shaw_rom_t h) { return h ? (void*)h->stream : nullptr; }
+uint64_t shaw_rom_kernel_launches(shaw_rom_t h) { return h ? h->launches : 0; }
+
+// computeRomOperatorsUsingFomJacsWithMatProp (rom_compute_jacobians.hpp:83-102), FP64 on the GPU:
+// tmp = J Phi with the matrix-free operator, then a cuBLAS DGEMM for Phi^T tmp.
+int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const double* phi_sp, uint64_t ks,
+                     double* rom_jvp, double* rom_jsp) {
+  if (!fom || !phi_vp || !phi_sp || !rom_jvp || !rom_jsp) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (kv == 0 || ks == 0 || kv > 65535 || ks > 65535) return shaw::fail(SHAW_ERR_INVALID_ARG, "bad mode counts");
+  uint64_t nvp = 0, nsp = 0;
+  shaw::fom_sizes(fom, &nvp, &nsp);
+  cudaStream_t s = (cudaStream_t)shaw_fom_stream(fom);
+  cublasHandle_t blas = nullptr;
+  double *pv = nullptr, *ps = nullptr, *tmp = nullptr, *out = nullptr;
+  int rc = SHAW_OK;
+  auto cleanup = [&]() {
+    if (blas) cublasDestroy(blas);
+    cudaFree(pv); cudaFree(ps); cudaFree(tmp); cudaFree(out);
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&pv, nvp * kv * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&ps, nsp * ks * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&tmp, std::max(nvp * ks, nsp * kv) * sizeof(double))) != cudaSuccess ||
+      (e = cudaMalloc(&out, kv * ks * sizeof(double))) != cudaSuccess) {
+    cleanup();
+    return shaw::cuda_fail(e, "cudaMalloc (projection)");
+  }
+  if (cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(blas, s) != CUBLAS_STATUS_SUCCESS) {
+    cleanup();
+    return shaw::fail(SHAW_ERR_CUDA, "cublas init failed");
+  }
+  const double one = 1.0, zero = 0.0;
+  do {
+    if ((e = cudaMemcpyAsync(pv, phi_vp, nvp * kv * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(ps, phi_sp, nsp * ks * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+      rc = shaw::cuda_fail(e, "cudaMemcpyAsync (basis)");
+      break;
+    }
+    // tmp (nvp x ks) = Jvp PhiSp ; romJvp row-major kv x ks == column-major ks x kv = tmp^T PhiVp
+    if ((rc = shaw::fom_apply(fom, 0, ps, tmp, (uint32_t)ks, s))) break;
+    if (cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)ks, (int)kv, (int)nvp, &one, tmp, (int)nvp, pv, (int)nvp,
+                    &zero, out, (int)ks) != CUBLAS_STATUS_SUCCESS) {
+      rc = shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (projection vp)");
+      break;
+    }
+    if ((e = cudaMemcpyAsync(rom_jvp, out, kv * ks * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+      rc = shaw::cuda_fail(e, "cudaMemcpyAsync (romJvp)");
+      break;
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { rc = shaw::cuda_fail(e, "sync"); break; }
+    // tmp (nsp x kv) = Jsp PhiVp ; romJsp row-major ks x kv == column-major kv x ks = tmp^T PhiSp
+    if ((rc = shaw::fom_apply(fom, 1, pv, tmp, (uint32_t)kv, s))) break;
+    if (cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)kv, (int)ks, (int)nsp, &one, tmp, (int)nsp, ps, (int)nsp,
+                    &zero, out, (int)kv) != CUBLAS_STATUS_SUCCESS) {
+      rc = shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (projection sp)");
+      break;
+    }
+    if ((e = cudaMemcpyAsync(rom_jsp, out, kv * ks * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+      rc = shaw::cuda_fail(e, "cudaMemcpyAsync (romJsp)");
+      break;
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { rc = shaw::cuda_fail(e, "sync"); break; }
+  } while (false);
+  cudaStreamSynchronize(s);
+  cleanup();
+  return rc;
+}
+
+}  // extern "C"

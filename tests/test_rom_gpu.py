@@ -1,0 +1,158 @@
+"""ROM parity on the GPU against the oracle: FP64 projection of the operators,
+rank-1 (cluster-resident persistent kernel) and rank-2 (DGEMM) leapfrogs, the
+in-loop ROM seismogram, and the mixed (FP32 hi+lo) rank-1 form against FP64.
+
+Tolerances: FP64 paths 1e-12 relative (normwise) to the oracle; the mixed path
+1e-6 relative (normwise, seismogram and states) to the FP64 GPU path.
+"""
+import numpy as np
+import pytest
+
+from conftest import mesh_dir
+
+pytestmark = pytest.mark.gpu
+
+MAT = [2000.0, 0.0, 0.0, 5000.0, 0.0, 0.0]
+
+
+def relerr(a, b):
+    s = np.max(np.abs(b))
+    return np.max(np.abs(a - b)) / (s if s > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def setup(shaw, oracle):
+    """POD bases of the 21x51 mesh from oracle FOM snapshots (numpy thin SVD)."""
+    m = shaw.Mesh.load(mesh_dir("fullMesh21x51"))
+    m.set_material("unilayer", MAT)
+    om = oracle.OracleMesh(mesh_dir("fullMesh21x51"))
+    om.set_material("unilayer", [(MAT[0:3], MAT[3:6])])
+    snaps_v, snaps_s = [], []
+    for d, a, p in ((400.0, 30.0, 40.0), (900.0, 60.0, 45.0), (1500.0, 120.0, 50.0), (700.0, 150.0, 60.0)):
+        out = om.fom_run(1, 600, 1.0, [om.map_source(d, a)], [0], [p], [10.0], [], 0, 3, 3)
+        snaps_v.append(out["snaps_vp"][:, :, 0])
+        snaps_s.append(out["snaps_sp"][:, :, 0])
+    uv = np.linalg.svd(np.hstack(snaps_v), full_matrices=False)[0]
+    us = np.linalg.svd(np.hstack(snaps_s), full_matrices=False)[0]
+    return m, om, uv, us
+
+
+def test_projection_matches_oracle(shaw, setup):
+    m, om, uv, us = setup
+    for kv, ks in ((24, 40), (64, 64), (200, 256)):
+        pv, ps = np.asfortranarray(uv[:, :kv]), np.asfortranarray(us[:, :ks])
+        f = shaw.Fom(m, 1, 1)
+        av, as_ = shaw.rom_project(f, pv, ps)
+        ov, os_ = om.rom_operators(pv, ps)
+        assert av.shape == (kv, ks) and as_.shape == (ks, kv)
+        assert relerr(av, ov) <= 1e-12 and relerr(as_, os_) <= 1e-12
+        f.close()
+
+
+def _rom_inputs(shaw, setup, k, src_specs):
+    m, om, uv, us = setup
+    pv, ps = np.asfortranarray(uv[:, :k]), np.asfortranarray(us[:, :k])
+    av, as_ = om.rom_operators(pv, ps)
+    gids = [om.map_source(d, a) for d, a in src_specs]
+    b = np.column_stack([om.rom_forcing_vector(pv, g) for g in gids])
+    return pv, av, as_, b
+
+
+@pytest.mark.parametrize("k", [32, 128, 256])
+def test_rank1_fp64_matches_oracle(shaw, oracle, setup, k):
+    pv, av, as_, b = _rom_inputs(shaw, setup, k, [(1111.0, 88.0)])
+    n, dt = 2000, 1.0
+    r = shaw.Rom(av, as_, b, rank=1)
+    r.set_signals("ricker", 40.0, 10.0)
+    r.set_snapshots(5, 5, n)
+    rcv = [setup[0].map_receiver(a) for a in (10, 45, 90, 135, 170)]
+    r.set_receivers(pv[rcv, :], 5, n)
+    r.run(dt, n)
+    ref = oracle.rom_run(av, as_, b, n, dt, [0], [40.0], [10.0], 5, 5)
+    svp, ssp = r.snapshots()
+    assert relerr(svp, ref["snaps_vp"]) <= 1e-12
+    assert relerr(ssp, ref["snaps_sp"]) <= 1e-12
+    xv, xs = r.get_state()
+    assert relerr(xv, ref["final_vp"]) <= 1e-12 and relerr(xs, ref["final_sp"]) <= 1e-12
+    seis = r.seismogram()[:, :, 0]
+    assert relerr(seis, pv[rcv, :] @ ref["snaps_vp"][:, :, 0]) <= 1e-12
+    assert r.kernel_launches == 1  # the whole time loop is one persistent launch
+    r.close()
+
+
+def stable_system(k, seed):
+    """A reduced pair with As = -Av^T and ||dt Av|| < 2: the leapfrog is symplectic and
+    bounded over any number of steps, so long runs measure arithmetic, not growth."""
+    rng = np.random.default_rng(seed)
+    q1 = np.linalg.qr(rng.standard_normal((k, k)))[0]
+    q2 = np.linalg.qr(rng.standard_normal((k, k)))[0]
+    av = q1 @ np.diag(np.linspace(0.05, 1.0, k)) @ q2.T
+    return av, -av.T.copy(), rng.standard_normal(k) * 1e-3
+
+
+def test_rank1_mixed_within_1e6_of_fp64(shaw):
+    k, n, dt = 256, 20000, 0.5
+    av, as_, b = stable_system(k, 5)
+    pv = np.random.default_rng(6).standard_normal((13, k)) / np.sqrt(k)
+    out = {}
+    for prec in (shaw.FP64, shaw.MIXED_FP32):
+        r = shaw.Rom(av, as_, b, rank=1, precision=prec)
+        r.set_signals("gaussDer", 60.0, 180.0)
+        r.set_receivers(pv, 1, n)
+        r.run(dt, n)
+        out[prec] = (r.seismogram(), r.get_state())
+        r.close()
+    assert np.max(np.abs(out[shaw.FP64][0])) > 0
+    assert relerr(out[shaw.MIXED_FP32][0], out[shaw.FP64][0]) <= 1e-6
+    assert relerr(out[shaw.MIXED_FP32][1][0], out[shaw.FP64][1][0]) <= 1e-6
+
+
+def test_rank1_advance_in_pieces(shaw, setup):
+    pv, av, as_, b = _rom_inputs(shaw, setup, 64, [(500.0, 45.0)])
+    r = shaw.Rom(av, as_, b, rank=1)
+    r.set_signals("sinusoid", 40.0, 0.0)
+    r.run(1.0, 300)
+    whole = r.get_state()
+    r.reset()
+    for k in (1, 99, 200):
+        r.advance(1.0, k)
+    r.synchronize()
+    part = r.get_state()
+    assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
+
+
+@pytest.mark.parametrize("M", [1, 5, 16])
+def test_rank2_fp64_matches_oracle(shaw, oracle, setup, M):
+    rng = np.random.default_rng(M)
+    specs = [(float(rng.uniform(200, 1500)), float(rng.uniform(0, 180))) for _ in range(M)]
+    pv, av, as_, b = _rom_inputs(shaw, setup, 48, specs)
+    periods = rng.uniform(30, 90, M)
+    n, dt = 400, 1.0
+    r = shaw.Rom(av, as_, b, rank=2)
+    r.set_signals("gaussDer", periods, 100.0)
+    r.set_snapshots(4, 8, n)
+    rcv = [setup[0].map_receiver(a) for a in (20, 80, 160)]
+    r.set_receivers(pv[rcv, :], 2, n)
+    r.run(dt, n)
+    ref = oracle.rom_run(av, as_, b, n, dt, [2] * M, periods, [100.0] * M, 4, 8)
+    svp, ssp = r.snapshots()
+    assert relerr(svp, ref["snaps_vp"]) <= 1e-12 and relerr(ssp, ref["snaps_sp"]) <= 1e-12
+    xv, xs = r.get_state()
+    assert relerr(xv, ref["final_vp"]) <= 1e-12 and relerr(xs, ref["final_sp"]) <= 1e-12
+    seis = r.seismogram()  # every 2 steps; snapshots every 4: odd seismogram samples are the snapshot steps
+    expect = np.einsum("rk,ktm->rtm", pv[rcv, :], ref["snaps_vp"])
+    assert relerr(seis[:, 1::2, :], expect) <= 1e-12
+
+
+def test_rom_error_paths(shaw, setup):
+    pv, av, as_, b = _rom_inputs(shaw, setup, 16, [(500.0, 45.0)])
+    with pytest.raises(shaw.ShawError) as e:
+        shaw.Rom(av, as_, np.column_stack([b, b]), rank=1)
+    assert e.value.code == shaw.ERR_INVALID_ARG
+    r = shaw.Rom(av, as_, b, rank=1)
+    with pytest.raises(shaw.ShawError) as e:
+        r.run(1.0, 10)
+    assert e.value.code == shaw.ERR_STATE
+    with pytest.raises(shaw.ShawError) as e:
+        r.set_snapshots(3, 3, 10)
+    assert e.value.code == shaw.ERR_FREQ_DIVISOR
