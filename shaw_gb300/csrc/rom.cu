@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "rom_tc.h"
 #include "shaw_internal.h"
 
 namespace cg = cooperative_groups;
@@ -248,6 +249,7 @@ struct shaw_rom_s {
   uint64_t kv = 0, ks = 0;
   uint32_t M = 1;
   int rank = 1, precision = SHAW_FP64;
+  shaw::tc::Plan* tc = nullptr;  // rank-2 tensor-core (TF32x3) path
   cudaStream_t stream = nullptr;
   cublasHandle_t blas = nullptr;
   double *Av = nullptr, *As = nullptr, *b = nullptr, *xv = nullptr, *xs = nullptr;
@@ -378,8 +380,8 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
   if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
   if (rank == 1 && precision != SHAW_FP64 && precision != SHAW_MIXED_FP32)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-1 ROM precision must be SHAW_FP64 or SHAW_MIXED_FP32");
-  if (rank == 2 && precision != SHAW_FP64)
-    return shaw::fail(SHAW_ERR_UNSUPPORTED, "this rank-2 ROM precision is not available");
+  if (rank == 2 && precision != SHAW_FP64 && precision != SHAW_MIXED_TF32X3)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-2 ROM precision must be SHAW_FP64 or SHAW_MIXED_TF32X3");
   RH* h = new RH();
   h->kv = kv; h->ks = ks; h->M = M; h->rank = rank; h->precision = precision;
   auto bail = [&](int rc) { shaw_rom_destroy(h); return rc; };
@@ -404,6 +406,10 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
   int rc = SHAW_OK;
   if (rank == 1) {
     rc = precision == SHAW_FP64 ? rank1_configure<false>(h) : rank1_configure<true>(h);
+  } else if (precision == SHAW_MIXED_TF32X3) {
+    rc = shaw::tc::create(h->tc, (uint32_t)kv, (uint32_t)ks, h->Av, h->As, M, h->b, h->stream);
+    if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
+      rc = shaw::fail(SHAW_ERR_CUDA, "tensor-core ROM setup failed");
   } else {
     if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) rc = shaw::fail(SHAW_ERR_CUDA, "cublasCreate failed");
     else if (cublasSetStream(h->blas, h->stream) != CUBLAS_STATUS_SUCCESS)
@@ -418,7 +424,8 @@ void shaw_rom_destroy(shaw_rom_t h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->blas) cublasDestroy(h->blas);
-  if (h->rank == 2) {
+  if (h->tc) shaw::tc::destroy(h->tc);
+  if (h->rank == 2 && !h->tc) {
     if (h->host_vp) cudaHostUnregister(h->host_vp);
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
@@ -453,7 +460,8 @@ int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
                            double* host_sp) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
-  if (h->rank == 2) {
+  const bool device_snaps = h->rank == 1 || h->tc;  // collected on the device by the persistent kernels
+  if (!device_snaps) {
     if (h->host_vp) cudaHostUnregister(h->host_vp);
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
@@ -468,7 +476,7 @@ int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
   if (nsteps % fsp) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Snapshot Sp frequency not a divisor of steps");
   const size_t bvp = h->kv * (nsteps / fvp) * h->M * sizeof(double);
   const size_t bsp = h->ks * (nsteps / fsp) * h->M * sizeof(double);
-  if (h->rank == 1) {
+  if (device_snaps) {
     SHAW_CUDA(cudaMalloc(&h->snap_vp, bvp));
     SHAW_CUDA(cudaMalloc(&h->snap_sp, bsp));
   } else {
@@ -491,6 +499,9 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
   if (R == 0) return SHAW_OK;
+  if (h->tc)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED,
+                      "the tensor-core rank-2 ROM records snapshots; form the seismogram from them");
   if (!phi_rows) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver rows");
   if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
   if (nsteps % freq) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Seismogram sampling frequency not a divisor of steps");
@@ -510,6 +521,10 @@ int shaw_rom_reset(shaw_rom_t h) {
   SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->kv * h->M * sizeof(double), h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->ks * h->M * sizeof(double), h->stream));
   if (h->seis) SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
+  if (h->tc) {
+    const int rc = shaw::tc::reset(h->tc, h->stream);
+    if (rc) return rc;
+  }
   h->step = 0;
   return SHAW_OK;
 }
@@ -530,6 +545,15 @@ int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
     h->step += nsteps;
     return SHAW_OK;
   }
+  if (h->tc) {
+    rc = shaw::tc::advance(h->tc, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay, h->snap_vp,
+                           h->snap_sp, h->fvp ? h->snap_nsteps / h->fvp : 0, h->fsp ? h->snap_nsteps / h->fsp : 0,
+                           (uint32_t)h->fvp, (uint32_t)h->fsp);
+    if (rc) return rc;
+    h->launches++;
+    h->step += nsteps;
+    return SHAW_OK;
+  }
   for (uint64_t s = 0; s < nsteps; ++s) {
     if ((rc = rank2_step(h, dt, h->step + 1))) return rc;
     h->step++;
@@ -546,6 +570,15 @@ int shaw_rom_synchronize(shaw_rom_t h) {
     const uint64_t Ts = std::min<uint64_t>(h->step / h->fsp, h->snap_nsteps / h->fsp);
     SHAW_CUDA(cudaMemcpy(h->host_vp, h->snap_vp, h->kv * Tv * sizeof(double), cudaMemcpyDeviceToHost));
     SHAW_CUDA(cudaMemcpy(h->host_sp, h->snap_sp, h->ks * Ts * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  if (h->tc) {
+    const int rc = shaw::tc::check(h->tc, h->stream);
+    if (rc) return rc;
+    if (h->fvp) {
+      const uint64_t Tv = h->snap_nsteps / h->fvp, Ts = h->snap_nsteps / h->fsp;
+      SHAW_CUDA(cudaMemcpy(h->host_vp, h->snap_vp, h->kv * Tv * h->M * sizeof(double), cudaMemcpyDeviceToHost));
+      SHAW_CUDA(cudaMemcpy(h->host_sp, h->snap_sp, h->ks * Ts * h->M * sizeof(double), cudaMemcpyDeviceToHost));
+    }
   }
   return SHAW_OK;
 }
@@ -564,6 +597,10 @@ int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps) {
 
 int shaw_rom_get_state(shaw_rom_t h, double* xv, double* xs) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (h->tc) {
+    const int rc = shaw::tc::get_state(h->tc, h->stream, h->xv, h->xs);
+    if (rc) return rc;
+  }
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   if (xv) SHAW_CUDA(cudaMemcpy(xv, h->xv, h->kv * h->M * sizeof(double), cudaMemcpyDeviceToHost));
   if (xs) SHAW_CUDA(cudaMemcpy(xs, h->xs, h->ks * h->M * sizeof(double), cudaMemcpyDeviceToHost));

@@ -156,3 +156,44 @@ def test_rom_error_paths(shaw, setup):
     with pytest.raises(shaw.ShawError) as e:
         r.set_snapshots(3, 3, 10)
     assert e.value.code == shaw.ERR_FREQ_DIVISOR
+
+
+def _fp64_vs_mixed(shaw, prec, k_v, k_s, M, n, dt, seed, freq=0, smax=1.0):
+    rng = np.random.default_rng(seed)
+    kmin = min(k_v, k_s)
+    av, as_, _ = stable_system(kmin, seed)
+    av, as_ = av * smax, as_ * smax
+    if k_v != k_s:  # embed the stable square pair in a rectangular one
+        big_v = np.zeros((k_v, k_s))
+        big_v[:kmin, :kmin] = av
+        big_s = np.zeros((k_s, k_v))
+        big_s[:kmin, :kmin] = as_
+        av, as_ = big_v, big_s
+    b = rng.standard_normal((k_v, M)) * 1e-3
+    periods = rng.uniform(30, 90, M)
+    out = {}
+    for p in (shaw.FP64, prec):
+        r = shaw.Rom(av, as_, b, rank=2, precision=p)
+        r.set_signals("gaussDer", periods, 40.0)
+        if freq:
+            r.set_snapshots(freq, freq, n)
+        r.run(dt, n)
+        out[p] = (r.get_state(), r.snapshots())
+        r.close()
+    return out[shaw.FP64], out[prec]
+
+
+def test_rank2_tf32x3_tensor_core_tiny(shaw):
+    """One CTA, one 128-mode tile, a few steps: the tcgen05 TF32x3 pipeline end to end.
+    The tensor pipe accumulates in FP32 with truncation, so this form is held to 1e-5."""
+    ((xv64, xs64), _), ((xvtc, xstc), _) = _fp64_vs_mixed(shaw, shaw.MIXED_TF32X3, 128, 128, 32, 20, 0.5, 1)
+    assert np.max(np.abs(xv64)) > 0
+    assert relerr(xvtc, xv64) <= 1e-5 and relerr(xstc, xs64) <= 1e-5
+
+
+@pytest.mark.parametrize("kv,ks,M", [(100, 72, 45), (256, 256, 300), (512, 512, 64)])
+def test_rank2_tf32x3_tensor_core_short_runs(shaw, kv, ks, M):
+    ((xv64, xs64), (sv64, ss64)), ((xvtc, xstc), (svtc, sstc)) = _fp64_vs_mixed(
+        shaw, shaw.MIXED_TF32X3, kv, ks, M, 200, 0.5, kv + M, freq=50, smax=0.2)
+    for a, b in ((xvtc, xv64), (xstc, xs64), (svtc, sv64), (sstc, ss64)):
+        assert relerr(a, b) <= 1e-5
