@@ -68,6 +68,9 @@ extern "C" {
 #define SHAW_MIXED_TF32X3     1  /* ROM: split TF32x3 products, FP32 accumulate, Kahan state */
 #define SHAW_MIXED_BF16X3     2  /* ROM: split BF16x3 products, FP32 accumulate, Kahan state */
 #define SHAW_MIXED_FP32       3  /* FP32 products, Kahan-compensated FP32 state             */
+#define SHAW_MIXED_OZAKI_BF16 4  /* ROM rank 2: BF16 tensor cores, 6 six-bit slices per
+                                    operand (Ozaki scheme), exact FP32 accumulation,
+                                    compensated FP32 state: FP64-grade GEMMs              */
 
 const char* shaw_last_error(void);
 const char* shaw_version(void);

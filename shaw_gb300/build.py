@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libshaw_gpu.so")
 EXE = os.path.join(BUILD, "shaw_exe")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["fom.cu", "rom.cu", "rom_tc.cu"]
+CU_SOURCES = ["fom.cu", "rom.cu", "rom_tc.cu", "rom_oz.cu"]
 CPP_SOURCES = ["host.cpp", "driver.cpp", "rom_driver.cpp", "yaml_lite.cpp"]
 
 

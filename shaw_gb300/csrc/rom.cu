@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "rom_oz.h"
 #include "rom_tc.h"
 #include "shaw_internal.h"
 
@@ -249,7 +250,9 @@ struct shaw_rom_s {
   uint64_t kv = 0, ks = 0;
   uint32_t M = 1;
   int rank = 1, precision = SHAW_FP64;
-  shaw::tc::Plan* tc = nullptr;  // rank-2 tensor-core (TF32x3) path
+  shaw::tc::Plan* tc = nullptr;  // rank-2 tensor-core TF32x3 path
+  shaw::oz::Plan* oz = nullptr;  // rank-2 tensor-core Ozaki BF16 path
+  bool persistent2() const { return tc != nullptr || oz != nullptr; }
   cudaStream_t stream = nullptr;
   cublasHandle_t blas = nullptr;
   double *Av = nullptr, *As = nullptr, *b = nullptr, *xv = nullptr, *xs = nullptr;
@@ -380,8 +383,9 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
   if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
   if (rank == 1 && precision != SHAW_FP64 && precision != SHAW_MIXED_FP32)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-1 ROM precision must be SHAW_FP64 or SHAW_MIXED_FP32");
-  if (rank == 2 && precision != SHAW_FP64 && precision != SHAW_MIXED_TF32X3)
-    return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-2 ROM precision must be SHAW_FP64 or SHAW_MIXED_TF32X3");
+  if (rank == 2 && precision != SHAW_FP64 && precision != SHAW_MIXED_TF32X3 && precision != SHAW_MIXED_OZAKI_BF16)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED,
+                      "rank-2 ROM precision must be SHAW_FP64, SHAW_MIXED_TF32X3 or SHAW_MIXED_OZAKI_BF16");
   RH* h = new RH();
   h->kv = kv; h->ks = ks; h->M = M; h->rank = rank; h->precision = precision;
   auto bail = [&](int rc) { shaw_rom_destroy(h); return rc; };
@@ -410,6 +414,10 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
     rc = shaw::tc::create(h->tc, (uint32_t)kv, (uint32_t)ks, h->Av, h->As, M, h->b, h->stream);
     if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = shaw::fail(SHAW_ERR_CUDA, "tensor-core ROM setup failed");
+  } else if (precision == SHAW_MIXED_OZAKI_BF16) {
+    rc = shaw::oz::create(h->oz, (uint32_t)kv, (uint32_t)ks, Av, As, M, b, h->stream);
+    if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
+      rc = shaw::fail(SHAW_ERR_CUDA, "Ozaki tensor-core ROM setup failed");
   } else {
     if (cublasCreate(&h->blas) != CUBLAS_STATUS_SUCCESS) rc = shaw::fail(SHAW_ERR_CUDA, "cublasCreate failed");
     else if (cublasSetStream(h->blas, h->stream) != CUBLAS_STATUS_SUCCESS)
@@ -425,7 +433,8 @@ void shaw_rom_destroy(shaw_rom_t h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->blas) cublasDestroy(h->blas);
   if (h->tc) shaw::tc::destroy(h->tc);
-  if (h->rank == 2 && !h->tc) {
+  if (h->oz) shaw::oz::destroy(h->oz);
+  if (h->rank == 2 && !h->persistent2()) {
     if (h->host_vp) cudaHostUnregister(h->host_vp);
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
@@ -460,7 +469,7 @@ int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
                            double* host_sp) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
-  const bool device_snaps = h->rank == 1 || h->tc;  // collected on the device by the persistent kernels
+  const bool device_snaps = h->rank == 1 || h->persistent2();  // collected on the device by persistent kernels
   if (!device_snaps) {
     if (h->host_vp) cudaHostUnregister(h->host_vp);
     if (h->host_sp) cudaHostUnregister(h->host_sp);
@@ -499,7 +508,7 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
   if (R == 0) return SHAW_OK;
-  if (h->tc)
+  if (h->persistent2())
     return shaw::fail(SHAW_ERR_UNSUPPORTED,
                       "the tensor-core rank-2 ROM records snapshots; form the seismogram from them");
   if (!phi_rows) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver rows");
@@ -521,8 +530,8 @@ int shaw_rom_reset(shaw_rom_t h) {
   SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->kv * h->M * sizeof(double), h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->ks * h->M * sizeof(double), h->stream));
   if (h->seis) SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
-  if (h->tc) {
-    const int rc = shaw::tc::reset(h->tc, h->stream);
+  if (h->tc || h->oz) {
+    const int rc = h->tc ? shaw::tc::reset(h->tc, h->stream) : shaw::oz::reset(h->oz, h->stream);
     if (rc) return rc;
   }
   h->step = 0;
@@ -545,10 +554,12 @@ int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
     h->step += nsteps;
     return SHAW_OK;
   }
-  if (h->tc) {
-    rc = shaw::tc::advance(h->tc, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay, h->snap_vp,
-                           h->snap_sp, h->fvp ? h->snap_nsteps / h->fvp : 0, h->fsp ? h->snap_nsteps / h->fsp : 0,
-                           (uint32_t)h->fvp, (uint32_t)h->fsp);
+  if (h->tc || h->oz) {
+    const unsigned long long Tv = h->fvp ? h->snap_nsteps / h->fvp : 0, Ts = h->fsp ? h->snap_nsteps / h->fsp : 0;
+    rc = h->tc ? shaw::tc::advance(h->tc, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay,
+                                   h->snap_vp, h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp)
+               : shaw::oz::advance(h->oz, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay,
+                                   h->snap_vp, h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp);
     if (rc) return rc;
     h->launches++;
     h->step += nsteps;
@@ -571,8 +582,8 @@ int shaw_rom_synchronize(shaw_rom_t h) {
     SHAW_CUDA(cudaMemcpy(h->host_vp, h->snap_vp, h->kv * Tv * sizeof(double), cudaMemcpyDeviceToHost));
     SHAW_CUDA(cudaMemcpy(h->host_sp, h->snap_sp, h->ks * Ts * sizeof(double), cudaMemcpyDeviceToHost));
   }
-  if (h->tc) {
-    const int rc = shaw::tc::check(h->tc, h->stream);
+  if (h->tc || h->oz) {
+    const int rc = h->tc ? shaw::tc::check(h->tc, h->stream) : shaw::oz::check(h->oz, h->stream);
     if (rc) return rc;
     if (h->fvp) {
       const uint64_t Tv = h->snap_nsteps / h->fvp, Ts = h->snap_nsteps / h->fsp;
@@ -597,8 +608,9 @@ int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps) {
 
 int shaw_rom_get_state(shaw_rom_t h, double* xv, double* xs) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
-  if (h->tc) {
-    const int rc = shaw::tc::get_state(h->tc, h->stream, h->xv, h->xs);
+  if (h->tc || h->oz) {
+    const int rc = h->tc ? shaw::tc::get_state(h->tc, h->stream, h->xv, h->xs)
+                         : shaw::oz::get_state(h->oz, h->stream, h->xv, h->xs);
     if (rc) return rc;
   }
   SHAW_CUDA(cudaStreamSynchronize(h->stream));

