@@ -162,6 +162,27 @@ typedef struct shaw_rom_s* shaw_rom_t;
 int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const double* phi_sp, uint64_t ks,
                      double* rom_jvp, double* rom_jsp);
 
+/* The same projection without any allocation.  It has no counterpart in the
+ * reference.  It exists for callers that cannot allocate device memory while
+ * they run: an application that hands the library a fixed memory budget up
+ * front, a code path where an allocation would synchronise the device, or a
+ * runtime that owns every device allocation itself.
+ *   - Every array is a DEVICE pointer owned by the caller: d_phi_vp nvp x kv and
+ *     d_phi_sp nsp x ks (LayoutLeft), d_rom_jvp kv x ks and d_rom_jsp ks x kv
+ *     (row-major).  The work is enqueued on `stream` (a cudaStream_t; 0 is the
+ *     default stream) and the call returns without waiting for it.
+ *   - The intermediate J*Phi columns pass through one fixed 16 MiB FP64 device
+ *     array inside the library; every GPU that loads the library holds it until
+ *     the process exits.  One column must fit: nvp and nsp must each be at most
+ *     2097152, otherwise the call returns SHAW_ERR_INVALID_ARG.
+ *   - It calls no cudaMalloc or cudaFree and no library routine that allocates.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU (other
+ *     streams, or unordered threads) race on it. */
+int shaw_rom_project_noalloc(shaw_fom_t fom, const double* d_phi_vp, uint64_t kv, const double* d_phi_sp,
+                             uint64_t ks, double* d_rom_jvp, double* d_rom_jsp, void* stream);
+
 /* The reduced system of runRomRankOneForcing (rank 1, M == 1) and
  * runRomRankTwoForcing (rank 2, M columns):
  *   xv += dt Av xs ;  xv[:,j] += (f_j(t_{n-1}) dt) b[:,j] ;  xs += dt As xv

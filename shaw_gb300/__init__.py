@@ -89,6 +89,7 @@ SIGNATURES = [
     ("shaw_fom_stream", _vp, [_vp]),
     ("shaw_fom_kernel_launches", ctypes.c_uint64, [_vp]),
     ("shaw_rom_project", ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _dp, ctypes.c_uint64, _dp, _dp]),
+    ("shaw_rom_project_noalloc", ctypes.c_int, [_vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64, _vp, _vp, _vp]),
     ("shaw_rom_create", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _dp, _dp, ctypes.c_int, ctypes.c_uint32,
                                        _dp, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("shaw_rom_destroy", None, [_vp]),

@@ -24,6 +24,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -230,6 +231,26 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
   }
   for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) a.xv[r] = A::value(xv[r]);
   for (uint32_t r = s0 + threadIdx.x; r < s1; r += kRomThreads) a.xs[r] = A::value(xs[r]);
+}
+
+// Reduced-operator block out[i * ldo + j0 + c] = sum_p phi[p + n*i] * tmp[p + n*c] for
+// i < k and c < ncols: one block per output, FP64 tree reduction (no library GEMM).
+__global__ void rom_project_dot_kernel(const double* __restrict__ phi, const double* __restrict__ tmp, uint64_t n,
+                                       double* __restrict__ out, uint64_t ldo, uint64_t j0) {
+  __shared__ double part[kRomWarps];
+  const uint32_t i = blockIdx.x, c = blockIdx.y;
+  const double* a = phi + (size_t)n * i;
+  const double* b = tmp + (size_t)n * c;
+  double acc = 0.0;
+  for (uint64_t p = threadIdx.x; p < n; p += kRomThreads) acc = fma(a[p], b[p], acc);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < kRomWarps ? part[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) out[(size_t)i * ldo + j0 + c] = v;
+  }
 }
 
 // Rank-2 forcing: XV[:, j] += (f_j(t_{n-1}) * dt) * b[:, j]   (one block per column)
@@ -696,3 +717,81 @@ int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const do
 }
 
 }  // extern "C"
+
+// ---- projection without allocation --------------------------------------------------
+// Some callers cannot allocate device memory during a call: a host application that
+// hands the library a fixed memory budget up front, a code path that runs where
+// allocation is forbidden or would synchronise the device, or a runtime that
+// manages every device allocation itself.  For them the projection below keeps
+// its intermediate J * Phi block in one fixed, statically sized device array.
+//
+// The array lives for as long as the library is loaded, on every GPU that loads
+// it.  Host code must not pass the array's name to a kernel (in host code that
+// name is a host-side stand-in, not a device address): its device address is
+// looked up once per device with cudaGetSymbolAddress.  All calls share the array,
+// so calls whose work overlaps on the GPU (different streams, or threads without
+// ordering) race on it; the array keeps whatever the last call left in it, and
+// every element this code reads is written first within the same call.
+namespace {
+
+constexpr uint64_t kProjectScratchDoubles = 1ull << 21;  // 16 MiB of FP64
+static __device__ __align__(256) double g_project_scratch[kProjectScratchDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_addr[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set up on first use).
+int project_scratch(double** out) {
+  int dev = 0;
+  SHAW_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return shaw::fail(SHAW_ERR_UNSUPPORTED, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_project_scratch);
+    if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGetSymbolAddress(project scratch)");
+    g_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return SHAW_OK;
+}
+
+// out (k_out x k_in, row-major) = PhiOut^T (J PhiIn), chunked through the scratch array.
+int project_block(shaw_fom_t fom, int dof, const double* phi_in, uint64_t n_in, uint64_t k_in,
+                  const double* phi_out, uint64_t n_out, uint64_t k_out, double* out, double* scratch,
+                  cudaStream_t s) {
+  uint64_t chunk = kProjectScratchDoubles / n_out;
+  if (chunk > 65535) chunk = 65535;
+  for (uint64_t j0 = 0; j0 < k_in; j0 += chunk) {
+    const uint64_t c = (k_in - j0 < chunk) ? k_in - j0 : chunk;
+    int rc = shaw::fom_apply(fom, dof, phi_in + n_in * j0, scratch, (uint32_t)c, s);
+    if (rc) return rc;
+    rom_project_dot_kernel<<<dim3((unsigned)k_out, (unsigned)c), kRomThreads, 0, s>>>(phi_out, scratch, n_out, out,
+                                                                                  k_in, j0);
+    SHAW_CUDA(cudaGetLastError());
+  }
+  return SHAW_OK;
+}
+
+}  // namespace
+
+extern "C" int shaw_rom_project_noalloc(shaw_fom_t fom, const double* d_phi_vp, uint64_t kv, const double* d_phi_sp,
+                                        uint64_t ks, double* d_rom_jvp, double* d_rom_jsp, void* stream) {
+  if (!fom || !d_phi_vp || !d_phi_sp || !d_rom_jvp || !d_rom_jsp)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (kv == 0 || ks == 0 || kv > 65535 || ks > 65535) return shaw::fail(SHAW_ERR_INVALID_ARG, "bad mode counts");
+  uint64_t nvp = 0, nsp = 0;
+  shaw::fom_sizes(fom, &nvp, &nsp);
+  if (nvp > kProjectScratchDoubles || nsp > kProjectScratchDoubles)
+    return shaw::fail(SHAW_ERR_INVALID_ARG,
+                      "mesh too large for the allocation-free projection: nvp and nsp must be <= 2097152 "
+                      "(one column of J*Phi must fit the 16 MiB scratch array); use shaw_rom_project");
+  double* scratch = nullptr;
+  int rc = project_scratch(&scratch);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // romJvp (kv x ks) = PhiVp^T (Jvp PhiSp);  romJsp (ks x kv) = PhiSp^T (Jsp PhiVp)
+  if ((rc = project_block(fom, 0, d_phi_sp, nsp, ks, d_phi_vp, nvp, kv, d_rom_jvp, scratch, s))) return rc;
+  return project_block(fom, 1, d_phi_vp, nvp, kv, d_phi_sp, nsp, ks, d_rom_jsp, scratch, s);
+}
