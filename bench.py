@@ -45,6 +45,9 @@ def parse():
     # smaller cases for profiling captures (the default is the benchmark workload)
     p.add_argument("--forcings", type=int, default=M)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extra", action="store_true", help="skip the other configurations' lines")
+    p.add_argument("--profile-rom", default=None, choices=["ozaki", "tf32x3", "fp64"],
+                   help="only run the rank-2 ROM (k=512, M=4096) for --steps steps, for profiler captures")
     return p.parse_args()
 
 
@@ -175,6 +178,100 @@ def cpu_baseline(np, budget_s=20.0):
     return dict(value=units / el, unit="DOF-updates/s", cores=threads, kind="port",
                 sample="%d leapfrog steps of %d of the 256 forcing columns on the 1000x2000 grid (%.1f s)"
                        % (steps, ms, el), seconds=el, steps=steps)
+
+
+def _timed(torch, stream_ptr, fn):
+    s = torch.cuda.ExternalStream(stream_ptr)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    fn()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def _relerr(np, a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def stable_rom(np, k, seed, smin, smax):
+    """Seeded reduced pair with As = -Av^T and singular values in [smin, smax]: a
+    bounded (symplectic) leapfrog standing in for a POD-projected SHAW ROM."""
+    rng = np.random.default_rng(seed)
+    q1 = np.linalg.qr(rng.standard_normal((k, k)))[0]
+    q2 = np.linalg.qr(rng.standard_normal((k, k)))[0]
+    av = q1 @ np.diag(np.linspace(smin, smax, k)) @ q2.T
+    return av, -av.T.copy()
+
+
+def extra_workloads(np, torch, shaw):
+    """The other configurations, each timed with CUDA events on its handle's stream."""
+    out = {}
+    # config 1: FOM rank-1 FP64, 101 theta x 201 r, one gaussDer source at 640 km on the axis
+    mesh = shaw.Mesh.generate(101, 201)
+    mesh.set_material("unilayer", MATERIAL)
+    dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
+    n = 2000
+    f = shaw.Fom(mesh, 1, 1)
+    f.set_sources([mesh.map_source(640.0, 0.0)], "gaussDer", 60.0, 180.0)
+    f.set_receivers([mesh.map_receiver(float(a)) for a in range(181)], 1, n)
+    f.run(dt, n)  # warm-up (graph instantiation)
+    f.reset()
+    t = _timed(torch, f.stream, lambda: f.advance(dt, n))
+    f.synchronize()
+    out["fom_rank1_101x201"] = {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t,
+                                "steps": n, "us_per_step": t / n * 1e6}
+    f.close()
+    # config 3: ROM rank-1, k = 256, 20000 steps, FP64 vs mixed (FP32 hi+lo, compensated)
+    k, n, dtr = 256, 20000, 0.5
+    av, as_ = stable_rom(np, k, 3, 0.004, 0.2)
+    b = np.random.default_rng(4).standard_normal(k) * 1e-3
+    rows = np.random.default_rng(5).standard_normal((181, k)) / np.sqrt(k)
+    res = {}
+    for prec in (shaw.FP64, shaw.MIXED_FP32):
+        r = shaw.Rom(av, as_, b, rank=1, precision=prec)
+        r.set_signals("gaussDer", 60.0, 180.0)
+        r.set_receivers(rows, 1, n)
+        r.reset()
+        t = _timed(torch, r.stream, lambda: r.advance(dtr, n))
+        r.synchronize()
+        res[prec] = (t, r.seismogram())
+        r.close()
+    out["rom_rank1_k256"] = {"metric": "ROM forcing-steps/s", "steps": n,
+                             "fp64": n / res[shaw.FP64][0], "mixed_fp32": n / res[shaw.MIXED_FP32][0],
+                             "speedup": res[shaw.FP64][0] / res[shaw.MIXED_FP32][0],
+                             "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1])}
+    # config 4: ROM rank-2, k = 512, M = 4096 forcings; FP64 (DGEMM) vs tensor-core forms
+    k, M, n = 512, 4096, 100
+    av, as_ = stable_rom(np, k, 7, 0.004, 0.2)
+    rng = np.random.default_rng(8)
+    b = rng.standard_normal((k, M)) * 1e-3
+    periods = rng.uniform(30.0, 90.0, M)
+    rows = rng.standard_normal((181, k)) / np.sqrt(k)
+    res = {}
+    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.MIXED_TF32X3):
+        r = shaw.Rom(av, as_, b, rank=2, precision=prec)
+        r.set_signals("gaussDer", periods, 180.0)
+        r.set_snapshots(n // 4, n // 4, n)
+        r.reset()
+        r.advance(dtr, 2 if prec == shaw.FP64 else n)  # warm-up
+        r.synchronize()
+        r.reset()
+        t = _timed(torch, r.stream, lambda: r.advance(dtr, n))
+        r.synchronize()
+        snaps = r.snapshots()[0]
+        res[prec] = (t, np.einsum("rk,ktm->rtm", rows, snaps), r.get_state()[0])
+        r.close()
+    t64 = res[shaw.FP64][0]
+    out["rom_rank2_k512_M4096"] = {
+        "metric": "ROM forcing-steps/s", "steps": n, "fp64": M * n / t64,
+        "ozaki_bf16": M * n / res[shaw.MIXED_OZAKI_BF16][0], "tf32x3": M * n / res[shaw.MIXED_TF32X3][0],
+        "speedup_ozaki": t64 / res[shaw.MIXED_OZAKI_BF16][0], "speedup_tf32x3": t64 / res[shaw.MIXED_TF32X3][0],
+        "seismogram_rel_err_ozaki": _relerr(np, res[shaw.MIXED_OZAKI_BF16][1], res[shaw.FP64][1]),
+        "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
+        "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
+        "operators": "seeded synthetic pair with As = -Av^T (bounded leapfrog), dt*sigma in [0.002, 0.1]"}
+    return out
 
 
 def run_reference(args):
@@ -341,6 +438,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if not args.no_extra:
+        line["other_configs"] = extra_workloads(np, torch, shaw)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(np).items() if k in
                                 ("value", "unit", "cores", "kind", "sample")}
@@ -355,7 +454,19 @@ def main():
     if args.forcings != M:
         M = args.forcings
         WORKLOAD = "FOM rank-2 FP64, 1000 theta x 2000 r grid, M=%d forcings" % M
-    if args.impl == "reference":
+    if args.profile_rom:
+        import numpy as np
+        import shaw_gb300 as shaw
+        shaw.build()
+        prec = {"ozaki": shaw.MIXED_OZAKI_BF16, "tf32x3": shaw.MIXED_TF32X3, "fp64": shaw.FP64}[args.profile_rom]
+        av, as_ = stable_rom(np, 512, 7, 0.004, 0.2)
+        rng = np.random.default_rng(8)
+        r = shaw.Rom(av, as_, rng.standard_normal((512, 4096)) * 1e-3, rank=2, precision=prec)
+        r.set_signals("gaussDer", rng.uniform(30.0, 90.0, 4096), 180.0)
+        r.run(0.5, args.steps)
+        print(json.dumps({"profile_rom": args.profile_rom, "steps": args.steps, "launches": r.kernel_launches}))
+        r.close()
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

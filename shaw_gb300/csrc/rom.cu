@@ -88,8 +88,8 @@ struct RomArgs {
   const double* b;    // kv (rank-1 forcing vector)
   double* xv;         // kv  (initial state in, final state out)
   double* xs;         // ks
-  int kind;
-  double period, delay, dt;
+  const double* fdt;  // [nsteps]: f(t_{n-1}) * dt of the launch's steps
+  double dt;
   uint32_t kv, ks, rows_v, rows_s;  // rows per CTA
   unsigned long long step0, nsteps;
   uint32_t fvp, fsp;
@@ -98,6 +98,7 @@ struct RomArgs {
   unsigned long long Tvp, Tsp;
   uint32_t R, fseis;
   const double* phi_rcv;  // R x kv row-major (PhiVp[gid_r, :])
+  const void* phi_rcv_t;  // the same rows as the kernel's element type (double, or df for the mixed form)
   double* seis;           // R x Tseis
   unsigned long long Tseis;
 };
@@ -187,8 +188,9 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
 
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
     const unsigned long long n = a.step0 + it + 1;
-    // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt
-    const double fdt = shaw::signal_value(a.kind, a.delay, a.period, (double)(n - 1) * a.dt) * a.dt;
+    // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt, from the table filled before the launch
+    // (RankOneForcing keeps the whole signal time series too: forcing_rank_one.hpp:169-178)
+    const double fdt = a.fdt[it];
     // 1. velocity rows of this CTA
     for (uint32_t r = v0 + warp; r < v1; r += kRomWarps) {
       const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
@@ -207,11 +209,10 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
     // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185)
     if (a.fseis && n % a.fseis == 0) {
       for (uint32_t r = crank * kRomWarps + warp; r < a.R; r += csize * kRomWarps) {
-        const double* prow = a.phi_rcv + (size_t)r * a.kv;
-        double acc = 0.0;
-        for (uint32_t k = lane; k < a.kv; k += 32) acc = fma(prow[k], A::value(xv[k]), acc);
-        acc = warp_sum(acc);
-        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = acc;
+        // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
+        const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
+        const T s = A::dot(prow, xv, a.kv, lane);
+        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = A::value(s);
       }
     }
     // 2. stress rows of this CTA
@@ -231,6 +232,18 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
   }
   for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) a.xv[r] = A::value(xv[r]);
   for (uint32_t r = s0 + threadIdx.x; r < s1; r += kRomThreads) a.xs[r] = A::value(xs[r]);
+}
+
+__global__ void rom_split_df_kernel(const double* in, df* out, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    out[e] = df_split(in[e]);
+}
+
+// table[s] = f(t) * dt at t = (step0 + s) * dt: the forcing of step step0 + s + 1.
+__global__ void rom_signal_table_kernel(int kind, double delay, double period, double dt, unsigned long long step0,
+                                        unsigned long long n, double* table) {
+  const unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (s < n) table[s] = shaw::signal_value(kind, delay, period, (double)(step0 + s) * dt) * dt;
 }
 
 // Reduced-operator block out[i * ldo + j0 + c] = sum_p phi[p + n*i] * tmp[p + n*c] for
@@ -289,6 +302,9 @@ struct shaw_rom_s {
   uint32_t R = 0;
   uint64_t fseis = 0, seis_T = 0, seis_nsteps = 0;
   double *phi_rcv = nullptr, *seis = nullptr;
+  void* phi_rcv_df = nullptr;  // receiver rows split into FP32 hi + lo (rank-1 mixed form)
+  double* fdt = nullptr;  // rank-1 forcing table of the current launch
+  uint64_t fdt_cap = 0;
   // rank-1 cluster launch shape
   uint32_t cluster = 1, rows_v = 0, rows_s = 0;
   size_t smem = 0;
@@ -312,7 +328,9 @@ int rank1_configure(RH* h) {
     const size_t bytes = rank1_smem_bytes<T>((uint32_t)h->kv, (uint32_t)h->ks, rv, rs);
     if (bytes <= budget) {
       // prefer the smallest cluster whose per-CTA row slice keeps the warps busy
-      if (rv > 64 && c < 16) continue;
+      // FP64 GEMV rows are the cost on GB300's narrow FP64 pipe: spread them over up
+      // to 16 CTAs (the cluster barrier costs less than the extra rows per CTA)
+      if (rv > 16 && c < 16) continue;
       h->cluster = c; h->rows_v = rv; h->rows_s = rs; h->smem = bytes;
       return SHAW_OK;
     }
@@ -325,11 +343,23 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   RomArgs a;
   std::memset(&a, 0, sizeof(a));
   a.Av = h->Av; a.As = h->As; a.b = h->b; a.xv = h->xv; a.xs = h->xs;
-  a.kind = h->h_kind[0]; a.period = h->h_period[0]; a.delay = h->h_delay[0]; a.dt = dt;
+  if (h->fdt_cap < nsteps) {
+    if (h->fdt) cudaFree(h->fdt);
+    h->fdt = nullptr;
+    h->fdt_cap = 0;
+    SHAW_CUDA(cudaMalloc(&h->fdt, nsteps * sizeof(double)));
+    h->fdt_cap = nsteps;
+  }
+  rom_signal_table_kernel<<<(unsigned)((nsteps + 255) / 256), 256, 0, h->stream>>>(
+      h->h_kind[0], h->h_delay[0], h->h_period[0], dt, h->step, nsteps, h->fdt);
+  h->launches++;
+  SHAW_CUDA(cudaGetLastError());
+  a.fdt = h->fdt; a.dt = dt;
   a.kv = (uint32_t)h->kv; a.ks = (uint32_t)h->ks; a.rows_v = h->rows_v; a.rows_s = h->rows_s;
   a.step0 = h->step; a.nsteps = nsteps;
   a.fvp = (uint32_t)h->fvp; a.fsp = (uint32_t)h->fsp; a.snap_vp = h->snap_vp; a.snap_sp = h->snap_sp;
   a.R = h->R; a.fseis = (uint32_t)h->fseis; a.phi_rcv = h->phi_rcv; a.seis = h->seis; a.Tseis = h->seis_T;
+  a.phi_rcv_t = MIXED ? static_cast<const void*>(h->phi_rcv_df) : static_cast<const void*>(h->phi_rcv);
   auto kern = rom_rank1_cluster_kernel<MIXED>;
   SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
   if (h->cluster > 8) SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -460,7 +490,7 @@ void shaw_rom_destroy(shaw_rom_t h) {
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
   void* bufs[] = {h->Av, h->As, h->b, h->xv, h->xs, h->kind, h->period, h->delay,
-                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis};
+                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->phi_rcv_df};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -526,6 +556,7 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   if (h->phi_rcv) { cudaFree(h->phi_rcv); h->phi_rcv = nullptr; }
+  if (h->phi_rcv_df) { cudaFree(h->phi_rcv_df); h->phi_rcv_df = nullptr; }
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
   if (R == 0) return SHAW_OK;
@@ -541,6 +572,13 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   SHAW_CUDA(cudaMemcpyAsync(h->phi_rcv, phi_rows, (size_t)R * h->kv * sizeof(double), cudaMemcpyHostToDevice,
                             h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
+  if (h->rank == 1 && h->precision == SHAW_MIXED_FP32) {
+    SHAW_CUDA(cudaMalloc(&h->phi_rcv_df, (size_t)R * h->kv * sizeof(df)));
+    rom_split_df_kernel<<<256, 256, 0, h->stream>>>(h->phi_rcv, static_cast<df*>(h->phi_rcv_df),
+                                                    (size_t)R * h->kv);
+    h->launches++;
+    SHAW_CUDA(cudaGetLastError());
+  }
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   h->R = R; h->fseis = freq; h->seis_T = T; h->seis_nsteps = nsteps;
   return SHAW_OK;

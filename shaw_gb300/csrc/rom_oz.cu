@@ -43,7 +43,10 @@ using namespace shaw::ptx;
 
 namespace {
 
-constexpr int kThreads = 256;
+// warps: 0 bulk-copy producer, 1 MMA issuer, 2 TMEM owner, 3 idle, 4..11 epilogue
+// (two groups of four: warp w reads TMEM lanes 32*(w%4).., each group half the columns)
+constexpr int kThreads = 384;
+constexpr int kEpiThreads = 256;
 constexpr int kSlices = 6;
 constexpr int kDiags = 6;                     // d = s + t in [0, 5]
 constexpr int kKc = 32;                       // BF16 K-elements per pipeline stage (64 bytes per row)
@@ -131,7 +134,10 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
         if (!mbar_wait(&sh->full[s], ph)) { raise(sh, err, 4u); break; }
         tc_fence_after();
         const uint32_t abase = smem_u32(stages + (size_t)s * C::kStage);
-        const uint32_t bbase = abase + C::kABytes;
+        // descriptors of the stage's first A / B slice; the others differ only in the
+        // start-address field (16-byte units, no carry: shared addresses < 256 KB)
+        const uint64_t adesc0 = smem_desc(abase, 128, 512);
+        const uint64_t bdesc0 = smem_desc(abase + C::kABytes, 128, 512);
 #pragma unroll
         for (uint32_t k = 0; k < kKc / 16; ++k) {
 #pragma unroll
@@ -139,8 +145,8 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
 #pragma unroll
             for (int sa = 0; sa <= d; ++sa) {
               const int tb = d - sa;
-              const uint64_t adesc = smem_desc(abase + sa * kATile + k * 256, 128, 512);
-              const uint64_t bdesc = smem_desc(bbase + tb * C::kBTile + k * 256, 128, 512);
+              const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
+              const uint64_t bdesc = bdesc0 + ((tb * C::kBTile + k * 256) >> 4);
               mma_f16(sh->tmem + d * NB, adesc, bdesc, idesc, (c > 0 || k > 0 || sa > 0) ? 1u : 0u);
             }
           }
@@ -162,21 +168,32 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
   mtc += n_mt;
 }
 
-// Read the 6 diagonal accumulators of 8 columns for this thread's row and combine
-// them exactly into y (double-float), unscaled.
+// 2^e as an FP32 factor pair (e may leave the normal range of one factor).
+__device__ __forceinline__ void pow2_pair(int e, float& f1, float& f2) {
+  const int e1 = e / 2, e2 = e - e1;
+  f1 = __int_as_float((e1 + 127) << 23);
+  f2 = __int_as_float((e2 + 127) << 23);
+}
+
+// Read the 6 diagonal accumulators of 8 columns for this thread's row (TMEM lanes of
+// quarter q) and combine them exactly: every D_d is an integer below 2^24, so
+// Y = sum_d D_d * 2^(6(5-d)) is an exact int64 and y = Y * 2^-42 (before scaling).
+// Returns y as a double-float pair.
 template <int NB>
-__device__ __forceinline__ void load_combine8(uint32_t tmem, int ew, uint32_t j0, float* yh, float* yl) {
+__device__ __forceinline__ void load_combine8(uint32_t tmem, int q, uint32_t j0, float* yh, float* yl) {
   float D[kDiags][8];
 #pragma unroll
-  for (int d = 0; d < kDiags; ++d) tmem_ld8(tmem + ((uint32_t)(ew * 32) << 16) + d * NB + j0, D[d]);
+  for (int d = 0; d < kDiags; ++d) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + d * NB + j0, D[d]);
   tmem_wait_ld();
 #pragma unroll
   for (int jj = 0; jj < 8; ++jj) {
-    float h = 0.f, l = 0.f;
+    long long Y = 0;
 #pragma unroll
-    for (int d = kDiags - 1; d >= 0; --d) df_add1(h, l, ldexpf(D[d][jj], -6 * (d + 2)));
-    yh[jj] = h;
-    yl[jj] = l;
+    for (int d = 0; d < kDiags; ++d) Y += (long long)__float2int_rn(D[d][jj]) << (6 * (kDiags - 1 - d));
+    const float h = __ll2float_rn(Y);
+    const float l = __ll2float_rn(Y - __float2ll_rn(h));
+    yh[jj] = h * 0x1p-42f;  // exact power-of-two scalings
+    yl[jj] = l * 0x1p-42f;
   }
 }
 
@@ -187,7 +204,7 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
                                             const int* beta, uint8_t* tiles) {
   using C = Cfg<NB>;
   const uint32_t t = threadIdx.x - 128;
-  for (uint32_t e = t; e < kp * NB; e += 128) {
+  for (uint32_t e = t; e < kp * NB; e += kEpiThreads) {
     const uint32_t j = e / kp, row = e - j * kp;
     const size_t si = (size_t)(col0 + j) * kp + row;
     float vh = ldexpf(xh[si], -beta[j]), vl = ldexpf(xl[si], -beta[j]);
@@ -226,7 +243,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
   uint8_t* stages = smem;
   Shared* sh = reinterpret_cast<Shared*>(smem + kStages * C::kStage);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ew = warp - 4;
+  const int ew = warp - 4;                     // >= 0 on the epilogue warps
+  const int q = warp & 3;                      // TMEM lane quarter of this warp
+  const uint32_t jbeg = (uint32_t)((ew >> 2) * (NB / 2)), jend = jbeg + NB / 2;  // this group's columns
   const uint32_t n_mt_v = a.kvp / 128, n_mt_s = a.ksp / 128, n_kc_v = a.ksp / kKc, n_kc_s = a.kvp / kKc;
   const uint32_t col0 = blockIdx.x * NB;
   uint8_t* bvt = a.bvt + (size_t)blockIdx.x * n_kc_s * C::kBBytes;
@@ -238,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       mbar_init(&sh->empty[s], 1);
     }
     mbar_init(&sh->acc_full, 1);
-    mbar_init(&sh->acc_empty, 128);
+    mbar_init(&sh->acc_empty, kEpiThreads);
     sh->abort = 0;
     mbar_init_fence();
   }
@@ -254,14 +273,14 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
 
   // B tiles of the current XS (the state may be non-zero when advancing in pieces)
   if (ew >= 0) {
-    for (uint32_t e = threadIdx.x - 128; e < a.ksp * NB; e += 128) {
+    for (uint32_t e = threadIdx.x - 128; e < a.ksp * NB; e += kEpiThreads) {
       const uint32_t j = e / a.ksp, row = e - j * a.ksp;
       const float v = a.xsh[(size_t)(col0 + j) * a.ksp + row];
       atomicMax(&sh->colmax[j], __float_as_uint(fabsf(v)));
     }
-    asm volatile("bar.sync 1, 128;" ::: "memory");
+    asm volatile("bar.sync 1, 256;" ::: "memory");
     column_exponents<NB>(sh, sh->beta_s);
-    asm volatile("bar.sync 1, 128;" ::: "memory");
+    asm volatile("bar.sync 1, 256;" ::: "memory");
     slice_state<NB>(a.xsh, a.xsl, a.ksp, col0, sh->beta_s, bst);
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
@@ -279,22 +298,24 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
                          ? signal_value(a.kind[col], a.delay[col], a.period[col], (double)(n - 1) * a.dt) * a.dt
                          : 0.0;
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
     }
     // ---------------- velocity: XV += dt Av XS + fdt b ----------------
     gemm_phase<NB>(stages, sh, a.Av, bst, n_mt_v, n_kc_v, it, mtc, a.error, [&](uint32_t mt) {
-      const uint32_t row = mt * 128 + ew * 32 + lane;
+      const uint32_t row = mt * 128 + q * 32 + lane;
       const int alpha = a.alpha_v[row];
-      for (uint32_t j0 = 0; j0 < NB; j0 += 8) {
+      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
         float yh[8], yl[8];
-        load_combine8<NB>(sh->tmem, ew, j0, yh, yl);
+        load_combine8<NB>(sh->tmem, q, j0, yh, yl);
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
           const uint32_t j = j0 + jj, col = col0 + j;
           const int e = alpha + sh->beta_s[j];
           const size_t si = (size_t)col * a.kvp + row;
           float xh = a.xvh[si], xl = a.xvl[si];
-          df_fma(xh, xl, dth, dtl, ldexpf(yh[jj], e), ldexpf(yl[jj], e));
+          float s1, s2;
+          pow2_pair(e, s1, s2);
+          df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
           const double f = sh->fdt[j];
           const float fh = (float)f, fl = (float)(f - (double)fh);
           df_fma(xh, xl, fh, fl, a.bh[si], a.bl[si]);
@@ -307,9 +328,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       }
     });
     if (ew >= 0) {
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
       column_exponents<NB>(sh, sh->beta_v);
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
       if (!sh->abort) slice_state<NB>(a.xvh, a.xvl, a.kvp, col0, sh->beta_v, bvt);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
@@ -317,18 +338,20 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     if (sh->abort) break;
     // ---------------- stress: XS += dt As XV ----------------
     gemm_phase<NB>(stages, sh, a.As, bvt, n_mt_s, n_kc_s, it, mtc, a.error, [&](uint32_t mt) {
-      const uint32_t row = mt * 128 + ew * 32 + lane;
+      const uint32_t row = mt * 128 + q * 32 + lane;
       const int alpha = a.alpha_s[row];
-      for (uint32_t j0 = 0; j0 < NB; j0 += 8) {
+      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
         float yh[8], yl[8];
-        load_combine8<NB>(sh->tmem, ew, j0, yh, yl);
+        load_combine8<NB>(sh->tmem, q, j0, yh, yl);
 #pragma unroll
         for (int jj = 0; jj < 8; ++jj) {
           const uint32_t j = j0 + jj, col = col0 + j;
           const int e = alpha + sh->beta_v[j];
           const size_t si = (size_t)col * a.ksp + row;
           float xh = a.xsh[si], xl = a.xsl[si];
-          df_fma(xh, xl, dth, dtl, ldexpf(yh[jj], e), ldexpf(yl[jj], e));
+          float s1, s2;
+          pow2_pair(e, s1, s2);
+          df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
           a.xsh[si] = xh;
           a.xsl[si] = xl;
           note_max(sh, j, xh);
@@ -338,9 +361,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       }
     });
     if (ew >= 0) {
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
       column_exponents<NB>(sh, sh->beta_s);
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, 256;" ::: "memory");
       if (!sh->abort) slice_state<NB>(a.xsh, a.xsl, a.ksp, col0, sh->beta_s, bst);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
