@@ -269,6 +269,26 @@ int shaw_run_input_file(const char* yaml_path);
  * with the reference's message on invalid input. */
 int shaw_parse_input(const char* yaml_path, char* out, size_t cap);
 
+/* ---- POD: thin SVD of a snapshot matrix ------------------------------------
+ * Replaces doThinSVDm0 (method 1, BDCSVD) and doThinSVDm1 (method 2, Householder
+ * QR then SVD of R) of src/tools/main_eigen_svd.cc:113-197.  snaps is the host
+ * n x t snapshot matrix (LayoutLeft, one snapshot per column); on return lsv holds
+ * the n x min(n,t) left singular vectors (LayoutLeft) and sv the min(n,t) singular
+ * values in decreasing order.  Computed in FP64 on the GPU (QR, SVD of the triangle,
+ * back-transformation).  Each singular vector is determined up to its sign: compare
+ * subspaces, not raw vectors, with the reference's output.  Method 2 needs n >= t
+ * (SHAW_ERR_UNSUPPORTED otherwise), as in the reference. */
+int shaw_pod(const double* snaps, uint64_t n, uint64_t t, int method, double* lsv, double* sv);
+/* computeThinSVD --dirs ... --informat ... --outformat ... --method ...
+ * (main_eigen_svd.cc:199-305): for "vp" then "sp", concatenate the columns of
+ * <dir>/snaps_<dof>_0 over dirs, run shaw_pod, write sva_<dof> (text, one value per
+ * line, 17 significant digits) and lsv_<dof> (binary with size_t extents) into the
+ * current directory.  As in the reference, the snapshot reader receives the
+ * `outformat` string (main_eigen_svd.cc:302 passes the two formats in swapped order)
+ * and reads only "binary"; the sva/lsv formats do not depend on either string. */
+int shaw_pod_tool(const char* const* dirs, uint32_t ndirs, const char* informat, const char* outformat,
+                  int method);
+
 #ifdef __cplusplus
 }
 #endif

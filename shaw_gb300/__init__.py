@@ -20,6 +20,7 @@ from . import build as _build_mod
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libshaw_gpu.so")
 EXE_PATH = os.path.join(_HERE, "_build", "shaw_exe")
+POD_EXE_PATH = os.path.join(_HERE, "_build", "computeThinSVD")
 
 OK = 0
 ERR_INVALID_ARG = 1
@@ -48,7 +49,7 @@ class ShawError(RuntimeError):
 
 
 def build():
-    """Compile libshaw_gpu.so and shaw_exe for sm_103a (idempotent)."""
+    """Compile libshaw_gpu.so, shaw_exe and computeThinSVD for sm_103a (idempotent)."""
     return _build_mod.build()
 
 
@@ -90,6 +91,9 @@ SIGNATURES = [
     ("shaw_fom_kernel_launches", ctypes.c_uint64, [_vp]),
     ("shaw_rom_project", ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _dp, ctypes.c_uint64, _dp, _dp]),
     ("shaw_rom_project_noalloc", ctypes.c_int, [_vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64, _vp, _vp, _vp]),
+    ("shaw_pod", ctypes.c_int, [_dp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _dp, _dp]),
+    ("shaw_pod_tool", ctypes.c_int, [ctypes.POINTER(ctypes.c_char_p), ctypes.c_uint32, ctypes.c_char_p,
+                                     ctypes.c_char_p, ctypes.c_int]),
     ("shaw_rom_create", ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _dp, _dp, ctypes.c_int, ctypes.c_uint32,
                                        _dp, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("shaw_rom_destroy", None, [_vp]),
@@ -342,6 +346,26 @@ def rom_project(fom, phi_vp, phi_sp):
     as_ = np.zeros((ks, kv))
     _check(lib().shaw_rom_project(fom.h, _p(pv, _dp), kv, _p(ps, _dp), ks, _p(av, _dp), _p(as_, _dp)))
     return av, as_
+
+
+def pod(snaps, method=2):
+    """Thin SVD of the n x t snapshot matrix on the GPU (computeThinSVD,
+    src/tools/main_eigen_svd.cc:113-197): returns (U n x min(n,t), singular values).
+    Each column of U is determined up to its sign."""
+    a = np.asfortranarray(snaps, np.float64)
+    n, t = a.shape
+    k = min(n, t)
+    u = np.zeros((n, k), order="F")
+    sv = np.zeros(k)
+    _check(lib().shaw_pod(_p(a, _dp), n, t, method, _p(u, _dp), _p(sv, _dp)))
+    return u, sv
+
+
+def pod_tool(dirs, informat="binary", outformat="binary", method=2):
+    """computeThinSVD --dirs ... --informat ... --outformat ... --method ...: writes
+    sva_vp, lsv_vp, sva_sp, lsv_sp into the current directory."""
+    arr = (ctypes.c_char_p * len(dirs))(*[os.fsencode(d) for d in dirs])
+    _check(lib().shaw_pod_tool(arr, len(dirs), informat.encode(), outformat.encode(), method))
 
 
 class Rom:

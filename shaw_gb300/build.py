@@ -16,10 +16,11 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(BUILD, "libshaw_gpu.so")
 EXE = os.path.join(BUILD, "shaw_exe")
+POD_EXE = os.path.join(BUILD, "computeThinSVD")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["fom.cu", "rom.cu", "rom_tc.cu", "rom_oz.cu"]
-CPP_SOURCES = ["host.cpp", "driver.cpp", "rom_driver.cpp", "yaml_lite.cpp"]
+CU_SOURCES = ["fom.cu", "rom.cu", "rom_tc.cu", "rom_oz.cu", "pod.cu"]
+CPP_SOURCES = ["host.cpp", "driver.cpp", "rom_driver.cpp", "pod_driver.cpp", "yaml_lite.cpp"]
 
 
 def _nvcc():
@@ -81,13 +82,14 @@ def build(verbose=False, ptxas_info=False):
             if o.strip():
                 print(o)
     if jobs or not os.path.exists(LIB):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas"])
-    main_o = os.path.join(BUILD, "main.cpp.o")
-    main_s = os.path.join(CSRC, "main.cpp")
-    if _stale(main_o, [main_s] + headers):
-        _run(["g++", "-O3", "-std=c++17", "-I", INCLUDE, "-c", main_s, "-o", main_o])
-    if _stale(EXE, [main_o, LIB]):
-        _run(["g++", "-o", EXE, main_o, "-L", BUILD, "-lshaw_gpu", "-Wl,-rpath,$ORIGIN"])
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas", "-lcusolver"])
+    for src, exe in (("main.cpp", EXE), ("pod_main.cpp", POD_EXE)):
+        obj = os.path.join(BUILD, src + ".o")
+        s = os.path.join(CSRC, src)
+        if _stale(obj, [s] + headers):
+            _run(["g++", "-O3", "-std=c++17", "-I", INCLUDE, "-c", s, "-o", obj])
+        if _stale(exe, [obj, LIB]):
+            _run(["g++", "-o", exe, obj, "-L", BUILD, "-lshaw_gpu", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
