@@ -271,7 +271,57 @@ def extra_workloads(np, torch, shaw):
         "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
         "operators": "seeded synthetic pair with As = -Av^T (bounded leapfrog), dt*sigma in [0.002, 0.1]"}
+    out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw)
     return out
+
+
+def batched_workload(np, torch, shaw, n_inst=64, seed=20261205):
+    """64 reduced systems, k ~ U{64, 128, ..., 1024}, M ~ U[16, 2048] (seeded), advanced
+    together: FP64 (cuBLAS DGEMM per instance) vs the Ozaki tensor-core batch (one
+    persistent launch, autotuned tile widths and schedule)."""
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(1, 17, n_inst) * 64
+    Ms = rng.integers(16, 2049, n_inst)
+    insts = []
+    for i, (k, M) in enumerate(zip(ks, Ms)):
+        av, as_ = stable_rom(np, int(k), seed + i, 0.004, 0.2)
+        insts.append(dict(rom_jvp=av, rom_jsp=as_, b=rng.standard_normal((k, M)) * 1e-3, kind="gaussDer",
+                          period=rng.uniform(30.0, 90.0, M), delay=180.0))
+    flops = float(sum(4.0 * k * k * M for k, M in zip(ks, Ms)))
+    cols = int(Ms.sum())
+    dtr, n64, n_oz, n_cmp = 0.5, 6, 120, 6
+    rows = {i: np.random.default_rng(i).standard_normal((181, int(ks[i]))) / np.sqrt(ks[i]) for i in range(n_inst)}
+    res = {}
+    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
+        bt = shaw.RomBatch(insts, precision=prec)
+        report = bt.tune(dtr, 4) if prec != shaw.FP64 else ""
+        bt.reset()
+        bt.advance(dtr, 2)  # warm-up
+        bt.synchronize()
+        bt.reset()
+        n = n64 if prec == shaw.FP64 else n_oz
+        l0 = bt.kernel_launches
+        t = _timed(torch, bt.stream, lambda: bt.advance(dtr, n))
+        bt.synchronize()
+        launches = bt.kernel_launches - l0
+        # states after n_cmp steps for the accuracy comparison
+        bt.reset()
+        bt.advance(dtr, n_cmp)
+        bt.synchronize()
+        seis = [rows[i] @ bt.get_state(i)[0] for i in range(n_inst)]
+        res[prec] = dict(t=t, n=n, seis=seis, describe=bt.describe(), report=report, launches=launches)
+        bt.close()
+    r64, roz = res[shaw.FP64], res[shaw.MIXED_OZAKI_BF16]
+    err = max(_relerr(np, a, b) for a, b in zip(roz["seis"], r64["seis"]))
+    v64, voz = cols * r64["n"] / r64["t"], cols * roz["n"] / roz["t"]
+    return {"metric": "ROM forcing-steps/s", "instances": n_inst, "total_forcings": cols,
+            "k_range": [int(ks.min()), int(ks.max())], "M_range": [int(Ms.min()), int(Ms.max())],
+            "fp64": v64, "ozaki_bf16": voz, "speedup_ozaki": voz / v64,
+            "fp64_steps": r64["n"], "ozaki_steps": roz["n"], "ozaki_launches": roz["launches"],
+            "algorithmic_tflops_fp64": flops * r64["n"] / r64["t"] / 1e12,
+            "algorithmic_tflops_ozaki": flops * roz["n"] / roz["t"] / 1e12,
+            "seismogram_rel_err_ozaki": err, "error_after_steps": n_cmp,
+            "tiling": roz["describe"], "autotuner": roz["report"].strip().split("\n")}
 
 
 def run_reference(args):

@@ -215,6 +215,48 @@ int shaw_rom_get_seismogram(shaw_rom_t h, double* out);
 void* shaw_rom_stream(shaw_rom_t h);
 uint64_t shaw_rom_kernel_launches(shaw_rom_t h);
 
+/* ---- Batched ROM: many rank-2 reduced systems of uneven size ---------------
+ * No counterpart in the reference, which runs one reduced system per process
+ * (runRomRankTwoForcing, src/kokkos/torevise/run_rom_rank_two_forcing.hpp:119-201).
+ * Every instance is that system with its own kv, ks, operators, forcing vectors b
+ * (kv x M LayoutLeft, column j = rhoInv[src_j] PhiVp[src_j, :]) and per-column
+ * signals; all advance with one dt.  precision: SHAW_FP64 (cuBLAS DGEMMs per
+ * instance) or SHAW_MIXED_OZAKI_BF16 (all instances, all steps, one persistent
+ * tensor-core launch; kv, ks <= 1024). */
+typedef struct shaw_rom_batch_s* shaw_rom_batch_t;
+typedef struct {
+  uint64_t kv, ks;
+  uint32_t num_forcings;
+  const double* rom_jvp; /* kv x ks row-major */
+  const double* rom_jsp; /* ks x kv row-major */
+  const double* b;       /* kv x num_forcings LayoutLeft */
+  const int32_t* kind;   /* num_forcings signal kinds, periods and delays */
+  const double* period;
+  const double* delay;
+} shaw_rom_instance_desc;
+int shaw_rom_batch_create(uint32_t num_instances, const shaw_rom_instance_desc* inst, int precision,
+                          shaw_rom_batch_t* out);
+void shaw_rom_batch_destroy(shaw_rom_batch_t h);
+/* Autotuner (tensor-core batches): times tile widths of 16, 32 and 64 forcing columns,
+ * each with a model-cost and a measured-cost longest-first schedule, over trial_steps
+ * steps; keeps the fastest and leaves the batch reset.  A report of the candidates
+ * goes to report[cap] (may be NULL). */
+int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, char* report, size_t cap);
+/* Reduced-state snapshots of instance i: kv x (nsteps/freq_vp) x M and
+ * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */
+int shaw_rom_batch_set_snapshots(shaw_rom_batch_t h, uint32_t i, uint64_t freq_vp, uint64_t freq_sp,
+                                 uint64_t nsteps, double* host_vp, double* host_sp);
+int shaw_rom_batch_reset(shaw_rom_batch_t h);
+int shaw_rom_batch_advance(shaw_rom_batch_t h, double dt, uint64_t nsteps);
+int shaw_rom_batch_run(shaw_rom_batch_t h, double dt, uint64_t nsteps);
+int shaw_rom_batch_synchronize(shaw_rom_batch_t h);
+/* States of instance i: xv kv x M, xs ks x M (LayoutLeft, host arrays). */
+int shaw_rom_batch_get_state(shaw_rom_batch_t h, uint32_t i, double* xv, double* xs);
+int shaw_rom_batch_describe(shaw_rom_batch_t h, char* out, size_t cap);
+void* shaw_rom_batch_stream(shaw_rom_batch_t h);
+uint64_t shaw_rom_batch_kernel_launches(shaw_rom_batch_t h);
+uint64_t shaw_rom_batch_step(shaw_rom_batch_t h);
+
 /* ======================================================================== *
  *  Host-side setup (the reference's main.cc + MeshInfo + material + mappers) *
  * ======================================================================== */

@@ -91,6 +91,20 @@ SIGNATURES = [
     ("shaw_fom_kernel_launches", ctypes.c_uint64, [_vp]),
     ("shaw_rom_project", ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _dp, ctypes.c_uint64, _dp, _dp]),
     ("shaw_rom_project_noalloc", ctypes.c_int, [_vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64, _vp, _vp, _vp]),
+    ("shaw_rom_batch_create", ctypes.c_int, [ctypes.c_uint32, _vp, ctypes.c_int, ctypes.POINTER(_vp)]),
+    ("shaw_rom_batch_destroy", None, [_vp]),
+    ("shaw_rom_batch_tune", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_size_t]),
+    ("shaw_rom_batch_set_snapshots", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
+                                                    ctypes.c_uint64, _dp, _dp]),
+    ("shaw_rom_batch_reset", ctypes.c_int, [_vp]),
+    ("shaw_rom_batch_advance", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
+    ("shaw_rom_batch_run", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
+    ("shaw_rom_batch_synchronize", ctypes.c_int, [_vp]),
+    ("shaw_rom_batch_get_state", ctypes.c_int, [_vp, ctypes.c_uint32, _dp, _dp]),
+    ("shaw_rom_batch_describe", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_size_t]),
+    ("shaw_rom_batch_stream", _vp, [_vp]),
+    ("shaw_rom_batch_kernel_launches", ctypes.c_uint64, [_vp]),
+    ("shaw_rom_batch_step", ctypes.c_uint64, [_vp]),
     ("shaw_pod", ctypes.c_int, [_dp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _dp, _dp]),
     ("shaw_pod_tool", ctypes.c_int, [ctypes.POINTER(ctypes.c_char_p), ctypes.c_uint32, ctypes.c_char_p,
                                      ctypes.c_char_p, ctypes.c_int]),
@@ -346,6 +360,98 @@ def rom_project(fom, phi_vp, phi_sp):
     as_ = np.zeros((ks, kv))
     _check(lib().shaw_rom_project(fom.h, _p(pv, _dp), kv, _p(ps, _dp), ks, _p(av, _dp), _p(as_, _dp)))
     return av, as_
+
+
+class RomInstanceDesc(ctypes.Structure):
+    _fields_ = [("kv", ctypes.c_uint64), ("ks", ctypes.c_uint64), ("num_forcings", ctypes.c_uint32),
+                ("rom_jvp", _dp), ("rom_jsp", _dp), ("b", _dp), ("kind", _i32p), ("period", _dp), ("delay", _dp)]
+
+
+class RomBatch:
+    """Many rank-2 reduced systems of uneven size advanced together on the GPU.
+
+    instances: sequence of dicts with keys rom_jvp (kv x ks), rom_jsp (ks x kv), b
+    (kv x M) and the per-column signals kind, period, delay (scalars broadcast)."""
+
+    def __init__(self, instances, precision=FP64):
+        self._keep = []
+        descs = (RomInstanceDesc * len(instances))()
+        self.shapes = []
+        for d, inst in zip(descs, instances):
+            av = np.ascontiguousarray(inst["rom_jvp"], np.float64)
+            as_ = np.ascontiguousarray(inst["rom_jsp"], np.float64)
+            kv, ks = av.shape
+            b = np.asfortranarray(np.asarray(inst["b"], np.float64).reshape(kv, -1, order="F"))
+            M = b.shape[1]
+            k = np.ascontiguousarray(np.broadcast_to(
+                np.asarray([SIGNAL.get(x, x) for x in np.atleast_1d(inst.get("kind", "gaussDer"))], np.int32), (M,)))
+            p = np.ascontiguousarray(np.broadcast_to(np.asarray(inst["period"], np.float64), (M,)))
+            dl = np.ascontiguousarray(np.broadcast_to(np.asarray(inst.get("delay", 0.0), np.float64), (M,)))
+            self._keep += [av, as_, b, k, p, dl]
+            d.kv, d.ks, d.num_forcings = kv, ks, M
+            d.rom_jvp, d.rom_jsp, d.b = _p(av, _dp), _p(as_, _dp), _p(b, _dp)
+            d.kind, d.period, d.delay = _p(k, _i32p), _p(p, _dp), _p(dl, _dp)
+            self.shapes.append((kv, ks, M))
+        h = _vp()
+        _check(lib().shaw_rom_batch_create(len(instances), ctypes.cast(descs, _vp), precision, ctypes.byref(h)))
+        self.h = h
+        self._keep = []
+        self._snaps = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().shaw_rom_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def tune(self, dt, trial_steps=4):
+        buf = ctypes.create_string_buffer(4096)
+        _check(lib().shaw_rom_batch_tune(self.h, dt, trial_steps, buf, len(buf)))
+        return buf.value.decode()
+
+    def describe(self):
+        buf = ctypes.create_string_buffer(512)
+        _check(lib().shaw_rom_batch_describe(self.h, buf, len(buf)))
+        return buf.value.decode()
+
+    def set_snapshots(self, i, freq_vp, freq_sp, nsteps):
+        kv, ks, M = self.shapes[i]
+        svp = np.zeros((kv, nsteps // freq_vp, M), order="F")
+        ssp = np.zeros((ks, nsteps // freq_sp, M), order="F")
+        _check(lib().shaw_rom_batch_set_snapshots(self.h, i, freq_vp, freq_sp, nsteps, _p(svp, _dp), _p(ssp, _dp)))
+        self._snaps[i] = (svp, ssp)
+
+    def snapshots(self, i):
+        return self._snaps[i]
+
+    def reset(self):
+        _check(lib().shaw_rom_batch_reset(self.h))
+
+    def advance(self, dt, nsteps):
+        _check(lib().shaw_rom_batch_advance(self.h, dt, nsteps))
+
+    def run(self, dt, nsteps):
+        _check(lib().shaw_rom_batch_run(self.h, dt, nsteps))
+
+    def synchronize(self):
+        _check(lib().shaw_rom_batch_synchronize(self.h))
+
+    def get_state(self, i):
+        kv, ks, M = self.shapes[i]
+        xv = np.zeros((kv, M), order="F")
+        xs = np.zeros((ks, M), order="F")
+        _check(lib().shaw_rom_batch_get_state(self.h, i, _p(xv, _dp), _p(xs, _dp)))
+        return xv, xs
+
+    @property
+    def stream(self):
+        return lib().shaw_rom_batch_stream(self.h)
+
+    @property
+    def kernel_launches(self):
+        return lib().shaw_rom_batch_kernel_launches(self.h)
 
 
 def pod(snaps, method=2):

@@ -285,7 +285,7 @@ struct shaw_rom_s {
   uint32_t M = 1;
   int rank = 1, precision = SHAW_FP64;
   shaw::tc::Plan* tc = nullptr;  // rank-2 tensor-core TF32x3 path
-  shaw::oz::Plan* oz = nullptr;  // rank-2 tensor-core Ozaki BF16 path
+  shaw::oz::Batch* oz = nullptr;  // rank-2 tensor-core Ozaki BF16 path (a batch of one)
   bool persistent2() const { return tc != nullptr || oz != nullptr; }
   cudaStream_t stream = nullptr;
   cublasHandle_t blas = nullptr;
@@ -466,7 +466,10 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
     if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = shaw::fail(SHAW_ERR_CUDA, "tensor-core ROM setup failed");
   } else if (precision == SHAW_MIXED_OZAKI_BF16) {
-    rc = shaw::oz::create(h->oz, (uint32_t)kv, (uint32_t)ks, Av, As, M, b, h->stream);
+    shaw::oz::InstanceDesc d;
+    d.kv = (uint32_t)kv; d.ks = (uint32_t)ks; d.M = M; d.Av = Av; d.As = As; d.b = b;
+    rc = shaw::oz::create(h->oz, 1, &d, h->stream);
+    if (rc == SHAW_OK) rc = shaw::oz::set_signals(h->oz, 0, h->kind, h->period, h->delay);
     if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = shaw::fail(SHAW_ERR_CUDA, "Ozaki tensor-core ROM setup failed");
   } else {
@@ -615,10 +618,13 @@ int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
   }
   if (h->tc || h->oz) {
     const unsigned long long Tv = h->fvp ? h->snap_nsteps / h->fvp : 0, Ts = h->fsp ? h->snap_nsteps / h->fsp : 0;
-    rc = h->tc ? shaw::tc::advance(h->tc, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay,
-                                   h->snap_vp, h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp)
-               : shaw::oz::advance(h->oz, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay,
-                                   h->snap_vp, h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp);
+    if (h->tc) {
+      rc = shaw::tc::advance(h->tc, h->stream, dt, h->step, nsteps, h->kind, h->period, h->delay, h->snap_vp,
+                             h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp);
+    } else {
+      rc = shaw::oz::set_snapshots(h->oz, 0, h->snap_vp, h->snap_sp, Tv, Ts, (uint32_t)h->fvp, (uint32_t)h->fsp);
+      if (rc == SHAW_OK) rc = shaw::oz::advance(h->oz, h->stream, dt, h->step, nsteps);
+    }
     if (rc) return rc;
     h->launches++;
     h->step += nsteps;
@@ -669,7 +675,7 @@ int shaw_rom_get_state(shaw_rom_t h, double* xv, double* xs) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (h->tc || h->oz) {
     const int rc = h->tc ? shaw::tc::get_state(h->tc, h->stream, h->xv, h->xs)
-                         : shaw::oz::get_state(h->oz, h->stream, h->xv, h->xs);
+                         : shaw::oz::get_state(h->oz, 0, h->stream, h->xv, h->xs);
     if (rc) return rc;
   }
   SHAW_CUDA(cudaStreamSynchronize(h->stream));

@@ -1,5 +1,6 @@
 // rom_oz.cu -- rank-2 ROM leapfrog with FP64-grade reduced GEMMs on the BF16 tensor
-// cores (tcgen05, kind::f16), using the Ozaki splitting scheme with exact accumulation.
+// cores (tcgen05, kind::f16), using the Ozaki splitting scheme with exact accumulation,
+// for one reduced system or a batch of uneven ones in a single persistent launch.
 //
 // Reference: runRomRankTwoForcing (src/kokkos/torevise/run_rom_rank_two_forcing.hpp:149-188)
 //   XV += dt Av XS ;  XV[:,j] += (f_j dt) b[:,j] ;  XS += dt As XV
@@ -16,19 +17,28 @@
 //     diagonal d = s + t (up to 6 pairs) below 2^24: the FP32 accumulators in TMEM
 //     hold every partial sum exactly, whatever their rounding mode;
 //   * pairs with s + t <= 5 (21 MMAs per K-step) give ~2^-36 relative accuracy; the 6
-//     diagonal sums are combined in the epilogue in FP32 double-float and scaled back.
-// State: FP32 hi + lo pairs (compensated) in global memory; the epilogue re-slices
-// the new state into the next GEMM's BF16 B tiles after each half-step.
-// Each CTA owns NB forcing columns and runs the whole time loop (persistent).
-// All waits are bounded: a wait that runs out sets an error flag, the kernel leaves
-// its loop, releases TMEM and returns.
+//     diagonal sums are combined exactly in int64 in the epilogue and scaled back.
+// State: FP32 hi + lo pairs (compensated) in global memory; the epilogue re-slices the
+// new state into the next GEMM's BF16 B tiles after each half-step.
+//
+// Work decomposition: forcing columns are independent for the whole run, so the unit
+// of work is a TILE = (instance, block of nb columns), advanced through all time steps
+// by one CTA.  A persistent grid of at most one CTA per SM runs a host-built schedule:
+// CTA c advances the tiles order[cta_begin[c] .. cta_begin[c+1]) one after another.
+// Tile widths nb in {16, 32, 64} and the schedule (longest-processing-time-first over
+// modelled or measured tile costs) are picked by the autotuner `tune`.
+// All waits are bounded: a wait that runs out sets an error flag, the kernel leaves its
+// loops at the next block-wide vote, releases TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
+#include <numeric>
+#include <queue>
 #include <string>
 #include <vector>
 
@@ -52,16 +62,15 @@ constexpr int kDiags = 6;                     // d = s + t in [0, 5]
 constexpr int kKc = 32;                       // BF16 K-elements per pipeline stage (64 bytes per row)
 constexpr uint32_t kRowBytes = kKc * 2;
 constexpr uint32_t kATile = 128 * kRowBytes;  // one slice of a 128 x 32 operator tile: 8 KB
+constexpr uint32_t kABytes = kSlices * kATile;
+constexpr uint32_t kMaxNb = 64;
+constexpr uint32_t kStageBytes = kABytes + kSlices * kMaxNb * kRowBytes;  // 72 KB
 constexpr int kStages = 3;
+constexpr uint32_t kTmemCols = 512;           // two accumulator sets at columns 0 and 256 when 6 nb <= 256
 
-template <int NB>
-struct Cfg {
-  static constexpr uint32_t kBTile = NB * kRowBytes;
-  static constexpr uint32_t kABytes = kSlices * kATile;
-  static constexpr uint32_t kBBytes = kSlices * kBTile;
-  static constexpr uint32_t kStage = kABytes + kBBytes;
-  static constexpr uint32_t kTmemCols = (kDiags * NB <= 256) ? 256 : 512;
-};
+__host__ __device__ constexpr uint32_t btile_bytes(uint32_t nb) { return nb * kRowBytes; }
+__host__ __device__ constexpr uint32_t bstage_bytes(uint32_t nb) { return kSlices * nb * kRowBytes; }
+__host__ __device__ constexpr uint32_t acc_buffers(uint32_t nb) { return (kDiags * nb <= 256) ? 2u : 1u; }
 
 // Byte offset of (row r, k) in a K-major, no-swizzle BF16 tile of 32 K-elements:
 // core matrices of 8 rows x 16 bytes, K-direction stride 128 B, 8-row-group stride 512 B.
@@ -69,7 +78,8 @@ __host__ __device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k) {
   return (((r >> 3) * 4u + (k >> 3)) << 7) + ((r & 7u) << 4) + ((k & 7u) << 1);
 }
 
-struct OzArgs {
+// One reduced system on the device.
+struct OzInst {
   const uint8_t* Av;  // [kvp/128][ksp/32][slice][8 KB]
   const uint8_t* As;  // [ksp/128][kvp/32][slice][8 KB]
   const int* alpha_v;
@@ -77,27 +87,42 @@ struct OzArgs {
   const float* bh;
   const float* bl;  // [Mp][kvp]
   float *xvh, *xvl, *xsh, *xsl;
-  uint8_t* bvt;  // per CTA [kvp/32][slice][NB x 64 B]: slices of XV (B of the stress GEMM)
-  uint8_t* bst;  // per CTA [ksp/32][slice][NB x 64 B]: slices of XS (B of the velocity GEMM)
   const int* kind;
   const double* period;
   const double* delay;
   double *snap_vp, *snap_sp;
   unsigned long long Tvp, Tsp;
   uint32_t fvp, fsp;
-  uint32_t kv, ks, kvp, ksp, M;
+  uint32_t kv, ks, kvp, ksp, M, Mp;
+};
+
+struct OzTile {
+  uint32_t inst, col0, nb, pad;
+};
+
+struct OzArgs {
+  const OzInst* inst;
+  const OzTile* tiles;
+  const uint32_t* order;      // tile indices, grouped by CTA
+  const uint32_t* cta_begin;  // [ctas + 1]
+  uint8_t* bvt;               // per CTA: slices of XV (B of the stress GEMM)
+  uint8_t* bst;               // per CTA: slices of XS (B of the velocity GEMM)
+  size_t bscratch;            // bytes of bvt / bst per CTA
   double dt;
   unsigned long long step0, nsteps;
   unsigned int* error;
+  unsigned long long* tile_ns;  // per tile: device time of its last run
 };
 
 struct Shared {
-  uint64_t full[kStages], empty[kStages], acc_full, acc_empty;
+  uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], drain;
   uint32_t tmem;
   int abort;
-  int beta_v[64], beta_s[64];
-  unsigned int colmax[64];
-  double fdt[64];
+  int beta_v[kMaxNb], beta_s[kMaxNb];
+  unsigned int colmax[kMaxNb];
+  double fdt[kMaxNb];
+  OzInst in;
+  OzTile tile;
 };
 
 __device__ __forceinline__ void raise(Shared* sh, unsigned int* err, unsigned int code) {
@@ -105,39 +130,58 @@ __device__ __forceinline__ void raise(Shared* sh, unsigned int* err, unsigned in
   sh->abort = 1;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Accumulator set and its parity for the next M-tile; `uses` counts completed uses of
+// each set.  Every role walks the same sequence, so they agree without communicating.
+__device__ __forceinline__ void acc_next(uint32_t nbuf, uint32_t (&uses)[2], uint32_t& buf, uint32_t& par) {
+  buf = (nbuf == 2) ? ((uses[0] + uses[1]) & 1u) : 0u;
+  par = uses[buf] & 1u;
+  uses[buf]++;
+}
+
 // One GEMM phase: for every 128-row M-tile, D_d = sum over K of the slice pairs on
-// diagonal d, then the epilogue `epi(mt)` runs on warps 4..7.
-template <int NB, typename Epi>
+// diagonal d into an accumulator set; the epilogue `epi(mt, tmem_cols)` runs on warps
+// 4..11 while the MMAs of the next M-tile fill the other set.
+template <typename Epi>
 __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const uint8_t* Aop, const uint8_t* Bop,
-                                           uint32_t n_mt, uint32_t n_kc, uint32_t& it, uint32_t& mtc,
-                                           unsigned int* err, Epi epi) {
-  using C = Cfg<NB>;
+                                           uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
+                                           uint32_t (&uses)[2], unsigned int* err, Epi epi) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb), nbuf = acc_buffers(nb);
   if (warp == 0 && lane == 0) {
     for (uint32_t q = 0; q < n_mt * n_kc && !sh->abort; ++q) {
       const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
       if (!mbar_wait(&sh->empty[s], ph ^ 1u)) { raise(sh, err, 1u); break; }
       const uint32_t mt = q / n_kc, c = q - mt * n_kc;
-      uint8_t* st = stages + (size_t)s * C::kStage;
-      mbar_expect_tx(&sh->full[s], C::kStage);
-      bulk_g2s(st, Aop + ((size_t)mt * n_kc + c) * C::kABytes, C::kABytes, &sh->full[s]);
-      bulk_g2s(st + C::kABytes, Bop + (size_t)c * C::kBBytes, C::kBBytes, &sh->full[s]);
+      uint8_t* st = stages + (size_t)s * kStageBytes;
+      mbar_expect_tx(&sh->full[s], kABytes + bbytes);
+      bulk_g2s(st, Aop + ((size_t)mt * n_kc + c) * kABytes, kABytes, &sh->full[s]);
+      bulk_g2s(st + kABytes, Bop + (size_t)c * bbytes, bbytes, &sh->full[s]);
     }
   } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = idesc_bf16(NB);
+    const uint32_t idesc = idesc_bf16(nb);
+    uint32_t lu[2] = {uses[0], uses[1]};
     for (uint32_t mt = 0; mt < n_mt && !sh->abort; ++mt) {
-      if (!mbar_wait(&sh->acc_empty, ((mtc + mt) & 1u) ^ 1u)) { raise(sh, err, 2u); break; }
+      uint32_t buf, par;
+      acc_next(nbuf, lu, buf, par);
+      if (!mbar_wait(&sh->acc_empty[buf], par ^ 1u)) { raise(sh, err, 2u); break; }
       tc_fence_after();
+      const uint32_t dcol = sh->tmem + buf * 256u;
       for (uint32_t c = 0; c < n_kc && !sh->abort; ++c) {
         const uint32_t q = mt * n_kc + c;
         const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
         if (!mbar_wait(&sh->full[s], ph)) { raise(sh, err, 4u); break; }
         tc_fence_after();
-        const uint32_t abase = smem_u32(stages + (size_t)s * C::kStage);
+        const uint32_t abase = smem_u32(stages + (size_t)s * kStageBytes);
         // descriptors of the stage's first A / B slice; the others differ only in the
         // start-address field (16-byte units, no carry: shared addresses < 256 KB)
         const uint64_t adesc0 = smem_desc(abase, 128, 512);
-        const uint64_t bdesc0 = smem_desc(abase + C::kABytes, 128, 512);
+        const uint64_t bdesc0 = smem_desc(abase + kABytes, 128, 512);
 #pragma unroll
         for (uint32_t k = 0; k < kKc / 16; ++k) {
 #pragma unroll
@@ -146,26 +190,33 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
             for (int sa = 0; sa <= d; ++sa) {
               const int tb = d - sa;
               const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
-              const uint64_t bdesc = bdesc0 + ((tb * C::kBTile + k * 256) >> 4);
-              mma_f16(sh->tmem + d * NB, adesc, bdesc, idesc, (c > 0 || k > 0 || sa > 0) ? 1u : 0u);
+              const uint64_t bdesc = bdesc0 + ((tb * btile + k * 256) >> 4);
+              mma_f16(dcol + d * nb, adesc, bdesc, idesc, (c > 0 || k > 0 || sa > 0) ? 1u : 0u);
             }
           }
         }
         mma_commit(&sh->empty[s]);
       }
-      mma_commit(&sh->acc_full);
+      mma_commit(&sh->acc_full[buf]);
     }
   } else if (warp >= 4) {
+    uint32_t lu[2] = {uses[0], uses[1]};
     for (uint32_t mt = 0; mt < n_mt; ++mt) {
-      if (!mbar_wait(&sh->acc_full, (mtc + mt) & 1u)) { raise(sh, err, 8u); break; }
+      uint32_t buf, par;
+      acc_next(nbuf, lu, buf, par);
+      if (!mbar_wait(&sh->acc_full[buf], par)) { raise(sh, err, 8u); break; }
       tc_fence_after();
-      if (!sh->abort) epi(mt);
+      if (!sh->abort) epi(mt, sh->tmem + buf * 256u);
       tc_fence_before();
-      mbar_arrive(&sh->acc_empty);
+      mbar_arrive(&sh->acc_empty[buf]);
     }
   }
+  // every thread advances the counters the same way
   it += n_mt * n_kc;
-  mtc += n_mt;
+  for (uint32_t mt = 0; mt < n_mt; ++mt) {
+    uint32_t buf, par;
+    acc_next(nbuf, uses, buf, par);
+  }
 }
 
 // 2^e as an FP32 factor pair (e may leave the normal range of one factor).
@@ -179,11 +230,11 @@ __device__ __forceinline__ void pow2_pair(int e, float& f1, float& f2) {
 // quarter q) and combine them exactly: every D_d is an integer below 2^24, so
 // Y = sum_d D_d * 2^(6(5-d)) is an exact int64 and y = Y * 2^-42 (before scaling).
 // Returns y as a double-float pair.
-template <int NB>
-__device__ __forceinline__ void load_combine8(uint32_t tmem, int q, uint32_t j0, float* yh, float* yl) {
+__device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q, uint32_t j0, float* yh,
+                                              float* yl) {
   float D[kDiags][8];
 #pragma unroll
-  for (int d = 0; d < kDiags; ++d) tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + d * NB + j0, D[d]);
+  for (int d = 0; d < kDiags; ++d) tmem_ld8(tcols + ((uint32_t)(q * 32) << 16) + d * nb + j0, D[d]);
   tmem_wait_ld();
 #pragma unroll
   for (int jj = 0; jj < 8; ++jj) {
@@ -197,34 +248,47 @@ __device__ __forceinline__ void load_combine8(uint32_t tmem, int q, uint32_t j0,
   }
 }
 
-// Slice a state block (rows x NB, column-major, double-float) into the BF16 B tiles
-// with per-column exponents beta[j] (|x| < 2^beta).
-template <int NB>
-__device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t col0,
+// Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
+// into the BF16 B tiles with per-column exponents beta[j] (|x| < 2^beta).
+__device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t nb,
                                             const int* beta, uint8_t* tiles) {
-  using C = Cfg<NB>;
   const uint32_t t = threadIdx.x - 128;
-  for (uint32_t e = t; e < kp * NB; e += kEpiThreads) {
-    const uint32_t j = e / kp, row = e - j * kp;
-    const size_t si = (size_t)(col0 + j) * kp + row;
-    float vh = ldexpf(xh[si], -beta[j]), vl = ldexpf(xl[si], -beta[j]);
-    uint8_t* base = tiles + (size_t)(row / kKc) * C::kBBytes + tile_off(j, row % kKc);
+  const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);
+  const uint32_t n = kp * nb;
+  for (uint32_t e0 = t; e0 < n; e0 += 4 * kEpiThreads) {
+    float vh[4], vl[4];
+    uint32_t jj[4], rr[4];
 #pragma unroll
-    for (int s = 0; s < kSlices; ++s) {
-      const float th = vh * 64.f, tl = vl * 64.f;
-      float a = rintf(th);
-      a = fminf(64.f, fmaxf(-64.f, a));
-      two_sum(th - a, tl, vh, vl);
-      *reinterpret_cast<__nv_bfloat16*>(base + s * C::kBTile) = __float2bfloat16_rn(a);
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t e = e0 + u * kEpiThreads;
+      jj[u] = e / kp;
+      rr[u] = e - jj[u] * kp;
+      if (e < n) {
+        vh[u] = xh[(size_t)jj[u] * kp + rr[u]];
+        vl[u] = xl[(size_t)jj[u] * kp + rr[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (e0 + u * kEpiThreads >= n) break;
+      float h = ldexpf(vh[u], -beta[jj[u]]), l = ldexpf(vl[u], -beta[jj[u]]);
+      uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + tile_off(jj[u], rr[u] % kKc);
+#pragma unroll
+      for (int s = 0; s < kSlices; ++s) {
+        const float th = h * 64.f, tl = l * 64.f;
+        float a = rintf(th);
+        a = fminf(64.f, fmaxf(-64.f, a));
+        two_sum(th - a, tl, h, l);
+        *reinterpret_cast<__nv_bfloat16*>(base + s * btile) = __float2bfloat16_rn(a);
+      }
     }
   }
 }
 
 // Column exponents from the maxima gathered in colmax: |x| < 2^beta.
-template <int NB>
-__device__ __forceinline__ void column_exponents(Shared* sh, int* beta) {
+__device__ __forceinline__ void column_exponents(Shared* sh, uint32_t nb, int* beta) {
   const uint32_t t = threadIdx.x - 128;
-  if (t < NB) {
+  if (t < nb) {
     const float m = __uint_as_float(sh->colmax[t]);
     beta[t] = (m > 0.f) ? ilogbf(m) + 1 : 0;
     sh->colmax[t] = 0u;
@@ -236,148 +300,184 @@ __device__ __forceinline__ void note_max(Shared* sh, uint32_t j, float v) {
   if ((threadIdx.x & 31) == 0) atomicMax(&sh->colmax[j], m);
 }
 
-template <int NB>
+__device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
 __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) {
-  using C = Cfg<NB>;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* stages = smem;
-  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * C::kStage);
+  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ew = warp - 4;                     // >= 0 on the epilogue warps
-  const int q = warp & 3;                      // TMEM lane quarter of this warp
-  const uint32_t jbeg = (uint32_t)((ew >> 2) * (NB / 2)), jend = jbeg + NB / 2;  // this group's columns
-  const uint32_t n_mt_v = a.kvp / 128, n_mt_s = a.ksp / 128, n_kc_v = a.ksp / kKc, n_kc_s = a.kvp / kKc;
-  const uint32_t col0 = blockIdx.x * NB;
-  uint8_t* bvt = a.bvt + (size_t)blockIdx.x * n_kc_s * C::kBBytes;
-  uint8_t* bst = a.bst + (size_t)blockIdx.x * n_kc_v * C::kBBytes;
+  const int ew = warp - 4;  // >= 0 on the epilogue warps
+  const int q = warp & 3;   // TMEM lane quarter of this warp
+  uint8_t* bvt = a.bvt + (size_t)blockIdx.x * a.bscratch;
+  uint8_t* bst = a.bst + (size_t)blockIdx.x * a.bscratch;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&sh->full[s], 1);
       mbar_init(&sh->empty[s], 1);
     }
-    mbar_init(&sh->acc_full, 1);
-    mbar_init(&sh->acc_empty, kEpiThreads);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sh->acc_full[b], 1);
+      mbar_init(&sh->acc_empty[b], kEpiThreads);
+    }
+    mbar_init(&sh->drain, 1);
     sh->abort = 0;
     mbar_init_fence();
   }
-  if (threadIdx.x < 64) {
-    sh->colmax[threadIdx.x] = 0u;
-    sh->beta_v[threadIdx.x] = 0;
-    sh->beta_s[threadIdx.x] = 0;
-  }
-  if (warp == 2) tmem_alloc(&sh->tmem, C::kTmemCols);
+  if (warp == 2) tmem_alloc(&sh->tmem, kTmemCols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
 
-  // B tiles of the current XS (the state may be non-zero when advancing in pieces)
-  if (ew >= 0) {
-    for (uint32_t e = threadIdx.x - 128; e < a.ksp * NB; e += kEpiThreads) {
-      const uint32_t j = e / a.ksp, row = e - j * a.ksp;
-      const float v = a.xsh[(size_t)(col0 + j) * a.ksp + row];
-      atomicMax(&sh->colmax[j], __float_as_uint(fabsf(v)));
-    }
-    asm volatile("bar.sync 1, 256;" ::: "memory");
-    column_exponents<NB>(sh, sh->beta_s);
-    asm volatile("bar.sync 1, 256;" ::: "memory");
-    slice_state<NB>(a.xsh, a.xsl, a.ksp, col0, sh->beta_s, bst);
-    asm volatile("fence.proxy.async.global;" ::: "memory");
-  }
-  __syncthreads();
-
   const float dth = (float)a.dt, dtl = (float)(a.dt - (double)dth);
-  uint32_t it = 0, mtc = 0;
-  for (unsigned long long st = 0; st < a.nsteps && !sh->abort; ++st) {
-    const unsigned long long n = a.step0 + st + 1;
-    if (ew >= 0) {
-      const uint32_t t = threadIdx.x - 128;
-      if (t < NB) {
-        const uint32_t col = col0 + t;
-        sh->fdt[t] = col < a.M
-                         ? signal_value(a.kind[col], a.delay[col], a.period[col], (double)(n - 1) * a.dt) * a.dt
-                         : 0.0;
-      }
-      asm volatile("bar.sync 1, 256;" ::: "memory");
+  uint32_t it = 0, uses[2] = {0u, 0u};
+  unsigned long long t_start = 0;
+  for (uint32_t ti = a.cta_begin[blockIdx.x]; ti < a.cta_begin[blockIdx.x + 1]; ++ti) {
+    if (threadIdx.x == 0) {
+      t_start = global_ns();
+      sh->tile = a.tiles[a.order[ti]];
+      sh->in = a.inst[sh->tile.inst];
     }
-    // ---------------- velocity: XV += dt Av XS + fdt b ----------------
-    gemm_phase<NB>(stages, sh, a.Av, bst, n_mt_v, n_kc_v, it, mtc, a.error, [&](uint32_t mt) {
-      const uint32_t row = mt * 128 + q * 32 + lane;
-      const int alpha = a.alpha_v[row];
-      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-        float yh[8], yl[8];
-        load_combine8<NB>(sh->tmem, q, j0, yh, yl);
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const uint32_t j = j0 + jj, col = col0 + j;
-          const int e = alpha + sh->beta_s[j];
-          const size_t si = (size_t)col * a.kvp + row;
-          float xh = a.xvh[si], xl = a.xvl[si];
-          float s1, s2;
-          pow2_pair(e, s1, s2);
-          df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-          const double f = sh->fdt[j];
-          const float fh = (float)f, fl = (float)(f - (double)fh);
-          df_fma(xh, xl, fh, fl, a.bh[si], a.bl[si]);
-          a.xvh[si] = xh;
-          a.xvl[si] = xl;
-          note_max(sh, j, xh);
-          if (a.snap_vp && a.fvp && n % a.fvp == 0 && row < a.kv && col < a.M)
-            a.snap_vp[row + (size_t)a.kv * ((n / a.fvp - 1) + a.Tvp * col)] = (double)xh + (double)xl;
-        }
-      }
-    });
+    if (threadIdx.x < kMaxNb) {
+      sh->colmax[threadIdx.x] = 0u;
+      sh->beta_v[threadIdx.x] = 0;
+      sh->beta_s[threadIdx.x] = 0;
+    }
+    if (__syncthreads_or(sh->abort != 0)) break;
+    const OzInst& in = sh->in;
+    const uint32_t nb = sh->tile.nb, col0 = sh->tile.col0;
+    const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
+    const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
+    float* const xvh = in.xvh + (size_t)col0 * in.kvp;
+    float* const xvl = in.xvl + (size_t)col0 * in.kvp;
+    float* const xsh = in.xsh + (size_t)col0 * in.ksp;
+    float* const xsl = in.xsl + (size_t)col0 * in.ksp;
+    const float* const bh = in.bh + (size_t)col0 * in.kvp;
+    const float* const bl = in.bl + (size_t)col0 * in.kvp;
+
+    // B tiles of the current XS (the state may be non-zero when advancing in pieces)
     if (ew >= 0) {
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      column_exponents<NB>(sh, sh->beta_v);
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      if (!sh->abort) slice_state<NB>(a.xvh, a.xvl, a.kvp, col0, sh->beta_v, bvt);
+      for (uint32_t e = threadIdx.x - 128; e < in.ksp * nb; e += kEpiThreads) {
+        const uint32_t j = e / in.ksp, row = e - j * in.ksp;
+        atomicMax(&sh->colmax[j], __float_as_uint(fabsf(xsh[(size_t)j * in.ksp + row])));
+      }
+      epi_barrier();
+      column_exponents(sh, nb, sh->beta_s);
+      epi_barrier();
+      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
-    __syncthreads();
-    if (sh->abort) break;
-    // ---------------- stress: XS += dt As XV ----------------
-    gemm_phase<NB>(stages, sh, a.As, bvt, n_mt_s, n_kc_s, it, mtc, a.error, [&](uint32_t mt) {
-      const uint32_t row = mt * 128 + q * 32 + lane;
-      const int alpha = a.alpha_s[row];
-      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-        float yh[8], yl[8];
-        load_combine8<NB>(sh->tmem, q, j0, yh, yl);
-#pragma unroll
-        for (int jj = 0; jj < 8; ++jj) {
-          const uint32_t j = j0 + jj, col = col0 + j;
-          const int e = alpha + sh->beta_v[j];
-          const size_t si = (size_t)col * a.ksp + row;
-          float xh = a.xsh[si], xl = a.xsl[si];
-          float s1, s2;
-          pow2_pair(e, s1, s2);
-          df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-          a.xsh[si] = xh;
-          a.xsl[si] = xl;
-          note_max(sh, j, xh);
-          if (a.snap_sp && a.fsp && n % a.fsp == 0 && row < a.ks && col < a.M)
-            a.snap_sp[row + (size_t)a.ks * ((n / a.fsp - 1) + a.Tsp * col)] = (double)xh + (double)xl;
+    if (__syncthreads_or(sh->abort != 0)) break;
+
+    for (unsigned long long st = 0; st < a.nsteps; ++st) {
+      const unsigned long long n = a.step0 + st + 1;
+      if (ew >= 0) {
+        const uint32_t t = threadIdx.x - 128;
+        if (t < nb) {
+          const uint32_t col = col0 + t;
+          sh->fdt[t] = col < in.M ? signal_value(in.kind[col], in.delay[col], in.period[col], (double)(n - 1) * a.dt) *
+                                        a.dt
+                                  : 0.0;
         }
+        epi_barrier();
       }
-    });
-    if (ew >= 0) {
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      column_exponents<NB>(sh, sh->beta_s);
-      asm volatile("bar.sync 1, 256;" ::: "memory");
-      if (!sh->abort) slice_state<NB>(a.xsh, a.xsl, a.ksp, col0, sh->beta_s, bst);
-      asm volatile("fence.proxy.async.global;" ::: "memory");
+      // ---------------- velocity: XV += dt Av XS + fdt b ----------------
+      gemm_phase(stages, sh, in.Av, bst, n_mt_v, n_kc_v, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+        const uint32_t row = mt * 128 + q * 32 + lane;
+        const int alpha = in.alpha_v[row];
+        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+          float ph[8], pl[8], qh[8], ql[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
+            const size_t si = (size_t)(j0 + jj) * in.kvp + row;
+            ph[jj] = xvh[si];
+            pl[jj] = xvl[si];
+            qh[jj] = bh[si];
+            ql[jj] = bl[si];
+          }
+          float yh[8], yl[8];
+          load_combine8(tcols, nb, q, j0, yh, yl);
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const uint32_t j = j0 + jj, col = col0 + j;
+            const int e = alpha + sh->beta_s[j];
+            const size_t si = (size_t)j * in.kvp + row;
+            float xh = ph[jj], xl = pl[jj];
+            float s1, s2;
+            pow2_pair(e, s1, s2);
+            df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
+            const double f = sh->fdt[j];
+            const float fh = (float)f, fl = (float)(f - (double)fh);
+            df_fma(xh, xl, fh, fl, qh[jj], ql[jj]);
+            xvh[si] = xh;
+            xvl[si] = xl;
+            note_max(sh, j, xh);
+            if (in.snap_vp && in.fvp && n % in.fvp == 0 && row < in.kv && col < in.M)
+              in.snap_vp[row + (size_t)in.kv * ((n / in.fvp - 1) + in.Tvp * col)] = (double)xh + (double)xl;
+          }
+        }
+      });
+      if (ew >= 0) {
+        epi_barrier();
+        column_exponents(sh, nb, sh->beta_v);
+        epi_barrier();
+        if (!sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt);
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+      }
+      if (__syncthreads_or(sh->abort != 0)) break;
+      // ---------------- stress: XS += dt As XV ----------------
+      gemm_phase(stages, sh, in.As, bvt, n_mt_s, n_kc_s, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+        const uint32_t row = mt * 128 + q * 32 + lane;
+        const int alpha = in.alpha_s[row];
+        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+          float ph[8], pl[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const size_t si = (size_t)(j0 + jj) * in.ksp + row;
+            ph[jj] = xsh[si];
+            pl[jj] = xsl[si];
+          }
+          float yh[8], yl[8];
+          load_combine8(tcols, nb, q, j0, yh, yl);
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const uint32_t j = j0 + jj, col = col0 + j;
+            const int e = alpha + sh->beta_v[j];
+            const size_t si = (size_t)j * in.ksp + row;
+            float xh = ph[jj], xl = pl[jj];
+            float s1, s2;
+            pow2_pair(e, s1, s2);
+            df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
+            xsh[si] = xh;
+            xsl[si] = xl;
+            note_max(sh, j, xh);
+            if (in.snap_sp && in.fsp && n % in.fsp == 0 && row < in.ks && col < in.M)
+              in.snap_sp[row + (size_t)in.ks * ((n / in.fsp - 1) + in.Tsp * col)] = (double)xh + (double)xl;
+          }
+        }
+      });
+      if (ew >= 0) {
+        epi_barrier();
+        column_exponents(sh, nb, sh->beta_s);
+        epi_barrier();
+        if (!sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst);
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+      }
+      if (__syncthreads_or(sh->abort != 0)) break;
     }
-    __syncthreads();
+    if (threadIdx.x == 0 && a.tile_ns) a.tile_ns[a.order[ti]] = global_ns() - t_start;
+    if (__syncthreads_or(sh->abort != 0)) break;
   }
   // drain: no MMA may still be in flight when TMEM is released
   if (warp == 1 && lane == 0) {
-    mma_commit(&sh->acc_full);
-    mbar_wait(&sh->acc_full, mtc & 1u);
+    mma_commit(&sh->drain);
+    if (!mbar_wait(&sh->drain, 0)) atomicOr(a.error, 16u);
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 2) tmem_dealloc(sh->tmem, C::kTmemCols);
+  if (warp == 2) tmem_dealloc(sh->tmem, kTmemCols);
 }
 
 // state (hi + lo, [Mp][kp]) -> FP64 LayoutLeft k x M
@@ -427,111 +527,235 @@ void slice_operator(const double* A, uint32_t rows, uint32_t cols, uint32_t rows
   }
 }
 
+// Longest processing time first: tiles by decreasing cost, each to the least-loaded CTA.
+void lpt_schedule(const std::vector<double>& cost, uint32_t ctas, std::vector<uint32_t>& order,
+                  std::vector<uint32_t>& begin, double& makespan) {
+  std::vector<uint32_t> idx(cost.size());
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return cost[x] > cost[y]; });
+  using Slot = std::pair<double, uint32_t>;
+  std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> pq;
+  for (uint32_t c = 0; c < ctas; ++c) pq.push({0.0, c});
+  std::vector<std::vector<uint32_t>> per(ctas);
+  makespan = 0.0;
+  for (uint32_t t : idx) {
+    Slot s = pq.top();
+    pq.pop();
+    per[s.second].push_back(t);
+    s.first += cost[t];
+    makespan = std::max(makespan, s.first);
+    pq.push(s);
+  }
+  order.clear();
+  begin.assign(ctas + 1, 0u);
+  for (uint32_t c = 0; c < ctas; ++c) {
+    begin[c] = (uint32_t)order.size();
+    order.insert(order.end(), per[c].begin(), per[c].end());
+  }
+  begin[ctas] = (uint32_t)order.size();
+}
+
 }  // namespace
 
-struct Plan {
-  uint32_t kv = 0, ks = 0, kvp = 0, ksp = 0, M = 0, Mp = 0, nb = 32, ctas = 0;
-  uint8_t *Av = nullptr, *As = nullptr, *bvt = nullptr, *bst = nullptr;
-  int *alpha_v = nullptr, *alpha_s = nullptr;
-  float *bh = nullptr, *bl = nullptr, *xvh = nullptr, *xvl = nullptr, *xsh = nullptr, *xsl = nullptr;
+struct Batch {
+  std::vector<OzInst> inst;  // host copy of the device table
+  OzInst* d_inst = nullptr;
+  std::vector<void*> owned;  // device buffers of the instances
+  // tiling
+  uint32_t width = 32;
+  std::string sched_source = "model";
+  std::vector<OzTile> tiles;
+  std::vector<uint32_t> order, begin;
+  uint32_t ctas = 0, max_tiles = 0;
+  double model_makespan = 0.0;
+  OzTile* d_tiles = nullptr;
+  uint32_t *d_order = nullptr, *d_begin = nullptr;
+  uint8_t *bvt = nullptr, *bst = nullptr;
+  size_t bscratch = 0;
   unsigned int* error = nullptr;
+  unsigned long long* tile_ns = nullptr;
   size_t smem = 0;
+  int sms = 0;
+  bool table_dirty = true, tiles_dirty = true;
 };
 
-int create(Plan*& p, uint32_t kv, uint32_t ks, const double* hAv, const double* hAs, uint32_t M, const double* hb,
-           cudaStream_t s) {
-  if (kv > 1024 || ks > 1024)
-    return fail(SHAW_ERR_UNSUPPORTED, "the Ozaki tensor-core ROM supports at most 1024 modes per dof");
-  p = new Plan();
-  p->kv = kv; p->ks = ks; p->M = M;
-  p->kvp = round_up(kv, 128); p->ksp = round_up(ks, 128);
-  p->nb = (M >= 64 * 152) ? 64 : 32;
-  p->Mp = round_up(M, p->nb);
-  p->ctas = p->Mp / p->nb;
-  std::vector<uint16_t> sv, ss;
-  std::vector<int> av, as;
-  slice_operator(hAv, kv, ks, p->kvp, p->ksp, sv, av);
-  slice_operator(hAs, ks, kv, p->ksp, p->kvp, ss, as);
-  std::vector<float> bh((size_t)p->Mp * p->kvp, 0.f), bl((size_t)p->Mp * p->kvp, 0.f);
-  for (uint32_t c = 0; c < M; ++c)
-    for (uint32_t r = 0; r < kv; ++r) {
-      const double v = hb[(size_t)c * kv + r];
-      const float h = (float)v;
-      bh[(size_t)c * p->kvp + r] = h;
-      bl[(size_t)c * p->kvp + r] = (float)(v - (double)h);
-    }
-  const size_t btile_bytes = (size_t)kSlices * p->nb * kRowBytes;  // per K-chunk
+namespace {
+
+uint32_t tile_width_for(uint32_t M, uint32_t W) {
+  uint32_t nb = 16;
+  while (nb < W && nb < M) nb *= 2;
+  return nb;
+}
+
+// Modelled cost of one tile per step (arbitrary units): the 2 x 21 slice-pair MMAs of
+// 128 x nb x 16 and the per-element epilogue and re-slicing work.
+double tile_model_cost(const OzInst& in, uint32_t nb) {
+  return (double)nb * ((double)in.kvp * in.ksp * 21.0 / 2048.0 + 15.0 * (in.kvp + in.ksp)) + 2000.0;
+}
+
+void build_tiles(Batch* p, uint32_t W) {
+  p->width = W;
+  p->tiles.clear();
+  for (uint32_t i = 0; i < (uint32_t)p->inst.size(); ++i) {
+    const uint32_t nb = tile_width_for(p->inst[i].M, W);
+    for (uint32_t c = 0; c < p->inst[i].M; c += nb) p->tiles.push_back({i, c, nb, 0u});
+  }
+  p->ctas = std::min<uint32_t>((uint32_t)p->tiles.size(), (uint32_t)p->sms);
+  std::vector<double> cost(p->tiles.size());
+  for (size_t t = 0; t < p->tiles.size(); ++t) cost[t] = tile_model_cost(p->inst[p->tiles[t].inst], p->tiles[t].nb);
+  lpt_schedule(cost, p->ctas, p->order, p->begin, p->model_makespan);
+  p->sched_source = "model";
+  p->tiles_dirty = true;
+}
+
+int upload(Batch* p, cudaStream_t s) {
+  if (p->table_dirty) {
+    SHAW_CUDA(cudaMemcpyAsync(p->d_inst, p->inst.data(), p->inst.size() * sizeof(OzInst), cudaMemcpyHostToDevice, s));
+    p->table_dirty = false;
+  }
+  if (p->tiles_dirty) {
+    SHAW_CUDA(cudaMemcpyAsync(p->d_tiles, p->tiles.data(), p->tiles.size() * sizeof(OzTile), cudaMemcpyHostToDevice, s));
+    SHAW_CUDA(cudaMemcpyAsync(p->d_order, p->order.data(), p->order.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                              s));
+    SHAW_CUDA(cudaMemcpyAsync(p->d_begin, p->begin.data(), p->begin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                              s));
+    p->tiles_dirty = false;
+  }
+  return SHAW_OK;
+}
+
+}  // namespace
+
+int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
+  p = nullptr;
+  if (n == 0 || !d) return fail(SHAW_ERR_INVALID_ARG, "empty batch");
+  for (uint32_t i = 0; i < n; ++i) {
+    if (d[i].kv == 0 || d[i].ks == 0 || d[i].M == 0 || !d[i].Av || !d[i].As || !d[i].b)
+      return fail(SHAW_ERR_INVALID_ARG, "instance " + std::to_string(i) + ": empty sizes or null operator");
+    if (d[i].kv > 1024 || d[i].ks > 1024)
+      return fail(SHAW_ERR_UNSUPPORTED, "the Ozaki tensor-core ROM supports at most 1024 modes per dof");
+  }
+  Batch* b = new Batch();
+  int dev = 0;
   cudaError_t e;
-  auto bail = [&](cudaError_t err, const char* w) {
-    const int rc = cuda_fail(err, w);
-    destroy(p);
-    p = nullptr;
+  auto bail = [&](int rc) {
+    destroy(b);
     return rc;
   };
-#define OZ_TRY(call) do { e = (call); if (e != cudaSuccess) return bail(e, #call); } while (0)
-  OZ_TRY(cudaMalloc(&p->Av, sv.size() * 2));
-  OZ_TRY(cudaMalloc(&p->As, ss.size() * 2));
-  OZ_TRY(cudaMalloc(&p->alpha_v, p->kvp * sizeof(int)));
-  OZ_TRY(cudaMalloc(&p->alpha_s, p->ksp * sizeof(int)));
-  OZ_TRY(cudaMalloc(&p->bh, bh.size() * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->bl, bl.size() * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->xvh, (size_t)p->Mp * p->kvp * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->xvl, (size_t)p->Mp * p->kvp * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->xsh, (size_t)p->Mp * p->ksp * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->xsl, (size_t)p->Mp * p->ksp * sizeof(float)));
-  OZ_TRY(cudaMalloc(&p->bvt, (size_t)p->ctas * (p->kvp / kKc) * btile_bytes));
-  OZ_TRY(cudaMalloc(&p->bst, (size_t)p->ctas * (p->ksp / kKc) * btile_bytes));
-  OZ_TRY(cudaMalloc(&p->error, sizeof(unsigned int)));
-  OZ_TRY(cudaMemcpyAsync(p->Av, sv.data(), sv.size() * 2, cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaMemcpyAsync(p->As, ss.data(), ss.size() * 2, cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaMemcpyAsync(p->alpha_v, av.data(), av.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaMemcpyAsync(p->alpha_s, as.data(), as.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaMemcpyAsync(p->bh, bh.data(), bh.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaMemcpyAsync(p->bl, bl.data(), bl.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-  OZ_TRY(cudaStreamSynchronize(s));  // the host vectors go out of scope
+#define OZ_TRY(call) do { e = (call); if (e != cudaSuccess) return bail(cuda_fail(e, #call)); } while (0)
+  OZ_TRY(cudaGetDevice(&dev));
+  OZ_TRY(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+  uint32_t kmax_p = 128;
+  b->inst.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    OzInst& in = b->inst[i];
+    std::memset(&in, 0, sizeof(in));
+    in.kv = d[i].kv; in.ks = d[i].ks; in.M = d[i].M;
+    in.kvp = round_up(in.kv, 128); in.ksp = round_up(in.ks, 128); in.Mp = round_up(in.M, kMaxNb);
+    kmax_p = std::max(kmax_p, std::max(in.kvp, in.ksp));
+    b->max_tiles += (in.M + 15) / 16;
+    std::vector<uint16_t> sv, ss;
+    std::vector<int> av, as;
+    slice_operator(d[i].Av, in.kv, in.ks, in.kvp, in.ksp, sv, av);
+    slice_operator(d[i].As, in.ks, in.kv, in.ksp, in.kvp, ss, as);
+    std::vector<float> bh((size_t)in.Mp * in.kvp, 0.f), bl((size_t)in.Mp * in.kvp, 0.f);
+    for (uint32_t c = 0; c < in.M; ++c)
+      for (uint32_t r = 0; r < in.kv; ++r) {
+        const double v = d[i].b[(size_t)c * in.kv + r];
+        const float h = (float)v;
+        bh[(size_t)c * in.kvp + r] = h;
+        bl[(size_t)c * in.kvp + r] = (float)(v - (double)h);
+      }
+    auto alloc = [&](void** ptr, size_t bytes) {
+      const cudaError_t r = cudaMalloc(ptr, bytes);
+      if (r == cudaSuccess) b->owned.push_back(*ptr);
+      return r;
+    };
+    const size_t nv = (size_t)in.Mp * in.kvp, ns = (size_t)in.Mp * in.ksp;
+    OZ_TRY(alloc((void**)&in.Av, sv.size() * 2));
+    OZ_TRY(alloc((void**)&in.As, ss.size() * 2));
+    OZ_TRY(alloc((void**)&in.alpha_v, in.kvp * sizeof(int)));
+    OZ_TRY(alloc((void**)&in.alpha_s, in.ksp * sizeof(int)));
+    OZ_TRY(alloc((void**)&in.bh, nv * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.bl, nv * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.xvh, nv * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.xvl, nv * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.xsh, ns * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.xsl, ns * sizeof(float)));
+    OZ_TRY(cudaMemcpyAsync((void*)in.Av, sv.data(), sv.size() * 2, cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaMemcpyAsync((void*)in.As, ss.data(), ss.size() * 2, cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaMemcpyAsync((void*)in.alpha_v, av.data(), av.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaMemcpyAsync((void*)in.alpha_s, as.data(), as.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaMemcpyAsync((void*)in.bh, bh.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaMemcpyAsync((void*)in.bl, bl.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
+    OZ_TRY(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  }
+  b->bscratch = (size_t)(kmax_p / kKc) * bstage_bytes(kMaxNb);
+  OZ_TRY(cudaMalloc(&b->d_inst, n * sizeof(OzInst)));
+  OZ_TRY(cudaMalloc(&b->d_tiles, b->max_tiles * sizeof(OzTile)));
+  OZ_TRY(cudaMalloc(&b->d_order, b->max_tiles * sizeof(uint32_t)));
+  OZ_TRY(cudaMalloc(&b->d_begin, ((size_t)b->sms + 1) * sizeof(uint32_t)));
+  OZ_TRY(cudaMalloc(&b->bvt, (size_t)b->sms * b->bscratch));
+  OZ_TRY(cudaMalloc(&b->bst, (size_t)b->sms * b->bscratch));
+  OZ_TRY(cudaMalloc(&b->error, sizeof(unsigned int)));
+  OZ_TRY(cudaMalloc(&b->tile_ns, b->max_tiles * sizeof(unsigned long long)));
 #undef OZ_TRY
-  const uint32_t stage = p->nb == 64 ? Cfg<64>::kStage : Cfg<32>::kStage;
-  p->smem = (size_t)kStages * stage + sizeof(Shared);
+  b->smem = (size_t)kStages * kStageBytes + sizeof(Shared);
+  // default tiling: 32-column tiles (64 when a single wide system fills every SM twice)
+  build_tiles(b, (n == 1 && d[0].M >= 64u * (uint32_t)b->sms) ? 64u : 32u);
+  p = b;
   return reset(p, s);
 }
 
-int reset(Plan* p, cudaStream_t s) {
-  const size_t btile_bytes = (size_t)kSlices * p->nb * kRowBytes;
-  SHAW_CUDA(cudaMemsetAsync(p->xvh, 0, (size_t)p->Mp * p->kvp * sizeof(float), s));
-  SHAW_CUDA(cudaMemsetAsync(p->xvl, 0, (size_t)p->Mp * p->kvp * sizeof(float), s));
-  SHAW_CUDA(cudaMemsetAsync(p->xsh, 0, (size_t)p->Mp * p->ksp * sizeof(float), s));
-  SHAW_CUDA(cudaMemsetAsync(p->xsl, 0, (size_t)p->Mp * p->ksp * sizeof(float), s));
-  SHAW_CUDA(cudaMemsetAsync(p->bvt, 0, (size_t)p->ctas * (p->kvp / kKc) * btile_bytes, s));
-  SHAW_CUDA(cudaMemsetAsync(p->bst, 0, (size_t)p->ctas * (p->ksp / kKc) * btile_bytes, s));
+int set_signals(Batch* p, uint32_t i, const int* kind, const double* period, const double* delay) {
+  if (!p || i >= p->inst.size()) return fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  p->inst[i].kind = kind;
+  p->inst[i].period = period;
+  p->inst[i].delay = delay;
+  p->table_dirty = true;
+  return SHAW_OK;
+}
+
+int set_snapshots(Batch* p, uint32_t i, double* snap_vp, double* snap_sp, unsigned long long Tvp,
+                  unsigned long long Tsp, uint32_t fvp, uint32_t fsp) {
+  if (!p || i >= p->inst.size()) return fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  OzInst& in = p->inst[i];
+  if (in.snap_vp != snap_vp || in.snap_sp != snap_sp || in.Tvp != Tvp || in.Tsp != Tsp || in.fvp != fvp ||
+      in.fsp != fsp) {
+    in.snap_vp = snap_vp; in.snap_sp = snap_sp; in.Tvp = Tvp; in.Tsp = Tsp; in.fvp = fvp; in.fsp = fsp;
+    p->table_dirty = true;
+  }
+  return SHAW_OK;
+}
+
+int reset(Batch* p, cudaStream_t s) {
+  for (const OzInst& in : p->inst) {
+    const size_t nv = (size_t)in.Mp * in.kvp, ns = (size_t)in.Mp * in.ksp;
+    SHAW_CUDA(cudaMemsetAsync(in.xvh, 0, nv * sizeof(float), s));
+    SHAW_CUDA(cudaMemsetAsync(in.xvl, 0, nv * sizeof(float), s));
+    SHAW_CUDA(cudaMemsetAsync(in.xsh, 0, ns * sizeof(float), s));
+    SHAW_CUDA(cudaMemsetAsync(in.xsl, 0, ns * sizeof(float), s));
+  }
   SHAW_CUDA(cudaMemsetAsync(p->error, 0, sizeof(unsigned int), s));
   return SHAW_OK;
 }
 
-int advance(Plan* p, cudaStream_t s, double dt, unsigned long long step0, unsigned long long nsteps,
-            const int* kind, const double* period, const double* delay, double* snap_vp, double* snap_sp,
-            unsigned long long Tvp, unsigned long long Tsp, uint32_t fvp, uint32_t fsp) {
+int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsigned long long nsteps) {
+  for (size_t i = 0; i < p->inst.size(); ++i)
+    if (!p->inst[i].kind) return fail(SHAW_ERR_STATE, "instance " + std::to_string(i) + " has no signals");
+  if (int rc = upload(p, s)) return rc;
   OzArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.Av = p->Av; a.As = p->As; a.alpha_v = p->alpha_v; a.alpha_s = p->alpha_s; a.bh = p->bh; a.bl = p->bl;
-  a.xvh = p->xvh; a.xvl = p->xvl; a.xsh = p->xsh; a.xsl = p->xsl; a.bvt = p->bvt; a.bst = p->bst;
-  a.kind = kind; a.period = period; a.delay = delay;
-  a.snap_vp = snap_vp; a.snap_sp = snap_sp; a.Tvp = Tvp; a.Tsp = Tsp; a.fvp = fvp; a.fsp = fsp;
-  a.kv = p->kv; a.ks = p->ks; a.kvp = p->kvp; a.ksp = p->ksp; a.M = p->M;
-  a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error;
-  if (p->nb == 64) {
-    SHAW_CUDA(cudaFuncSetAttribute(rom_rank2_ozaki_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)p->smem));
-    rom_rank2_ozaki_kernel<64><<<p->ctas, kThreads, p->smem, s>>>(a);
-  } else {
-    SHAW_CUDA(cudaFuncSetAttribute(rom_rank2_ozaki_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)p->smem));
-    rom_rank2_ozaki_kernel<32><<<p->ctas, kThreads, p->smem, s>>>(a);
-  }
+  a.inst = p->d_inst; a.tiles = p->d_tiles; a.order = p->d_order; a.cta_begin = p->d_begin;
+  a.bvt = p->bvt; a.bst = p->bst; a.bscratch = p->bscratch;
+  a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error; a.tile_ns = p->tile_ns;
+  SHAW_CUDA(cudaFuncSetAttribute(rom_rank2_ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+  rom_rank2_ozaki_kernel<<<p->ctas, kThreads, p->smem, s>>>(a);
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
 }
 
-int check(Plan* p, cudaStream_t s) {
+int check(Batch* p, cudaStream_t s) {
   unsigned int err = 0;
   SHAW_CUDA(cudaMemcpyAsync(&err, p->error, sizeof(err), cudaMemcpyDeviceToHost, s));
   SHAW_CUDA(cudaStreamSynchronize(s));
@@ -541,17 +765,99 @@ int check(Plan* p, cudaStream_t s) {
   return SHAW_OK;
 }
 
-int get_state(Plan* p, cudaStream_t s, double* dxv, double* dxs) {
-  oz_gather_state_kernel<<<256, 256, 0, s>>>(p->xvh, p->xvl, p->kv, p->M, p->kvp, dxv);
-  oz_gather_state_kernel<<<256, 256, 0, s>>>(p->xsh, p->xsl, p->ks, p->M, p->ksp, dxs);
+int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs) {
+  if (i >= p->inst.size()) return fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  const OzInst& in = p->inst[i];
+  oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xvh, in.xvl, in.kv, in.M, in.kvp, dxv);
+  oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xsh, in.xsl, in.ks, in.M, in.ksp, dxs);
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
 }
 
-void destroy(Plan* p) {
+int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report) {
+  if (trial_steps == 0) trial_steps = 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SHAW_CUDA(cudaEventCreate(&e0));
+  SHAW_CUDA(cudaEventCreate(&e1));
+  int rc = SHAW_OK;
+  auto timed = [&](float& ms) -> int {
+    if (int r = reset(p, s)) return r;
+    if (int r = upload(p, s)) return r;
+    SHAW_CUDA(cudaEventRecord(e0, s));
+    if (int r = advance(p, s, dt, 0, trial_steps)) return r;
+    SHAW_CUDA(cudaEventRecord(e1, s));
+    if (int r = check(p, s)) return r;
+    SHAW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    return SHAW_OK;
+  };
+  struct Best {
+    float ms = 1e30f;
+    uint32_t width = 32;
+    std::vector<OzTile> tiles;
+    std::vector<uint32_t> order, begin;
+    uint32_t ctas = 0;
+    std::string source;
+  } best;
+  char line[256];
+  report.clear();
+  do {
+    float warm = 0.f;
+    build_tiles(p, 32);
+    if ((rc = timed(warm))) break;  // first launch: module load, caches
+    for (uint32_t W : {16u, 32u, 64u}) {
+      build_tiles(p, W);
+      float ms_model = 0.f;
+      if ((rc = timed(ms_model))) break;
+      std::vector<unsigned long long> ns(p->tiles.size());
+      SHAW_CUDA(cudaMemcpyAsync(ns.data(), p->tile_ns, ns.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                s));
+      SHAW_CUDA(cudaStreamSynchronize(s));
+      std::snprintf(line, sizeof(line), "width %u: %zu tiles on %u CTAs, model schedule %.3f ms", W,
+                    p->tiles.size(), p->ctas, ms_model);
+      report += line;
+      if (ms_model < best.ms) best = {ms_model, W, p->tiles, p->order, p->begin, p->ctas, "model"};
+      // schedule from the measured tile times
+      std::vector<double> cost(ns.begin(), ns.end());
+      double mk = 0.0;
+      lpt_schedule(cost, p->ctas, p->order, p->begin, mk);
+      p->sched_source = "measured";
+      p->tiles_dirty = true;
+      float ms_meas = 0.f;
+      if ((rc = timed(ms_meas))) break;
+      std::snprintf(line, sizeof(line), ", measured schedule %.3f ms\n", ms_meas);
+      report += line;
+      if (ms_meas < best.ms) best = {ms_meas, W, p->tiles, p->order, p->begin, p->ctas, "measured"};
+    }
+  } while (false);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  p->width = best.width;
+  p->tiles = best.tiles;
+  p->order = best.order;
+  p->begin = best.begin;
+  p->ctas = best.ctas;
+  p->sched_source = best.source;
+  p->tiles_dirty = true;
+  std::snprintf(line, sizeof(line), "chosen: width %u, %s schedule, %.3f ms per %llu steps\n", best.width,
+                best.source.c_str(), best.ms, trial_steps);
+  report += line;
+  return reset(p, s);
+}
+
+std::string describe(const Batch* p) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "tile width %u, %zu tiles, %u CTAs, %s schedule", p->width, p->tiles.size(),
+                p->ctas, p->sched_source.c_str());
+  return buf;
+}
+
+uint32_t num_ctas(const Batch* p) { return p->ctas; }
+
+void destroy(Batch* p) {
   if (!p) return;
-  void* bufs[] = {p->Av, p->As, p->bvt, p->bst, p->alpha_v, p->alpha_s, p->bh, p->bl,
-                  p->xvh, p->xvl, p->xsh, p->xsl, p->error};
+  for (void* b : p->owned) cudaFree(b);
+  void* bufs[] = {p->d_inst, p->d_tiles, p->d_order, p->d_begin, p->bvt, p->bst, p->error, p->tile_ns};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete p;

@@ -1,29 +1,47 @@
-// rom_oz.h -- host interface of the Ozaki-scheme BF16 tensor-core rank-2 ROM leapfrog (rom_oz.cu).
+// rom_oz.h -- host interface of the Ozaki-scheme BF16 tensor-core rank-2 ROM leapfrog
+// (rom_oz.cu).  One Batch advances one or many independent reduced systems (instances of
+// their own kv, ks and forcing count M) in a single persistent launch.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 namespace shaw {
 namespace oz {
 
-struct Plan;
+// One reduced system: Av kv x ks and As ks x kv row-major, b kv x M LayoutLeft (host arrays).
+struct InstanceDesc {
+  uint32_t kv = 0, ks = 0, M = 0;
+  const double *Av = nullptr, *As = nullptr, *b = nullptr;
+};
 
-// Slice the FP64 reduced operators (HOST, row-major) into row-scaled BF16 slices and
-// allocate the split state; hAv kv x ks, hAs ks x kv, hb kv x M (LayoutLeft), host arrays.
-int create(Plan*& p, uint32_t kv, uint32_t ks, const double* hAv, const double* hAs, uint32_t M,
-           const double* hb, cudaStream_t s);
-int reset(Plan* p, cudaStream_t s);
-// nsteps leapfrog steps starting after step step0, one persistent launch.
-int advance(Plan* p, cudaStream_t s, double dt, unsigned long long step0, unsigned long long nsteps,
-            const int* kind, const double* period, const double* delay, double* snap_vp, double* snap_sp,
-            unsigned long long Tvp, unsigned long long Tsp, uint32_t fvp, uint32_t fsp);
+struct Batch;
+
+// Slice every instance's operators into row-scaled BF16 slices, allocate the split
+// states, and pick the default tiling (tile width 32 columns, LPT schedule).
+int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s);
+// Per-column signals of instance i (device arrays of M entries, owned by the caller).
+int set_signals(Batch* p, uint32_t i, const int* kind, const double* period, const double* delay);
+// Device snapshot buffers of instance i (k x T x M LayoutLeft), or nullptr / frequency 0.
+int set_snapshots(Batch* p, uint32_t i, double* snap_vp, double* snap_sp, unsigned long long Tvp,
+                  unsigned long long Tsp, uint32_t fvp, uint32_t fsp);
+int reset(Batch* p, cudaStream_t s);
+// nsteps leapfrog steps of every instance, starting after step step0: one persistent launch.
+int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsigned long long nsteps);
 // SHAW_ERR_CUDA if a bounded pipeline wait ran out in the last launches.
-int check(Plan* p, cudaStream_t s);
-// FP64 copy of the states (device buffers kv x M and ks x M, LayoutLeft).
-int get_state(Plan* p, cudaStream_t s, double* dxv, double* dxs);
-void destroy(Plan* p);
+int check(Batch* p, cudaStream_t s);
+// FP64 copy of instance i's states (device buffers kv x M and ks x M, LayoutLeft).
+int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs);
+// Autotuner: times every tile width in {16, 32, 64} with a model-cost LPT schedule and a
+// schedule rebuilt from the measured per-tile times, keeps the fastest, and leaves all
+// states reset to zero.  `report` receives one line per candidate.
+int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report);
+// The current tiling in words (width, tiles, CTAs, schedule source).
+std::string describe(const Batch* p);
+uint32_t num_ctas(const Batch* p);
+void destroy(Batch* p);
 
 }  // namespace oz
 }  // namespace shaw

@@ -1,0 +1,142 @@
+"""Batched rank-2 ROM: many reduced systems of uneven size in one handle.
+
+Each instance is runRomRankTwoForcing's system (src/kokkos/torevise/
+run_rom_rank_two_forcing.hpp:149-188).  FP64 batches are held to 1e-12 of the oracle
+per instance; the tensor-core (Ozaki) batch must equal the single-system tensor-core
+path bit for bit (exact accumulation makes the result independent of the tiling) and
+stay within 1e-9 of FP64.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from test_rom_gpu import relerr, stable_system
+
+pytestmark = pytest.mark.gpu
+
+# (kv, ks, M): uneven modes (not multiples of 128 included) and forcing counts
+SHAPES = [(100, 72, 5), (128, 128, 37), (40, 40, 1), (256, 200, 70), (64, 96, 16)]
+
+
+def _instances(seed, shapes=SHAPES, smax=0.2):
+    rng = np.random.default_rng(seed)
+    out = []
+    for kv, ks, M in shapes:
+        kmin = min(kv, ks)
+        av, as_, _ = stable_system(kmin, int(rng.integers(1 << 30)))
+        big_v = np.zeros((kv, ks))
+        big_v[:kmin, :kmin] = av * smax
+        big_s = np.zeros((ks, kv))
+        big_s[:kmin, :kmin] = as_ * smax
+        out.append(dict(rom_jvp=big_v, rom_jsp=big_s, b=rng.standard_normal((kv, M)) * 1e-3,
+                        kind=rng.integers(0, 3, M), period=rng.uniform(30, 90, M), delay=rng.uniform(0, 60, M)))
+    return out
+
+
+def test_batch_fp64_matches_oracle(shaw, oracle):
+    insts = _instances(1)
+    n, dt = 300, 0.5
+    bt = shaw.RomBatch(insts, precision=shaw.FP64)
+    for i in range(len(insts)):
+        bt.set_snapshots(i, 3, 5, n)
+    bt.run(dt, n)
+    for i, d in enumerate(insts):
+        ref = oracle.rom_run(d["rom_jvp"], d["rom_jsp"], d["b"], n, dt, d["kind"], d["period"], d["delay"], 3, 5)
+        xv, xs = bt.get_state(i)
+        assert relerr(xv, ref["final_vp"]) <= 1e-12 and relerr(xs, ref["final_sp"]) <= 1e-12
+        svp, ssp = bt.snapshots(i)
+        assert relerr(svp, ref["snaps_vp"]) <= 1e-12 and relerr(ssp, ref["snaps_sp"]) <= 1e-12
+
+
+def test_batch_fp64_equals_single_system_path(shaw):
+    insts = _instances(2)
+    n, dt = 120, 0.5
+    bt = shaw.RomBatch(insts, precision=shaw.FP64)
+    bt.run(dt, n)
+    for i, d in enumerate(insts):
+        r = shaw.Rom(d["rom_jvp"], d["rom_jsp"], d["b"], rank=2)
+        r.set_signals(d["kind"], d["period"], d["delay"])
+        r.run(dt, n)
+        a, b = bt.get_state(i), r.get_state()
+        assert relerr(a[0], b[0]) <= 1e-14 and relerr(a[1], b[1]) <= 1e-14
+        r.close()
+
+
+def test_batch_ozaki_bitwise_equals_single_system(shaw):
+    insts = _instances(3)
+    n, dt = 150, 0.5
+    bt = shaw.RomBatch(insts, precision=shaw.MIXED_OZAKI_BF16)
+    bt.run(dt, n)
+    single = []
+    for d in insts:
+        r = shaw.Rom(d["rom_jvp"], d["rom_jsp"], d["b"], rank=2, precision=shaw.MIXED_OZAKI_BF16)
+        r.set_signals(d["kind"], d["period"], d["delay"])
+        r.run(dt, n)
+        single.append(r.get_state())
+        r.close()
+    for i in range(len(insts)):
+        a = bt.get_state(i)
+        assert np.array_equal(a[0], single[i][0]) and np.array_equal(a[1], single[i][1])
+    # the autotuner changes tile widths and the schedule, never the numbers
+    report = bt.tune(dt, 3)
+    assert "chosen" in report
+    bt.run(dt, n)
+    for i in range(len(insts)):
+        a = bt.get_state(i)
+        assert np.array_equal(a[0], single[i][0]) and np.array_equal(a[1], single[i][1])
+
+
+def test_batch_ozaki_within_1e9_of_fp64(shaw):
+    insts = _instances(4)
+    n, dt = 1000, 0.5
+    res = {}
+    for p in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
+        bt = shaw.RomBatch(insts, precision=p)
+        for i in range(len(insts)):
+            bt.set_snapshots(i, 100, 100, n)
+        bt.run(dt, n)
+        res[p] = [(bt.get_state(i), bt.snapshots(i)) for i in range(len(insts))]
+        bt.close()
+    for i in range(len(insts)):
+        (x64, s64), (xoz, soz) = res[shaw.FP64][i], res[shaw.MIXED_OZAKI_BF16][i]
+        errs = [relerr(xoz[0], x64[0]), relerr(xoz[1], x64[1]), relerr(soz[0], s64[0]), relerr(soz[1], s64[1])]
+        assert max(errs) <= 1e-9, (i, errs)
+
+
+def test_batch_ozaki_advance_in_pieces_and_tiles(shaw):
+    insts = _instances(5, shapes=[(384, 256, 100), (128, 128, 3), (512, 512, 33)])
+    bt = shaw.RomBatch(insts, precision=shaw.MIXED_OZAKI_BF16)
+    bt.run(0.5, 90)
+    whole = [bt.get_state(i) for i in range(3)]
+    bt.reset()
+    bt.advance(0.5, 10)
+    bt.advance(0.5, 80)
+    bt.synchronize()
+    for i in range(3):
+        part = bt.get_state(i)
+        assert np.array_equal(whole[i][0], part[0]) and np.array_equal(whole[i][1], part[1])
+    assert "tile width" in bt.describe()
+
+
+def test_batch_errors(shaw):
+    good = _instances(6, shapes=[(32, 32, 4)])
+    with pytest.raises(shaw.ShawError) as e:
+        shaw.RomBatch(good, precision=shaw.MIXED_TF32X3)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    big = _instances(6, shapes=[(1100, 64, 2)])
+    with pytest.raises(shaw.ShawError) as e:
+        shaw.RomBatch(big, precision=shaw.MIXED_OZAKI_BF16)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    bad = _instances(6, shapes=[(32, 32, 4)])
+    bad[0]["period"] = np.array([30.0, -1.0, 30.0, 30.0])
+    with pytest.raises(shaw.ShawError) as e:
+        shaw.RomBatch(bad, precision=shaw.FP64)
+    assert e.value.code == shaw.ERR_INVALID_ARG
+    bt = shaw.RomBatch(good, precision=shaw.FP64)
+    x = np.zeros(32 * 4)
+    xp = x.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    assert shaw.lib().shaw_rom_batch_get_state(bt.h, 3, xp, xp) == shaw.ERR_INVALID_ARG  # no instance 3
+    bt.set_snapshots(0, 2, 2, 10)
+    with pytest.raises(shaw.ShawError):
+        bt.advance(0.5, 11)
