@@ -55,10 +55,14 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def workload_inputs(np, mesh):
+def workload_inputs(np, mesh, rank=0, world=1):
+    """This rank's M forcing columns of the job's world * M seeded draws."""
+    from shaw_gb300.sharding import shard_range
     rng = np.random.default_rng(SEED)
-    depths = rng.uniform(200.0, 700.0, M)
-    periods = rng.uniform(30.0, 90.0, M)
+    depths = rng.uniform(200.0, 700.0, M * world)
+    periods = rng.uniform(30.0, 90.0, M * world)
+    lo, hi = shard_range(M * world, rank, world)
+    depths, periods = depths[lo:hi], periods[lo:hi]
     gids = [mesh.map_source(float(d), 0.0) for d in depths]
     rcv = [mesh.map_receiver(float(a)) for a in range(0, 181)]
     dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
@@ -380,7 +384,7 @@ def run_ours(args):
 
     mesh = shaw.Mesh.generate(NTH, NR)
     mesh.set_material("unilayer", MATERIAL)
-    gids, periods, rcv, dt = workload_inputs(np, mesh)
+    gids, periods, rcv, dt = workload_inputs(np, mesh, rank, world)
     dofs = (mesh.nvp + mesh.nsp) * M
     total_steps = args.warmup + args.steps
 
@@ -452,6 +456,11 @@ def run_ours(args):
     h2d = (mesh.nvp * (5 * 8 + 2 * 8 + 8 + 4 * 8 + 8) + mesh.nsp * (3 * 8 + 4 + 2 * 8 + 8 + 8)  # desc arrays
            + M * (8 + 4 + 8 + 8) + len(rcv) * 8)
     d2h = seis.nbytes
+    gathered = M
+    if dist:  # host gather of every rank's seismogram columns onto rank 0 (after the timed regions)
+        from shaw_gb300.sharding import gather_columns
+        full = gather_columns(seis, M * world, dist, group=dist.new_group(backend="gloo"))
+        gathered = full.shape[-1] if full is not None else 0
 
     if rank != 0:
         if dist:
@@ -471,7 +480,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings_per_gpu": M, "dt": dt,
                    "receivers": len(rcv), "seismogram_freq": 1,
                    "l2": "inputs larger than L2 (state 12.3 GB per GPU), no flush needed",
-                   "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU"},
+                   "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU",
+                   "seismogram_columns_gathered": gathered},
         "roofline": {"bound": "hbm", "kernel": "fom_stress_kernel", "achieved": ach, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm,
                      "traffic": TRAFFIC_STRESS_PER_FORCING * M,
