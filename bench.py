@@ -226,42 +226,56 @@ def extra_workloads(np, torch, shaw):
     out["fom_rank1_101x201"] = {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t,
                                 "steps": n, "us_per_step": t / n * 1e6}
     f.close()
-    # config 3: ROM rank-1, k = 256, 20000 steps, FP64 vs mixed (FP32 hi+lo, compensated)
-    k, n, dtr = 256, 20000, 0.5
-    av, as_ = stable_rom(np, k, 3, 0.004, 0.2)
-    b = np.random.default_rng(4).standard_normal(k) * 1e-3
-    rows = np.random.default_rng(5).standard_normal((181, k)) / np.sqrt(k)
+    basis = pod_basis(np, shaw, mesh, dt)
+    rcv = [mesh.map_receiver(float(a)) for a in range(181)]
+    rho_inv = mesh.arrays()["rho_inv_vp"]
+
+    def forcing_vectors(k, gids):
+        g = np.asarray(gids)
+        return np.asfortranarray(basis["phi_v"][g, :k].T * rho_inv[g][None, :])
+
+    # config 3: ROM rank-1, kv = ks = 256 modes, one new forcing (depth U[200,700] km,
+    # period U[30,90] s), 20000 steps, FP64 vs mixed (FP32 hi + lo, compensated)
+    k, n = 256, 20000
+    rng = np.random.default_rng(SEED + 3)
+    depth, period = float(rng.uniform(200.0, 700.0)), float(rng.uniform(30.0, 90.0))
+    av, as_ = basis["av"][:k, :k], basis["as"][:k, :k]
+    b = forcing_vectors(k, [mesh.map_source(depth, 0.0)])[:, 0]
+    rows = np.ascontiguousarray(basis["phi_v"][rcv, :k])
     res = {}
     for prec in (shaw.FP64, shaw.MIXED_FP32):
         r = shaw.Rom(av, as_, b, rank=1, precision=prec)
-        r.set_signals("gaussDer", 60.0, 180.0)
+        r.set_signals("gaussDer", period, 180.0)
         r.set_receivers(rows, 1, n)
         r.reset()
-        t = _timed(torch, r.stream, lambda: r.advance(dtr, n))
+        t = _timed(torch, r.stream, lambda: r.advance(dt, n))
         r.synchronize()
         res[prec] = (t, r.seismogram())
         r.close()
     out["rom_rank1_k256"] = {"metric": "ROM forcing-steps/s", "steps": n,
                              "fp64": n / res[shaw.FP64][0], "mixed_fp32": n / res[shaw.MIXED_FP32][0],
                              "speedup": res[shaw.FP64][0] / res[shaw.MIXED_FP32][0],
-                             "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1])}
+                             "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
+                             "seismogram_max_abs": float(np.max(np.abs(res[shaw.FP64][1]))),
+                             "forcing": {"depth_km": depth, "period_s": period, "delay_s": 180.0},
+                             "basis": basis["info"]}
     # config 4: ROM rank-2, k = 512, M = 4096 forcings; FP64 (DGEMM) vs tensor-core forms
     k, M, n = 512, 4096, 100
-    av, as_ = stable_rom(np, k, 7, 0.004, 0.2)
-    rng = np.random.default_rng(8)
-    b = rng.standard_normal((k, M)) * 1e-3
-    periods = rng.uniform(30.0, 90.0, M)
-    rows = rng.standard_normal((181, k)) / np.sqrt(k)
+    rng = np.random.default_rng(SEED + 4)
+    depths, periods = rng.uniform(200.0, 700.0, M), rng.uniform(30.0, 90.0, M)
+    av, as_ = basis["av"][:k, :k], basis["as"][:k, :k]
+    b = forcing_vectors(k, [mesh.map_source(float(d), 0.0) for d in depths])
+    rows = basis["phi_v"][rcv, :k]
     res = {}
     for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.MIXED_TF32X3):
         r = shaw.Rom(av, as_, b, rank=2, precision=prec)
         r.set_signals("gaussDer", periods, 180.0)
         r.set_snapshots(n // 4, n // 4, n)
         r.reset()
-        r.advance(dtr, 2 if prec == shaw.FP64 else n)  # warm-up
+        r.advance(dt, 2 if prec == shaw.FP64 else n)  # warm-up
         r.synchronize()
         r.reset()
-        t = _timed(torch, r.stream, lambda: r.advance(dtr, n))
+        t = _timed(torch, r.stream, lambda: r.advance(dt, n))
         r.synchronize()
         snaps = r.snapshots()[0]
         res[prec] = (t, np.einsum("rk,ktm->rtm", rows, snaps), r.get_state()[0])
@@ -274,27 +288,61 @@ def extra_workloads(np, torch, shaw):
         "seismogram_rel_err_ozaki": _relerr(np, res[shaw.MIXED_OZAKI_BF16][1], res[shaw.FP64][1]),
         "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
-        "operators": "seeded synthetic pair with As = -Av^T (bounded leapfrog), dt*sigma in [0.002, 0.1]"}
-    out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw)
+        "basis": "leading 512 modes of the POD basis of config 3"}
+    out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
     return out
 
 
-def batched_workload(np, torch, shaw, n_inst=64, seed=20261205):
-    """64 reduced systems, k ~ U{64, 128, ..., 1024}, M ~ U[16, 2048] (seeded), advanced
-    together: FP64 (cuBLAS DGEMM per instance) vs the Ozaki tensor-core batch (one
-    persistent launch, autotuned tile widths and schedule)."""
+def pod_basis(np, shaw, mesh, dt, kmax=1024, n_train=8):
+    """FOM -> POD -> Galerkin projection, all on the GPU, on the 101 x 201 grid of config 1.
+
+    Training: the config-1 source (640 km on the axis, period 60 s) plus 7 seeded sources
+    (depth U[200,700] km, angle U[0,180] deg, period U[30,90] s), 2000 steps, snapshots
+    every 5 steps: 400 snapshots per forcing, 3200 per dof.  (The 400 snapshots of the
+    config-1 source alone have numerical rank 175 < 256; their 256-mode Galerkin system
+    has an eigenvalue of dt^2 As Av with positive real part and the leapfrog diverges.)"""
+    rng = np.random.default_rng(5)
+    specs = [(640.0, 0.0, 60.0)] + [(float(rng.uniform(200, 700)), float(rng.uniform(0, 180)),
+                                     float(rng.uniform(30, 90))) for _ in range(n_train - 1)]
+    t0 = time.perf_counter()
+    f = shaw.Fom(mesh, 2, n_train)
+    f.set_sources([mesh.map_source(d, a) for d, a, _ in specs], "gaussDer", [p for _, _, p in specs], 180.0)
+    f.set_snapshots(5, 5, 2000)
+    f.run(dt, 2000)
+    svp, ssp = f.snapshots()
+    t_fom = time.perf_counter() - t0
+    phi_v, sv_v = shaw.pod(svp.reshape(svp.shape[0], -1, order="F"), method=2)
+    phi_s, sv_s = shaw.pod(ssp.reshape(ssp.shape[0], -1, order="F"), method=2)
+    t_pod = time.perf_counter() - t0 - t_fom
+    phi_v, phi_s = np.asfortranarray(phi_v[:, :kmax]), np.asfortranarray(phi_s[:, :kmax])
+    av, as_ = shaw.rom_project(f, phi_v, phi_s)
+    t_all = time.perf_counter() - t0
+    f.close()
+    info = ("POD of 3200 FOM snapshots per dof (8 training forcings x 400, config-1 grid): FOM %.2f s, "
+            "thin SVDs %.2f s, projection to %d modes %.2f s (GPU); sigma_k/sigma_1 (vp) k=256 %.1e, "
+            "512 %.1e, 1024 %.1e" % (t_fom, t_pod, kmax, t_all - t_fom - t_pod, sv_v[255] / sv_v[0],
+                                     sv_v[511] / sv_v[0], sv_v[kmax - 1] / sv_v[0]))
+    return {"phi_v": phi_v, "phi_s": phi_s, "av": av, "as": as_, "info": info}
+
+
+def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_inst=64, seed=20261205):
+    """64 reduced systems, k ~ U{64, 128, ..., 1024}, M ~ U[16, 2048] (seeded), each the
+    leading k modes of the POD basis with its own M axis sources (depth U[200,700] km,
+    period U[30,90] s), advanced together: FP64 (cuBLAS DGEMM per instance) vs the Ozaki
+    tensor-core batch (one persistent launch, autotuned tile widths and schedule)."""
     rng = np.random.default_rng(seed)
     ks = rng.integers(1, 17, n_inst) * 64
     Ms = rng.integers(16, 2049, n_inst)
     insts = []
-    for i, (k, M) in enumerate(zip(ks, Ms)):
-        av, as_ = stable_rom(np, int(k), seed + i, 0.004, 0.2)
-        insts.append(dict(rom_jvp=av, rom_jsp=as_, b=rng.standard_normal((k, M)) * 1e-3, kind="gaussDer",
-                          period=rng.uniform(30.0, 90.0, M), delay=180.0))
+    for k, M in zip(ks, Ms):
+        k = int(k)
+        gids = [mesh.map_source(float(d), 0.0) for d in rng.uniform(200.0, 700.0, M)]
+        insts.append(dict(rom_jvp=basis["av"][:k, :k], rom_jsp=basis["as"][:k, :k], b=forcing_vectors(k, gids),
+                          kind="gaussDer", period=rng.uniform(30.0, 90.0, M), delay=180.0))
     flops = float(sum(4.0 * k * k * M for k, M in zip(ks, Ms)))
     cols = int(Ms.sum())
-    dtr, n64, n_oz, n_cmp = 0.5, 6, 120, 6
-    rows = {i: np.random.default_rng(i).standard_normal((181, int(ks[i]))) / np.sqrt(ks[i]) for i in range(n_inst)}
+    dtr, n64, n_oz, n_cmp = dt, 6, 120, 6
+    rows = {i: basis["phi_v"][rcv, :int(ks[i])] for i in range(n_inst)}
     res = {}
     for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
         bt = shaw.RomBatch(insts, precision=prec)
