@@ -290,7 +290,44 @@ def extra_workloads(np, torch, shaw):
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
         "basis": "leading 512 modes of the POD basis of config 3"}
     out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
+    out["fom_rank2_2000x4000_M64"] = fom_fp64_vs_fp32(np, torch, shaw)
     return out
+
+
+def fom_fp64_vs_fp32(np, torch, shaw, nth=2000, nr=4000, M=64, n_time=20, n_err=1000):
+    """Config 5's FOM job: 2000 theta x 4000 r grid, M = 64 forcings (depth U[200,700] km,
+    period U[30,90] s, seeded), FP64 vs FP32 state.  Error probe: velocity traces over
+    n_err steps at the 64 source points and 10 grid rows (7 km) above each (the surface
+    receivers see nothing before t = delay + travel time, ~13000 steps at this dt)."""
+    mesh = shaw.Mesh.generate(nth, nr)
+    mesh.set_material("unilayer", MATERIAL)
+    dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
+    rng = np.random.default_rng(SEED + 5)
+    gids = [mesh.map_source(float(d), 0.0) for d in rng.uniform(200.0, 700.0, M)]
+    periods = rng.uniform(30.0, 90.0, M)
+    probe = list(gids) + [g + 10 * nth for g in gids]
+    dofs = (mesh.nvp + mesh.nsp) * M
+    res = {}
+    for prec in (shaw.FP64, shaw.MIXED_FP32):
+        f = shaw.Fom(mesh, 2, M, precision=prec)
+        f.set_sources(gids, "gaussDer", periods, 180.0)
+        f.set_receivers(probe, 1, n_err)
+        f.reset()
+        f.advance(dt, 3)  # warm-up
+        f.synchronize()
+        f.reset()
+        t = _timed(torch, f.stream, lambda: f.advance(dt, n_time))
+        f.synchronize()
+        f.run(dt, n_err)
+        res[prec] = (t, f.seismogram())
+        f.close()
+    v64, v32 = dofs * n_time / res[shaw.FP64][0], dofs * n_time / res[shaw.MIXED_FP32][0]
+    return {"metric": "FOM DOF-updates/s", "grid": [nth, nr], "forcings": M, "fp64": v64, "mixed_fp32": v32,
+            "speedup": v32 / v64, "timed_steps": n_time,
+            "trace_rel_err_fp32": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
+            "error_probe": "velocity at the 64 source points and 7 km above them, every step",
+            "error_after_steps": n_err,
+            "mixed_fp32_bytes_per_dof_update": 8, "fp64_bytes_per_dof_update": 16}
 
 
 def pod_basis(np, shaw, mesh, dt, kmax=1024, n_train=8):

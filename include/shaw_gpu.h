@@ -67,7 +67,7 @@ extern "C" {
 #define SHAW_FP64             0  /* plain FP64 (the oracle-parity path)                     */
 #define SHAW_MIXED_TF32X3     1  /* ROM: split TF32x3 products, FP32 accumulate, Kahan state */
 #define SHAW_MIXED_BF16X3     2  /* ROM: split BF16x3 products, FP32 accumulate, Kahan state */
-#define SHAW_MIXED_FP32       3  /* FP32 products, Kahan-compensated FP32 state             */
+#define SHAW_MIXED_FP32       3  /* ROM rank 1: FP32 hi+lo arithmetic; FOM: FP32 state     */
 #define SHAW_MIXED_OZAKI_BF16 4  /* ROM rank 2: BF16 tensor cores, 6 six-bit slices per
                                     operand (Ozaki scheme), exact FP32 accumulation,
                                     compensated FP32 state: FP64-grade GEMMs              */
@@ -103,7 +103,11 @@ typedef struct shaw_fom_s* shaw_fom_t;
 /* ShWavePP ctor + state allocation of FomProblemRank{One,Two}Forcing.
  * rank 1: one forcing, vector state, source added as KokkosBlas::mult does;
  * rank 2: num_forcings columns, source added as AddForcingRank2 does.
- * precision: SHAW_FP64. */
+ * precision: SHAW_FP64, or SHAW_MIXED_FP32: FP32 state and dt-folded stencil values
+ * (rounded from the FP64 values), FP32 FMAs, source increments computed in FP64 and
+ * rounded once; half the HBM bytes of FP64.  Snapshots, seismograms and states are
+ * returned in FP64.  Not an oracle-parity path: its seismograms differ from FP64 by
+ * ~1e-6 relative (measured, grows slowly with grid size and step count). */
 int shaw_fom_create(const shaw_fom_operator_desc* desc, int rank, uint32_t num_forcings, int precision,
                     shaw_fom_t* out);
 void shaw_fom_destroy(shaw_fom_t h);

@@ -63,12 +63,13 @@ struct FomCtl {
   unsigned int pad;
 };
 
-// Arguments shared by both half-step kernels (passed by value, < 4 KB).
+// Arguments shared by both half-step kernels (passed by value, < 4 KB).  The state
+// and the folded stencil values are FP64 (SHAW_FP64) or FP32 (SHAW_MIXED_FP32).
 struct FomArgs {
-  double* xv;          // [nvp][M]
-  double* xs;          // [nsp][M]
-  const double* cvp;   // 4 planes of nvp: N, S, W, E (dt folded)
-  const double* csp;   // 2 planes of nsp: A, B (dt folded)
+  void* xv;            // [nvp][M]
+  void* xs;            // [nsp][M]
+  const void* cvp;     // 4 planes of nvp: N, S, W, E (dt folded)
+  const void* csp;     // 2 planes of nsp: A, B (dt folded)
   const double* rho_inv;
   const unsigned long long* src;  // [M] source vp gid per column
   const int* kind;
@@ -87,19 +88,32 @@ struct FomArgs {
   FastDiv chunks_div, nth_div, sprow_div;
 };
 
-template <int VEC>
+// VEC consecutive columns of one point as one vector load/store (16 bytes at most).
+template <typename T, int VEC>
 struct VecT;
-template <>
-struct VecT<1> {
-  using type = double;
-  __device__ static double ld(const double* p) { return *p; }
-  __device__ static void st(double* p, double v) { *p = v; }
+template <typename T>
+struct VecT<T, 1> {
+  using type = T;
+  __device__ static T ld(const T* p) { return *p; }
+  __device__ static void st(T* p, T v) { *p = v; }
 };
 template <>
-struct VecT<2> {
+struct VecT<double, 2> {
   using type = double2;
   __device__ static double2 ld(const double* p) { return *reinterpret_cast<const double2*>(p); }
   __device__ static void st(double* p, double2 v) { *reinterpret_cast<double2*>(p) = v; }
+};
+template <>
+struct VecT<float, 2> {
+  using type = float2;
+  __device__ static float2 ld(const float* p) { return *reinterpret_cast<const float2*>(p); }
+  __device__ static void st(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+};
+template <>
+struct VecT<float, 4> {
+  using type = float4;
+  __device__ static float4 ld(const float* p) { return *reinterpret_cast<const float4*>(p); }
+  __device__ static void st(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 };
 
 __device__ __forceinline__ void fma_into(double& acc, double c, double x) { acc = fma(c, x, acc); }
@@ -107,8 +121,22 @@ __device__ __forceinline__ void fma_into(double2& acc, double c, double2 x) {
   acc.x = fma(c, x.x, acc.x);
   acc.y = fma(c, x.y, acc.y);
 }
+__device__ __forceinline__ void fma_into(float& acc, float c, float x) { acc = fmaf(c, x, acc); }
+__device__ __forceinline__ void fma_into(float2& acc, float c, float2 x) {
+  acc.x = fmaf(c, x.x, acc.x);
+  acc.y = fmaf(c, x.y, acc.y);
+}
+__device__ __forceinline__ void fma_into(float4& acc, float c, float4 x) {
+  acc.x = fmaf(c, x.x, acc.x);
+  acc.y = fmaf(c, x.y, acc.y);
+  acc.z = fmaf(c, x.z, acc.z);
+  acc.w = fmaf(c, x.w, acc.w);
+}
 __device__ __forceinline__ double& lane(double& v, int) { return v; }
 __device__ __forceinline__ double& lane(double2& v, int e) { return e == 0 ? v.x : v.y; }
+__device__ __forceinline__ float& lane(float& v, int) { return v; }
+__device__ __forceinline__ float& lane(float2& v, int e) { return e == 0 ? v.x : v.y; }
+__device__ __forceinline__ float& lane(float4& v, int e) { return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w; }
 
 // sp gid of the stp point of cell (j, i): interleaved numbering of the mesher.
 __device__ __forceinline__ uint32_t stp_gid(uint32_t j, uint32_t i, const FomArgs& a) {
@@ -127,19 +155,49 @@ __device__ __noinline__ double add_forcing(double x, const FomArgs& a, uint32_t 
   if (a.rank2) return __dadd_rn(x, __dmul_rn(__dmul_rn(ri, f), a.dt));  // AddForcingRank2: x += rhoInv*f*dt
   return __dadd_rn(x, __dmul_rn(__dmul_rn(a.dt, ri), f));              // KokkosBlas::mult(1, x, dt, rhoInv, f)
 }
+// FP32 state: the source increment in FP64, in the same order, rounded once.
+__device__ __noinline__ float add_forcing(float x, const FomArgs& a, uint32_t m, uint32_t p, uint32_t k_local,
+                                          unsigned long long host_step) {
+  const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
+  const double t = (double)(n - 1) * a.dt;
+  const double f = shaw::signal_value(a.kind[m], a.delay[m], a.period[m], t);
+  const double ri = a.rho_inv[p];
+  const double inc = a.rank2 ? __dmul_rn(__dmul_rn(ri, f), a.dt) : __dmul_rn(__dmul_rn(a.dt, ri), f);
+  return x + __double2float_rn(inc);
+}
+
+// Forcing of the VEC columns c*VEC.. that this thread owns at vp point p.
+template <typename V, int VEC>
+__device__ __forceinline__ void apply_forcing(V& v, const FomArgs& a, uint32_t c, uint32_t p, uint32_t k_local,
+                                              unsigned long long host_step) {
+  if (VEC == 1) {
+    if (a.src[c] == p) lane(v, 0) = add_forcing(lane(v, 0), a, c, p, k_local, host_step);
+  } else {
+#pragma unroll
+    for (int h = 0; h < VEC / 2; ++h) {
+      const ulonglong2 s2 = __ldg(reinterpret_cast<const ulonglong2*>(a.src) + (VEC / 2) * c + h);
+      const uint32_t m0 = VEC * c + 2 * h;
+      if (s2.x == p) lane(v, 2 * h) = add_forcing(lane(v, 2 * h), a, m0, p, k_local, host_step);
+      if (s2.y == p) lane(v, 2 * h + 1) = add_forcing(lane(v, 2 * h + 1), a, m0 + 1, p, k_local, host_step);
+    }
+  }
+}
 
 // updateVelocity (fom_update_kernels.hpp:60-90 rank-1, :132-167 rank-2) for one step.
-template <int VEC>
+template <typename T, int VEC>
 __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint32_t k_local,
                                                                 unsigned long long host_step) {
-  using V = VecT<VEC>;
+  using V = VecT<T, VEC>;
+  T* const xv = static_cast<T*>(a.xv);
+  const T* const xs = static_cast<const T*>(a.xs);
+  const T* const cvp = static_cast<const T*>(a.cvp);
   const uint32_t item = blockIdx.x * kThreads + threadIdx.x;
   if (item >= a.vp_items) return;
   const uint32_t p = shaw::fast_div(item, a.chunks_div);
   const uint32_t c = item - p * a.chunks;
   const uint32_t j = shaw::fast_div(p, a.nth_div);
   const uint32_t i = p - j * a.nth;
-  double* xp = a.xv + (size_t)p * a.M + c * VEC;
+  T* xp = xv + (size_t)p * a.M + c * VEC;
   typename V::type v = V::ld(xp);
   if (i != 0 && i + 1 != a.nth) {
     // interior theta: N/S are srp points, W/E stp points.  At the CMB (j == 0)
@@ -151,32 +209,29 @@ __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint3
     const uint32_t gW = stp_gid(j, i - 1, a);
     const uint32_t gE = stp_gid(j, i, a);
     const size_t nvp = (size_t)a.nth * a.nr;
-    const double cN = __ldg(a.cvp + p);
-    const double cS = __ldg(a.cvp + nvp + p);
-    const double cW = __ldg(a.cvp + 2 * nvp + p);
-    const double cE = __ldg(a.cvp + 3 * nvp + p);
+    const T cN = __ldg(cvp + p);
+    const T cS = __ldg(cvp + nvp + p);
+    const T cW = __ldg(cvp + 2 * nvp + p);
+    const T cE = __ldg(cvp + 3 * nvp + p);
     const size_t off = (size_t)c * VEC;
-    fma_into(v, cN, V::ld(a.xs + (size_t)gN * a.M + off));
-    fma_into(v, cS, V::ld(a.xs + (size_t)gS * a.M + off));
-    fma_into(v, cW, V::ld(a.xs + (size_t)gW * a.M + off));
-    fma_into(v, cE, V::ld(a.xs + (size_t)gE * a.M + off));
+    fma_into(v, cN, V::ld(xs + (size_t)gN * a.M + off));
+    fma_into(v, cS, V::ld(xs + (size_t)gS * a.M + off));
+    fma_into(v, cW, V::ld(xs + (size_t)gW * a.M + off));
+    fma_into(v, cE, V::ld(xs + (size_t)gE * a.M + off));
   }
   // forcing: the thread owning (src[m], m) adds it, evaluating the signal at t_{n-1}
-  if (VEC == 1) {
-    if (a.src[c] == p) lane(v, 0) = add_forcing(lane(v, 0), a, c, p, k_local, host_step);
-  } else {
-    const ulonglong2 s2 = __ldg(reinterpret_cast<const ulonglong2*>(a.src) + c);
-    if (s2.x == p) lane(v, 0) = add_forcing(lane(v, 0), a, 2 * c, p, k_local, host_step);
-    if (s2.y == p) lane(v, 1) = add_forcing(lane(v, 1), a, 2 * c + 1, p, k_local, host_step);
-  }
+  apply_forcing<typename V::type, VEC>(v, a, c, p, k_local, host_step);
   V::st(xp, v);
 }
 
 // updateStress (fom_update_kernels.hpp:93-104, :170-181) + fused receiver gather.
-template <int VEC>
+template <typename T, int VEC>
 __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_t k_local,
                                                               unsigned long long host_step) {
-  using V = VecT<VEC>;
+  using V = VecT<T, VEC>;
+  const T* const xv = static_cast<const T*>(a.xv);
+  T* const xs = static_cast<T*>(a.xs);
+  const T* const csp = static_cast<const T*>(a.csp);
   if (blockIdx.x >= a.sp_blocks) {
     // Seismogram::storeVelocitySignalAtReceivers (seismogram.hpp:193-214)
     const unsigned long long n = (host_step ? host_step : a.ctl->step_base + k_local + 1);
@@ -185,7 +240,7 @@ __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_
     if (idx >= a.R * a.M) return;
     const uint32_t r = idx % a.R, m = idx / a.R;
     const unsigned long long cnt = n / a.seis_freq - 1;
-    const double val = a.xv[(size_t)a.rcv[r] * a.M + m];
+    const double val = (double)xv[(size_t)a.rcv[r] * a.M + m];
     a.seis[r + (size_t)a.R * (cnt + (size_t)a.seis_T * m)] = val;
     if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
     return;
@@ -209,13 +264,13 @@ __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_
     gB = gA + 1;
   }
   const size_t nsp = (size_t)(a.nr - 1) * a.nth + (size_t)a.nr * (a.nth - 1);
-  const double cA = __ldg(a.csp + q);
-  const double cB = __ldg(a.csp + nsp + q);
-  double* sp = a.xs + (size_t)q * a.M + c * VEC;
+  const T cA = __ldg(csp + q);
+  const T cB = __ldg(csp + nsp + q);
+  T* sp = xs + (size_t)q * a.M + c * VEC;
   typename V::type s = V::ld(sp);
   const size_t off = (size_t)c * VEC;
-  fma_into(s, cA, V::ld(a.xv + (size_t)gA * a.M + off));
-  fma_into(s, cB, V::ld(a.xv + (size_t)gB * a.M + off));
+  fma_into(s, cA, V::ld(xv + (size_t)gA * a.M + off));
+  fma_into(s, cB, V::ld(xv + (size_t)gB * a.M + off));
   V::st(sp, s);
 }
 
@@ -266,21 +321,24 @@ __global__ void fom_apply_sp_kernel(const double* __restrict__ craw, const doubl
   y[(size_t)blockIdx.y * nsp + q] = sum;
 }
 
-__global__ void fom_fold_kernel(const double* raw, double* folded, double dt, size_t n) {
+// dt folded into the stencil values in FP64, then stored in the state's precision.
+template <typename T>
+__global__ void fom_fold_kernel(const double* raw, T* folded, double dt, size_t n) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x)
-    folded[k] = dt * raw[k];
+    folded[k] = (T)(dt * raw[k]);
 }
 
 __global__ void fom_advance_base_kernel(FomCtl* ctl, unsigned int by) { ctl->step_base += by; }
 __global__ void fom_set_base_kernel(FomCtl* ctl, unsigned long long v) { ctl->step_base = v; }
 
-// [N][M] -> [M][N] for the LayoutLeft snapshot copy.
-__global__ void fom_transpose_kernel(const double* in, double* out, uint32_t N, uint32_t M) {
+// [N][M] -> [M][N] FP64 for the LayoutLeft snapshot copy.
+template <typename T>
+__global__ void fom_transpose_kernel(const T* in, double* out, uint32_t N, uint32_t M) {
   __shared__ double tile[32][33];
   const uint32_t n0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
   for (uint32_t r = threadIdx.y; r < 32; r += 8) {
     const uint32_t n = n0 + r, m = m0 + threadIdx.x;
-    if (n < N && m < M) tile[r][threadIdx.x] = in[(size_t)n * M + m];
+    if (n < N && m < M) tile[r][threadIdx.x] = (double)in[(size_t)n * M + m];
   }
   __syncthreads();
   for (uint32_t r = threadIdx.y; r < 32; r += 8) {
@@ -297,13 +355,14 @@ struct shaw_fom_s {
   int rank = 1;
   int precision = SHAW_FP64;
   cudaStream_t stream = nullptr;
+  size_t esz = sizeof(double);  // bytes per state value and folded stencil value
   // device buffers
-  double* xv = nullptr;
-  double* xs = nullptr;
+  void* xv = nullptr;
+  void* xs = nullptr;
   double* cvp_raw = nullptr;
   double* csp_raw = nullptr;
-  double* cvp = nullptr;
-  double* csp = nullptr;
+  void* cvp = nullptr;
+  void* csp = nullptr;
   double* rho_inv = nullptr;
   unsigned long long* src = nullptr;
   int* kind = nullptr;
@@ -333,6 +392,12 @@ namespace {
 
 using H = shaw_fom_s;
 
+// Columns per thread: one 16-byte vector where M allows it.
+uint32_t state_vec(const H* h) {
+  if (h->esz == sizeof(float)) return (h->M % 4 == 0) ? 4u : (h->M % 2 == 0) ? 2u : 1u;
+  return (h->M % 2 == 0) ? 2u : 1u;
+}
+
 FomArgs make_args(const H* h, double dt) {
   FomArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -352,8 +417,7 @@ FomArgs make_args(const H* h, double dt) {
   a.nth = (uint32_t)h->nth;
   a.nr = (uint32_t)h->nr;
   a.M = h->M;
-  const int vec = (h->M % 2 == 0) ? 2 : 1;
-  a.chunks = h->M / vec;
+  a.chunks = h->M / state_vec(h);
   a.vp_items = (uint32_t)(h->nvp * a.chunks);
   a.sp_items = (uint32_t)(h->nsp * a.chunks);
   a.sp_row = (uint32_t)(2 * h->nth - 1);
@@ -370,10 +434,16 @@ FomArgs make_args(const H* h, double dt) {
 
 int launch_velocity(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
   const uint32_t blocks = (a.vp_items + kThreads - 1) / kThreads;
-  if (a.chunks * 2 == h->M)
-    fom_velocity_kernel<2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  else
-    fom_velocity_kernel<1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  const uint32_t vec = h->M / a.chunks;
+  if (h->esz == sizeof(float)) {
+    if (vec == 4) fom_velocity_kernel<float, 4><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    else if (vec == 2) fom_velocity_kernel<float, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    else fom_velocity_kernel<float, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  } else if (vec == 2) {
+    fom_velocity_kernel<double, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  } else {
+    fom_velocity_kernel<double, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  }
   h->launches++;
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
@@ -382,10 +452,16 @@ int launch_velocity(H* h, const FomArgs& a, uint32_t k_local, unsigned long long
 int launch_stress(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
   uint32_t blocks = a.sp_blocks;
   if (a.R && a.seis_freq) blocks += (a.R * a.M + kThreads - 1) / kThreads;
-  if (a.chunks * 2 == h->M)
-    fom_stress_kernel<2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  else
-    fom_stress_kernel<1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  const uint32_t vec = h->M / a.chunks;
+  if (h->esz == sizeof(float)) {
+    if (vec == 4) fom_stress_kernel<float, 4><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    else if (vec == 2) fom_stress_kernel<float, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    else fom_stress_kernel<float, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  } else if (vec == 2) {
+    fom_stress_kernel<double, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  } else {
+    fom_stress_kernel<double, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+  }
   h->launches++;
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
@@ -393,8 +469,13 @@ int launch_stress(H* h, const FomArgs& a, uint32_t k_local, unsigned long long h
 
 int ensure_folded(H* h, double dt) {
   if (h->folded_dt == dt) return SHAW_OK;
-  fom_fold_kernel<<<1024, 256, 0, h->stream>>>(h->cvp_raw, h->cvp, dt, 4 * h->nvp);
-  fom_fold_kernel<<<1024, 256, 0, h->stream>>>(h->csp_raw, h->csp, dt, 2 * h->nsp);
+  if (h->esz == sizeof(float)) {
+    fom_fold_kernel<float><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (float*)h->cvp, dt, 4 * h->nvp);
+    fom_fold_kernel<float><<<1024, 256, 0, h->stream>>>(h->csp_raw, (float*)h->csp, dt, 2 * h->nsp);
+  } else {
+    fom_fold_kernel<double><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (double*)h->cvp, dt, 4 * h->nvp);
+    fom_fold_kernel<double><<<1024, 256, 0, h->stream>>>(h->csp_raw, (double*)h->csp, dt, 2 * h->nsp);
+  }
   h->launches += 2;
   SHAW_CUDA(cudaGetLastError());
   h->folded_dt = dt;
@@ -406,13 +487,17 @@ int snapshot_copy(H* h, int dof, uint64_t col) {
   const uint64_t N = dof == 0 ? h->nvp : h->nsp;
   const uint64_t T = h->snap_nsteps / (dof == 0 ? h->snap_fvp : h->snap_fsp);
   double* host = dof == 0 ? h->host_vp : h->host_sp;
-  const double* dev = dof == 0 ? h->xv : h->xs;
-  if (h->M == 1) {
+  const void* dev = dof == 0 ? h->xv : h->xs;
+  if (h->M == 1 && h->esz == sizeof(double)) {
     SHAW_CUDA(cudaMemcpyAsync(host + N * col, dev, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return SHAW_OK;
   }
   dim3 grid((unsigned)((N + 31) / 32), (h->M + 31) / 32);
-  fom_transpose_kernel<<<grid, dim3(32, 8), 0, h->stream>>>(dev, h->staging, (uint32_t)N, h->M);
+  if (h->esz == sizeof(float))
+    fom_transpose_kernel<float><<<grid, dim3(32, 8), 0, h->stream>>>((const float*)dev, h->staging, (uint32_t)N, h->M);
+  else
+    fom_transpose_kernel<double><<<grid, dim3(32, 8), 0, h->stream>>>((const double*)dev, h->staging, (uint32_t)N,
+                                                                      h->M);
   h->launches++;
   SHAW_CUDA(cudaGetLastError());
   SHAW_CUDA(cudaMemcpy2DAsync(host + N * col, N * T * sizeof(double), h->staging, N * sizeof(double),
@@ -519,7 +604,8 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
   if (M == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "num_forcings must be >= 1");
   if (rank != 1 && rank != 2) return shaw::fail(SHAW_ERR_INVALID_ARG, "rank must be 1 or 2");
   if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
-  if (precision != SHAW_FP64) return shaw::fail(SHAW_ERR_UNSUPPORTED, "FOM precision must be SHAW_FP64");
+  if (precision != SHAW_FP64 && precision != SHAW_MIXED_FP32)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "FOM precision must be SHAW_FP64 or SHAW_MIXED_FP32");
   if (!d->graph_vp || !d->graph_sp || !d->labels_sp || !d->coords_vp || !d->coords_sp || !d->cot_vp ||
       !d->cot_sp || !d->coeff_vp || !d->rho_inv_vp || !d->shear_mod_sp)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "operator descriptor has a null array");
@@ -562,16 +648,17 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
   H* h = new H();
   h->nth = d->nth; h->nr = d->nr; h->nvp = nvp; h->nsp = nsp; h->M = M; h->rank = rank;
   h->precision = precision;
+  h->esz = precision == SHAW_MIXED_FP32 ? sizeof(float) : sizeof(double);
   auto bail = [&](int rc) { shaw_fom_destroy(h); return rc; };
   cudaError_t e;
 #define SHAW_TRY(call) do { e = (call); if (e != cudaSuccess) return bail(shaw::cuda_fail(e, #call)); } while (0)
   SHAW_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-  SHAW_TRY(cudaMalloc(&h->xv, nvp * M * sizeof(double)));
-  SHAW_TRY(cudaMalloc(&h->xs, nsp * M * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->xv, nvp * M * h->esz));
+  SHAW_TRY(cudaMalloc(&h->xs, nsp * M * h->esz));
   SHAW_TRY(cudaMalloc(&h->cvp_raw, 4 * nvp * sizeof(double)));
   SHAW_TRY(cudaMalloc(&h->csp_raw, 2 * nsp * sizeof(double)));
-  SHAW_TRY(cudaMalloc(&h->cvp, 4 * nvp * sizeof(double)));
-  SHAW_TRY(cudaMalloc(&h->csp, 2 * nsp * sizeof(double)));
+  SHAW_TRY(cudaMalloc(&h->cvp, 4 * nvp * h->esz));
+  SHAW_TRY(cudaMalloc(&h->csp, 2 * nsp * h->esz));
   SHAW_TRY(cudaMalloc(&h->rho_inv, nvp * sizeof(double)));
   SHAW_TRY(cudaMalloc(&h->src, M * sizeof(unsigned long long)));
   SHAW_TRY(cudaMalloc(&h->kind, M * sizeof(int)));
@@ -582,8 +669,8 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
   SHAW_TRY(cudaMemcpyAsync(h->csp_raw, cs.data(), cs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_TRY(cudaMemcpyAsync(h->rho_inv, d->rho_inv_vp, nvp * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_TRY(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
-  SHAW_TRY(cudaMemsetAsync(h->xv, 0, nvp * M * sizeof(double), h->stream));
-  SHAW_TRY(cudaMemsetAsync(h->xs, 0, nsp * M * sizeof(double), h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xv, 0, nvp * M * h->esz, h->stream));
+  SHAW_TRY(cudaMemsetAsync(h->xs, 0, nsp * M * h->esz, h->stream));
   SHAW_TRY(cudaStreamSynchronize(h->stream));
 #undef SHAW_TRY
   *out = h;
@@ -671,7 +758,7 @@ int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
     cudaHostUnregister(host_vp);
     return shaw::cuda_fail(e, "cudaHostRegister(host_sp)");
   }
-  if (h->M > 1 && !h->staging) {
+  if ((h->M > 1 || h->esz != sizeof(double)) && !h->staging) {
     e = cudaMalloc(&h->staging, std::max(h->nvp, h->nsp) * h->M * sizeof(double));
     if (e != cudaSuccess) {
       cudaHostUnregister(host_vp);
@@ -686,8 +773,8 @@ int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
 
 int shaw_fom_reset(shaw_fom_t h) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
-  SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->nvp * h->M * sizeof(double), h->stream));
-  SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->nsp * h->M * sizeof(double), h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->nvp * h->M * h->esz, h->stream));
+  SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->nsp * h->M * h->esz, h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
   if (h->seis)
     SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
@@ -784,28 +871,43 @@ int shaw_fom_get_seismogram(shaw_fom_t h, double* out) {
   return SHAW_OK;
 }
 
-static int copy_state(shaw_fom_t h, double* host, const double* chost, uint64_t N, double* dev, bool to_host) {
+}  // extern "C"
+
+namespace {
+
+// host LayoutLeft FP64 [N x M] <-> device row-major [N][M] in the state's precision
+// (FP32 states are written rounded to nearest and read back exactly).
+template <typename T>
+int copy_state_t(shaw_fom_t h, double* host, const double* chost, uint64_t N, void* dev, bool to_host) {
+  std::vector<T> tmp(N * h->M);
+  if (to_host) {
+    SHAW_CUDA(cudaMemcpyAsync(tmp.data(), dev, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+    for (uint64_t n = 0; n < N; ++n)
+      for (uint32_t m = 0; m < h->M; ++m) host[n + N * m] = (double)tmp[n * h->M + m];
+  } else {
+    for (uint64_t n = 0; n < N; ++n)
+      for (uint32_t m = 0; m < h->M; ++m) tmp[n * h->M + m] = (T)chost[n + N * m];
+    SHAW_CUDA(cudaMemcpyAsync(dev, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return SHAW_OK;
+}
+
+int copy_state(shaw_fom_t h, double* host, const double* chost, uint64_t N, void* dev, bool to_host) {
+  if (h->esz == sizeof(float)) return copy_state_t<float>(h, host, chost, N, dev, to_host);
   if (h->M == 1) {
     if (to_host) SHAW_CUDA(cudaMemcpyAsync(host, dev, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     else SHAW_CUDA(cudaMemcpyAsync(dev, chost, N * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     SHAW_CUDA(cudaStreamSynchronize(h->stream));
     return SHAW_OK;
   }
-  // host LayoutLeft [N x M] <-> device row-major [N][M]: transpose on the host side
-  std::vector<double> tmp(N * h->M);
-  if (to_host) {
-    SHAW_CUDA(cudaMemcpyAsync(tmp.data(), dev, tmp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    SHAW_CUDA(cudaStreamSynchronize(h->stream));
-    for (uint64_t n = 0; n < N; ++n)
-      for (uint32_t m = 0; m < h->M; ++m) host[n + N * m] = tmp[n * h->M + m];
-  } else {
-    for (uint64_t n = 0; n < N; ++n)
-      for (uint32_t m = 0; m < h->M; ++m) tmp[n * h->M + m] = chost[n + N * m];
-    SHAW_CUDA(cudaMemcpyAsync(dev, tmp.data(), tmp.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    SHAW_CUDA(cudaStreamSynchronize(h->stream));
-  }
-  return SHAW_OK;
+  return copy_state_t<double>(h, host, chost, N, dev, to_host);
 }
+
+}  // namespace
+
+extern "C" {
 
 int shaw_fom_get_state(shaw_fom_t h, double* vp, double* sp) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
