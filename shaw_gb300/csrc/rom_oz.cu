@@ -16,8 +16,9 @@
 //   * a slice product is an integer below 2^12, a K-sum below 2^22 (K <= 1024) and a
 //     diagonal d = s + t (up to 6 pairs) below 2^24: the FP32 accumulators in TMEM
 //     hold every partial sum exactly, whatever their rounding mode;
-//   * pairs with s + t <= 5 (21 MMAs per K-step) give ~2^-36 relative accuracy; the 6
-//     diagonal sums are combined exactly in int64 in the epilogue and scaled back.
+//   * pairs with s + t <= 5 give ~2^-36 relative accuracy; they are issued as 6 MMAs
+//     per K-step (operator slice s times the stacked state slices 0 .. 5-s), and the 6
+//     diagonal sums are combined with error-free FP32 additions in the epilogue.
 // State: FP32 hi + lo pairs (compensated) in global memory; the epilogue re-slices the
 // new state into the next GEMM's BF16 B tiles after each half-step.
 //
@@ -120,7 +121,7 @@ struct Shared {
   int abort;
   int beta_v[kMaxNb], beta_s[kMaxNb];
   unsigned int colmax[kMaxNb];
-  double fdt[kMaxNb];
+  float fdt_h[kMaxNb], fdt_l[kMaxNb];  // f_j(t_{n-1}) * dt of the current step, as FP32 hi + lo
   OzInst in;
   OzTile tile;
 };
@@ -164,7 +165,6 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
       bulk_g2s(st + kABytes, Bop + (size_t)c * bbytes, bbytes, &sh->full[s]);
     }
   } else if (warp == 1 && lane == 0) {
-    const uint32_t idesc = idesc_bf16(nb);
     uint32_t lu[2] = {uses[0], uses[1]};
     for (uint32_t mt = 0; mt < n_mt && !sh->abort; ++mt) {
       uint32_t buf, par;
@@ -182,16 +182,26 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
         // start-address field (16-byte units, no carry: shared addresses < 256 KB)
         const uint64_t adesc0 = smem_desc(abase, 128, 512);
         const uint64_t bdesc0 = smem_desc(abase + kABytes, 128, 512);
+        // The B slices of a stage are stacked along N (slice t = rows t*nb ..), and the
+        // diagonal accumulators along TMEM columns (diagonal d = columns d*nb ..), so
+        // operator slice sa times the state slices tb = 0 .. 5-sa is ONE MMA of
+        // N = (6-sa)*nb whose output columns start at diagonal sa: 6 MMAs per K-step
+        // instead of 21 pair MMAs, each A slice read from shared memory once.  N is
+        // capped at 256 (split into two MMAs for nb = 64).  The first MMA of a tile
+        // (sa = 0 covers every diagonal) starts the accumulation.
 #pragma unroll
         for (uint32_t k = 0; k < kKc / 16; ++k) {
 #pragma unroll
-          for (int d = 0; d < kDiags; ++d) {
-#pragma unroll
-            for (int sa = 0; sa <= d; ++sa) {
-              const int tb = d - sa;
-              const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
+          for (int sa = 0; sa < kSlices; ++sa) {
+            const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
+            const uint32_t acc = (c > 0 || k > 0 || sa > 0) ? 1u : 0u;
+            uint32_t tb = 0, left = (uint32_t)(kSlices - sa);
+            while (left) {
+              const uint32_t take = min(left, 256u / nb);
               const uint64_t bdesc = bdesc0 + ((tb * btile + k * 256) >> 4);
-              mma_f16(dcol + d * nb, adesc, bdesc, idesc, (c > 0 || k > 0 || sa > 0) ? 1u : 0u);
+              mma_f16(dcol + (sa + tb) * nb, adesc, bdesc, idesc_bf16(take * nb), acc);
+              tb += take;
+              left -= take;
             }
           }
         }
@@ -227,9 +237,10 @@ __device__ __forceinline__ void pow2_pair(int e, float& f1, float& f2) {
 }
 
 // Read the 6 diagonal accumulators of 8 columns for this thread's row (TMEM lanes of
-// quarter q) and combine them exactly: every D_d is an integer below 2^24, so
-// Y = sum_d D_d * 2^(6(5-d)) is an exact int64 and y = Y * 2^-42 (before scaling).
-// Returns y as a double-float pair.
+// quarter q) and combine them: every D_d is an integer below 2^24, so the terms
+// D_d * 2^(6(5-d)) are exact in FP32 and their sum Y (< 2^55) is formed with error-free
+// additions (TwoSum, smallest term first) into a double-float pair accurate to 2^-48;
+// y = Y * 2^-42 (before the row / column scaling).  No integer or 64-bit conversions.
 __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q, uint32_t j0, float* yh,
                                               float* yl) {
   float D[kDiags][8];
@@ -238,11 +249,15 @@ __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q
   tmem_wait_ld();
 #pragma unroll
   for (int jj = 0; jj < 8; ++jj) {
-    long long Y = 0;
+    float s = D[kDiags - 1][jj], e = 0.f;
 #pragma unroll
-    for (int d = 0; d < kDiags; ++d) Y += (long long)__float2int_rn(D[d][jj]) << (6 * (kDiags - 1 - d));
-    const float h = __ll2float_rn(Y);
-    const float l = __ll2float_rn(Y - __float2ll_rn(h));
+    for (int d = kDiags - 2; d >= 0; --d) {
+      float err;
+      two_sum(s, D[d][jj] * __int_as_float((127 + 6 * (kDiags - 1 - d)) << 23), s, err);
+      e += err;
+    }
+    const float h = s + e;
+    const float l = e - (h - s);
     yh[jj] = h * 0x1p-42f;  // exact power-of-two scalings
     yl[jj] = l * 0x1p-42f;
   }
@@ -295,9 +310,17 @@ __device__ __forceinline__ void column_exponents(Shared* sh, uint32_t nb, int* b
   }
 }
 
-__device__ __forceinline__ void note_max(Shared* sh, uint32_t j, float v) {
-  const unsigned int m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(v)));
-  if ((threadIdx.x & 31) == 0) atomicMax(&sh->colmax[j], m);
+// Column maxima of |x| over the warp's 32 rows for 8 columns j0 .. j0+7: eight warp
+// reductions, then lane jj publishes column j0+jj with one shared atomic.
+__device__ __forceinline__ void note_max8(Shared* sh, uint32_t j0, const float* xh) {
+  const int lane = threadIdx.x & 31;
+  unsigned int mine = 0u;
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    const unsigned int m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(xh[jj])));
+    if (lane == jj) mine = m;
+  }
+  if (lane < 8) atomicMax(&sh->colmax[j0 + lane], mine);
 }
 
 __device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -376,12 +399,18 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         const uint32_t t = threadIdx.x - 128;
         if (t < nb) {
           const uint32_t col = col0 + t;
-          sh->fdt[t] = col < in.M ? signal_value(in.kind[col], in.delay[col], in.period[col], (double)(n - 1) * a.dt) *
-                                        a.dt
-                                  : 0.0;
+          const double f =
+              col < in.M ? signal_value(in.kind[col], in.delay[col], in.period[col], (double)(n - 1) * a.dt) * a.dt
+                         : 0.0;
+          sh->fdt_h[t] = (float)f;
+          sh->fdt_l[t] = (float)(f - (double)sh->fdt_h[t]);
         }
         epi_barrier();
       }
+      // snapshot steps (StateObserver), decided once per step
+      const bool snap_v = in.snap_vp && in.fvp && n % in.fvp == 0;
+      const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
+      const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
       // ---------------- velocity: XV += dt Av XS + fdt b ----------------
       gemm_phase(stages, sh, in.Av, bst, n_mt_v, n_kc_v, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
         const uint32_t row = mt * 128 + q * 32 + lane;
@@ -407,15 +436,14 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             float s1, s2;
             pow2_pair(e, s1, s2);
             df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-            const double f = sh->fdt[j];
-            const float fh = (float)f, fl = (float)(f - (double)fh);
-            df_fma(xh, xl, fh, fl, qh[jj], ql[jj]);
+            df_fma(xh, xl, sh->fdt_h[j], sh->fdt_l[j], qh[jj], ql[jj]);
             xvh[si] = xh;
             xvl[si] = xl;
-            note_max(sh, j, xh);
-            if (in.snap_vp && in.fvp && n % in.fvp == 0 && row < in.kv && col < in.M)
-              in.snap_vp[row + (size_t)in.kv * ((n / in.fvp - 1) + in.Tvp * col)] = (double)xh + (double)xl;
+            ph[jj] = xh;
+            if (snap_v && row < in.kv && col < in.M)
+              in.snap_vp[row + (size_t)in.kv * (tv + in.Tvp * col)] = (double)xh + (double)xl;
           }
+          note_max8(sh, j0, ph);
         }
       });
       if (ew >= 0) {
@@ -451,10 +479,11 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
             xsh[si] = xh;
             xsl[si] = xl;
-            note_max(sh, j, xh);
-            if (in.snap_sp && in.fsp && n % in.fsp == 0 && row < in.ks && col < in.M)
-              in.snap_sp[row + (size_t)in.ks * ((n / in.fsp - 1) + in.Tsp * col)] = (double)xh + (double)xl;
+            ph[jj] = xh;
+            if (snap_s && row < in.ks && col < in.M)
+              in.snap_sp[row + (size_t)in.ks * (ts + in.Tsp * col)] = (double)xh + (double)xl;
           }
+          note_max8(sh, j0, ph);
         }
       });
       if (ew >= 0) {
