@@ -19,8 +19,11 @@
 //   * pairs with s + t <= 5 give ~2^-36 relative accuracy; they are issued as 6 MMAs
 //     per K-step (operator slice s times the stacked state slices 0 .. 5-s), and the 6
 //     diagonal sums are combined with error-free FP32 additions in the epilogue.
-// State: FP32 hi + lo pairs (compensated) in global memory; the epilogue re-slices the
-// new state into the next GEMM's BF16 B tiles after each half-step.
+// State: FP32 hi + lo pairs (compensated) in global memory.  The epilogue slices each
+// new state value into the next GEMM's BF16 B tiles as soon as it is computed, with a
+// per-column exponent predicted from the previous half-step (one bit of headroom);
+// columns whose new maximum leaves the predicted range are re-sliced exactly after
+// the phase.
 //
 // Work decomposition: forcing columns are independent for the whole run, so the unit
 // of work is a TILE = (instance, block of nb columns), advanced through all time steps
@@ -94,6 +97,8 @@ struct OzInst {
   double *snap_vp, *snap_sp;
   unsigned long long Tvp, Tsp;
   uint32_t fvp, fsp;
+  int* expo;  // [3][Mp]: per column, the exponent of the current XS slices and the predicted
+              // exponents of the next XV and XS slicing (kept across launches)
   uint32_t kv, ks, kvp, ksp, M, Mp;
 };
 
@@ -119,8 +124,10 @@ struct Shared {
   uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], drain;
   uint32_t tmem;
   int abort;
-  int beta_v[kMaxNb], beta_s[kMaxNb];
+  int beta_v[kMaxNb], beta_s[kMaxNb];   // exponents the current B tiles were sliced with
+  int pred_v[kMaxNb], pred_s[kMaxNb];   // predicted exponents for slicing the next new state
   unsigned int colmax[kMaxNb];
+  unsigned long long reslice_v, reslice_s;  // columns to re-slice exactly after a phase
   float fdt_h[kMaxNb], fdt_l[kMaxNb];  // f_j(t_{n-1}) * dt of the current step, as FP32 hi + lo
   OzInst in;
   OzTile tile;
@@ -266,7 +273,7 @@ __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q
 // Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
 // into the BF16 B tiles with per-column exponents beta[j] (|x| < 2^beta).
 __device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t nb,
-                                            const int* beta, uint8_t* tiles) {
+                                            const int* beta, uint8_t* tiles, unsigned long long mask) {
   const uint32_t t = threadIdx.x - 128;
   const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);
   const uint32_t n = kp * nb;
@@ -278,7 +285,7 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
       const uint32_t e = e0 + u * kEpiThreads;
       jj[u] = e / kp;
       rr[u] = e - jj[u] * kp;
-      if (e < n) {
+      if (e < n && ((mask >> jj[u]) & 1ull)) {
         vh[u] = xh[(size_t)jj[u] * kp + rr[u]];
         vl[u] = xl[(size_t)jj[u] * kp + rr[u]];
       }
@@ -286,6 +293,7 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (e0 + u * kEpiThreads >= n) break;
+      if (!((mask >> jj[u]) & 1ull)) continue;
       float h = ldexpf(vh[u], -beta[jj[u]]), l = ldexpf(vl[u], -beta[jj[u]]);
       uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + tile_off(jj[u], rr[u] % kKc);
 #pragma unroll
@@ -300,12 +308,61 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
   }
 }
 
+// Slice one state value (row, column j) into the B tiles with exponent beta (the
+// stacked-slice layout of slice_state).  Values at or above 2^beta are clamped; the
+// caller detects that from the column maximum and re-slices exactly.
+__device__ __forceinline__ void slice_value(float xh, float xl, int beta, uint32_t row, uint32_t j, uint32_t bbytes,
+                                            uint32_t btile, uint8_t* tiles) {
+  float h = ldexpf(xh, -beta), l = ldexpf(xl, -beta);
+  uint8_t* base = tiles + (size_t)(row / kKc) * bbytes + tile_off(j, row % kKc);
+#pragma unroll
+  for (int s = 0; s < kSlices; ++s) {
+    const float th = h * 64.f, tl = l * 64.f;
+    float a = rintf(th);
+    a = fminf(64.f, fmaxf(-64.f, a));
+    two_sum(th - a, tl, h, l);
+    *reinterpret_cast<__nv_bfloat16*>(base + s * btile) = __float2bfloat16_rn(a);
+  }
+}
+
+// "no exponent yet": the int whose four bytes are 0x80 (what a byte-wise memset writes)
+constexpr int kNoPrediction = (int)0x80808080;
+
+// After a phase that sliced its new state with the predicted exponents pred[]: keep
+// them (beta = pred) for every column whose new maximum m lies in [2^(pred-3), 2^pred)
+// -- no value clamped, at most 2 bits of headroom -- and mark the other columns in
+// *mask for an exact re-slice with beta = ilogb(m) + 1.  The next prediction is
+// ilogb(m) + 2 (one bit of headroom).  Epilogue threads t < nb; colmax is consumed;
+// *other (the other phase's mask, no longer read) is cleared.
+__device__ __forceinline__ void settle_exponents(Shared* sh, uint32_t nb, int* beta, int* pred,
+                                                 unsigned long long* mask, unsigned long long* other) {
+  const uint32_t t = threadIdx.x - 128;
+  if (t == 0) *other = 0ull;
+  if (t < nb) {
+    const float m = __uint_as_float(sh->colmax[t]);
+    sh->colmax[t] = 0u;
+    const int p = pred[t];
+    bool ok;
+    if (m == 0.f) {  // an all-zero column: its slices are zeros with any exponent
+      ok = p != kNoPrediction;
+      beta[t] = ok ? p : 0;
+    } else {
+      const int e = ilogbf(m);  // 2^e <= m < 2^(e+1)
+      ok = p != kNoPrediction && e + 1 <= p && p <= e + 3;
+      beta[t] = ok ? p : e + 1;
+      pred[t] = e + 2;
+    }
+    if (!ok) atomicOr(mask, 1ull << t);
+  }
+}
+
 // Column exponents from the maxima gathered in colmax: |x| < 2^beta.
-__device__ __forceinline__ void column_exponents(Shared* sh, uint32_t nb, int* beta) {
+__device__ __forceinline__ void column_exponents(Shared* sh, uint32_t nb, int* beta, int* pred) {
   const uint32_t t = threadIdx.x - 128;
   if (t < nb) {
     const float m = __uint_as_float(sh->colmax[t]);
     beta[t] = (m > 0.f) ? ilogbf(m) + 1 : 0;
+    if (m > 0.f) pred[t] = beta[t] + 1;
     sh->colmax[t] = 0u;
   }
 }
@@ -366,11 +423,15 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       sh->colmax[threadIdx.x] = 0u;
       sh->beta_v[threadIdx.x] = 0;
       sh->beta_s[threadIdx.x] = 0;
+      sh->pred_v[threadIdx.x] = kNoPrediction;
+      sh->pred_s[threadIdx.x] = kNoPrediction;
     }
+    if (threadIdx.x == 0) sh->reslice_v = sh->reslice_s = 0ull;
     if (__syncthreads_or(sh->abort != 0)) break;
     const OzInst& in = sh->in;
     const uint32_t nb = sh->tile.nb, col0 = sh->tile.col0;
     const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
+    const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);             // B-tile geometry
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
     float* const xvh = in.xvh + (size_t)col0 * in.kvp;
     float* const xvl = in.xvl + (size_t)col0 * in.kvp;
@@ -379,16 +440,27 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const float* const bh = in.bh + (size_t)col0 * in.kvp;
     const float* const bl = in.bl + (size_t)col0 * in.kvp;
 
-    // B tiles of the current XS (the state may be non-zero when advancing in pieces)
+    // B tiles of the current XS (the state may be non-zero when advancing in pieces):
+    // with the exponents the previous launch left (so a run in pieces slices exactly
+    // as an uninterrupted run), or exact exponents for a fresh state
     if (ew >= 0) {
       for (uint32_t e = threadIdx.x - 128; e < in.ksp * nb; e += kEpiThreads) {
         const uint32_t j = e / in.ksp, row = e - j * in.ksp;
         atomicMax(&sh->colmax[j], __float_as_uint(fabsf(xsh[(size_t)j * in.ksp + row])));
       }
       epi_barrier();
-      column_exponents(sh, nb, sh->beta_s);
+      column_exponents(sh, nb, sh->beta_s, sh->pred_s);
+      const uint32_t t = threadIdx.x - 128;
+      if (t < nb) {
+        const int bs = in.expo[col0 + t];
+        if (bs != kNoPrediction) {
+          sh->beta_s[t] = bs;
+          sh->pred_v[t] = in.expo[in.Mp + col0 + t];
+          sh->pred_s[t] = in.expo[2 * in.Mp + col0 + t];
+        }
+      }
       epi_barrier();
-      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst);
+      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
     if (__syncthreads_or(sh->abort != 0)) break;
@@ -440,6 +512,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             xvh[si] = xh;
             xvl[si] = xl;
             ph[jj] = xh;
+            const int pv = sh->pred_v[j];
+            if (pv != kNoPrediction) slice_value(xh, xl, pv, row, j, bbytes, btile, bvt);
             if (snap_v && row < in.kv && col < in.M)
               in.snap_vp[row + (size_t)in.kv * (tv + in.Tvp * col)] = (double)xh + (double)xl;
           }
@@ -448,9 +522,10 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       });
       if (ew >= 0) {
         epi_barrier();
-        column_exponents(sh, nb, sh->beta_v);
+        settle_exponents(sh, nb, sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s);
         epi_barrier();
-        if (!sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt);
+        const unsigned long long redo = sh->reslice_v;
+        if (redo && !sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo);
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       if (__syncthreads_or(sh->abort != 0)) break;
@@ -480,6 +555,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             xsh[si] = xh;
             xsl[si] = xl;
             ph[jj] = xh;
+            const int ps = sh->pred_s[j];
+            if (ps != kNoPrediction) slice_value(xh, xl, ps, row, j, bbytes, btile, bst);
             if (snap_s && row < in.ks && col < in.M)
               in.snap_sp[row + (size_t)in.ks * (ts + in.Tsp * col)] = (double)xh + (double)xl;
           }
@@ -488,12 +565,19 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       });
       if (ew >= 0) {
         epi_barrier();
-        column_exponents(sh, nb, sh->beta_s);
+        settle_exponents(sh, nb, sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v);
         epi_barrier();
-        if (!sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst);
+        const unsigned long long redo = sh->reslice_s;
+        if (redo && !sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo);
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       if (__syncthreads_or(sh->abort != 0)) break;
+    }
+    if (ew >= 0 && threadIdx.x - 128 < nb) {  // exponents for the next launch
+      const uint32_t t = threadIdx.x - 128;
+      in.expo[col0 + t] = sh->beta_s[t];
+      in.expo[in.Mp + col0 + t] = sh->pred_v[t];
+      in.expo[2 * in.Mp + col0 + t] = sh->pred_s[t];
     }
     if (threadIdx.x == 0 && a.tile_ns) a.tile_ns[a.order[ti]] = global_ns() - t_start;
     if (__syncthreads_or(sh->abort != 0)) break;
@@ -711,6 +795,7 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
     OZ_TRY(alloc((void**)&in.xvl, nv * sizeof(float)));
     OZ_TRY(alloc((void**)&in.xsh, ns * sizeof(float)));
     OZ_TRY(alloc((void**)&in.xsl, ns * sizeof(float)));
+    OZ_TRY(alloc((void**)&in.expo, 3 * (size_t)in.Mp * sizeof(int)));
     OZ_TRY(cudaMemcpyAsync((void*)in.Av, sv.data(), sv.size() * 2, cudaMemcpyHostToDevice, s));
     OZ_TRY(cudaMemcpyAsync((void*)in.As, ss.data(), ss.size() * 2, cudaMemcpyHostToDevice, s));
     OZ_TRY(cudaMemcpyAsync((void*)in.alpha_v, av.data(), av.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -764,6 +849,7 @@ int reset(Batch* p, cudaStream_t s) {
     SHAW_CUDA(cudaMemsetAsync(in.xvl, 0, nv * sizeof(float), s));
     SHAW_CUDA(cudaMemsetAsync(in.xsh, 0, ns * sizeof(float), s));
     SHAW_CUDA(cudaMemsetAsync(in.xsl, 0, ns * sizeof(float), s));
+    SHAW_CUDA(cudaMemsetAsync(in.expo, 0x80, 3 * (size_t)in.Mp * sizeof(int), s));  // kNoPrediction
   }
   SHAW_CUDA(cudaMemsetAsync(p->error, 0, sizeof(unsigned int), s));
   return SHAW_OK;
