@@ -63,7 +63,7 @@ def build(verbose=False, ptxas_info=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if _stale(o, [s] + headers):
-            cmd = [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
+            cmd = [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-fopenmp",
                                    "-I", INCLUDE, "-I", CSRC, "-c", s, "-o", o]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
@@ -82,7 +82,7 @@ def build(verbose=False, ptxas_info=False):
             if o.strip():
                 print(o)
     if jobs or not os.path.exists(LIB):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas", "-lcusolver"])
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas", "-lcusolver", "-lgomp"])
     for src, exe in (("main.cpp", EXE), ("pod_main.cpp", POD_EXE)):
         obj = os.path.join(BUILD, src + ".o")
         s = os.path.join(CSRC, src)

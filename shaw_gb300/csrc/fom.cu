@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -553,29 +554,32 @@ int set_step_base(H* h) {
   return SHAW_OK;
 }
 
-bool valid_structured_mesh(const shaw_fom_operator_desc* d, std::string& why) {
-  const uint64_t nth = d->nth, nr = d->nr;
-  if (nth < 2 || nr < 2) { why = "nth and nr must be >= 2"; return false; }
-  if (d->nvp != nth * nr) { why = "numPtsVp != nth*nr"; return false; }
-  if (d->nsp != (nr - 1) * nth + nr * (nth - 1)) { why = "numPtsSp != (nr-1)*nth + nr*(nth-1)"; return false; }
-  if (d->nvp * 4 >= (1ull << 32) || d->nsp * 2 >= (1ull << 32)) { why = "mesh too large for 32-bit indexing"; return false; }
-  const uint64_t row = 2 * nth - 1;
+// The first vp / sp row whose graph entries differ from the structured full mesh's, or
+// the row count when all match (rows checked in parallel on the host threads).
+uint64_t first_bad_vp(const shaw_fom_operator_desc* d) {
+  const uint64_t nth = d->nth, nr = d->nr, row = 2 * nth - 1;
   auto srp = [&](uint64_t j, uint64_t i) { return j * row + 2 * i; };
   auto stp = [&](uint64_t j, uint64_t i) { return (j + 1 < nr) ? j * row + 2 * i + 1 : j * row + i; };
-  for (uint64_t p = 0; p < d->nvp; ++p) {
-    const uint64_t j = p / nth, i = p % nth;
+  uint64_t bad = d->nvp;
+#pragma omp parallel for reduction(min : bad) schedule(static)
+  for (int64_t pp = 0; pp < (int64_t)d->nvp; ++pp) {
+    const uint64_t p = (uint64_t)pp, j = p / nth, i = p % nth;
     const int64_t* g = d->graph_vp + p * 5;
     const int64_t eW = (i >= 1) ? (int64_t)stp(j, i - 1) : (int64_t)stp(j, i);
     const int64_t eE = (i + 1 < nth) ? (int64_t)stp(j, i) : (int64_t)stp(j, i - 1);
     const int64_t eN = (j + 1 < nr) ? (int64_t)srp(j, i) : (int64_t)srp(j - 1, i);
     const int64_t eS = (j >= 1) ? (int64_t)srp(j - 1, i) : (int64_t)srp(j, i);
-    if (g[0] != (int64_t)p || g[1] != eW || g[2] != eN || g[3] != eE || g[4] != eS) {
-      why = "graph_vp row " + std::to_string(p) + " does not match the structured full mesh";
-      return false;
-    }
+    if (g[0] != (int64_t)p || g[1] != eW || g[2] != eN || g[3] != eE || g[4] != eS) bad = std::min(bad, p);
   }
-  for (uint64_t q = 0; q < d->nsp; ++q) {
-    const uint64_t j = q / row, rem = q % row;
+  return bad;
+}
+
+uint64_t first_bad_sp(const shaw_fom_operator_desc* d) {
+  const uint64_t nth = d->nth, nr = d->nr, row = 2 * nth - 1;
+  uint64_t bad = d->nsp;
+#pragma omp parallel for reduction(min : bad) schedule(static)
+  for (int64_t qq = 0; qq < (int64_t)d->nsp; ++qq) {
+    const uint64_t q = (uint64_t)qq, j = q / row, rem = q % row;
     const int64_t* g = d->graph_sp + q * 3;
     int64_t eA, eB;
     int lab;
@@ -586,10 +590,26 @@ bool valid_structured_mesh(const shaw_fom_operator_desc* d, std::string& why) {
       const uint64_t i = (j + 1 < nr) ? rem / 2 : rem;
       lab = 2; eA = (int64_t)(j * nth + i); eB = eA + 1;
     }
-    if (g[0] != (int64_t)q || g[1] != eA || g[2] != eB || d->labels_sp[q] != lab) {
-      why = "graph_sp row " + std::to_string(q) + " does not match the structured full mesh";
-      return false;
-    }
+    if (g[0] != (int64_t)q || g[1] != eA || g[2] != eB || d->labels_sp[q] != lab) bad = std::min(bad, q);
+  }
+  return bad;
+}
+
+bool valid_structured_mesh(const shaw_fom_operator_desc* d, std::string& why) {
+  const uint64_t nth = d->nth, nr = d->nr;
+  if (nth < 2 || nr < 2) { why = "nth and nr must be >= 2"; return false; }
+  if (d->nvp != nth * nr) { why = "numPtsVp != nth*nr"; return false; }
+  if (d->nsp != (nr - 1) * nth + nr * (nth - 1)) { why = "numPtsSp != (nr-1)*nth + nr*(nth-1)"; return false; }
+  if (d->nvp * 4 >= (1ull << 32) || d->nsp * 2 >= (1ull << 32)) { why = "mesh too large for 32-bit indexing"; return false; }
+  const uint64_t bv = first_bad_vp(d);
+  if (bv != d->nvp) {
+    why = "graph_vp row " + std::to_string(bv) + " does not match the structured full mesh";
+    return false;
+  }
+  const uint64_t bs = first_bad_sp(d);
+  if (bs != d->nsp) {
+    why = "graph_sp row " + std::to_string(bs) + " does not match the structured full mesh";
+    return false;
   }
   return true;
 }
@@ -616,9 +636,12 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
 
   // Stencil values in the reference's expression order (shwavepp.hpp:361-364, 441-454).
   const uint64_t nvp = d->nvp, nsp = d->nsp;
-  std::vector<double> cv(4 * nvp, 0.0), cs(2 * nsp, 0.0);
+  // every entry is written below (in parallel, which also spreads the first touch)
+  std::unique_ptr<double[]> cv(new double[4 * nvp]), cs(new double[2 * nsp]);
   const double three = 3.0, oneHalf = 1.0 / 2.0;
-  for (uint64_t p = 0; p < nvp; ++p) {
+#pragma omp parallel for schedule(static)
+  for (int64_t pp = 0; pp < (int64_t)nvp; ++pp) {
+    const uint64_t p = (uint64_t)pp;
     const int64_t* g = d->graph_vp + p * 5;
     const double rInv = d->coords_vp[p * 2 + 1];
     const double cot = d->cot_vp[p];
@@ -633,7 +656,9 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
     if (g[1] == g[3]) { cv[2 * nvp + p] = cW + cE; cv[3 * nvp + p] = 0.0; }
     else { cv[2 * nvp + p] = cW; cv[3 * nvp + p] = cE; }
   }
-  for (uint64_t q = 0; q < nsp; ++q) {
+#pragma omp parallel for schedule(static)
+  for (int64_t qq = 0; qq < (int64_t)nsp; ++qq) {
+    const uint64_t q = (uint64_t)qq;
     const double rInv = d->coords_sp[q * 2 + 1];
     const double G = d->shear_mod_sp[q];
     if (d->labels_sp[q] == 1) {
@@ -665,8 +690,8 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
   SHAW_TRY(cudaMalloc(&h->period, M * sizeof(double)));
   SHAW_TRY(cudaMalloc(&h->delay, M * sizeof(double)));
   SHAW_TRY(cudaMalloc(&h->ctl, sizeof(FomCtl)));
-  SHAW_TRY(cudaMemcpyAsync(h->cvp_raw, cv.data(), cv.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  SHAW_TRY(cudaMemcpyAsync(h->csp_raw, cs.data(), cs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->cvp_raw, cv.get(), 4 * nvp * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  SHAW_TRY(cudaMemcpyAsync(h->csp_raw, cs.get(), 2 * nsp * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_TRY(cudaMemcpyAsync(h->rho_inv, d->rho_inv_vp, nvp * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_TRY(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
   SHAW_TRY(cudaMemsetAsync(h->xv, 0, nvp * M * h->esz, h->stream));
