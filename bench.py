@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--no-extra", action="store_true", help="skip the other configurations' lines")
     p.add_argument("--profile-rom", default=None, choices=["ozaki", "tf32x3", "fp64"],
                    help="only run the rank-2 ROM (k=512, M=4096) for --steps steps, for profiler captures")
+    p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32"],
+                   help="only run the FOM on the 1000x2000 grid with --forcings columns for --steps steps")
     return p.parse_args()
 
 
@@ -611,6 +613,21 @@ def main():
         r.run(0.5, args.steps)
         print(json.dumps({"profile_rom": args.profile_rom, "steps": args.steps, "launches": r.kernel_launches}))
         r.close()
+    elif args.profile_fom:
+        import numpy as np
+        import shaw_gb300 as shaw
+        shaw.build()
+        mesh = shaw.Mesh.generate(NTH, NR)
+        mesh.set_material("unilayer", MATERIAL)
+        gids, periods, rcv, dt = workload_inputs(np, mesh)
+        m = args.forcings
+        f = shaw.Fom(mesh, 2, m, precision=shaw.FP64 if args.profile_fom == "fp64" else shaw.MIXED_FP32)
+        f.set_sources(gids[:m], "gaussDer", periods[:m], 180.0)
+        f.reset()
+        f.advance(dt, args.steps)
+        f.synchronize()
+        print(json.dumps({"profile_fom": args.profile_fom, "forcings": m, "steps": args.steps,
+                          "launches": f.kernel_launches}))
     elif args.impl == "reference":
         run_reference(args)
     else:
