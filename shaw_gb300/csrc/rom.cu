@@ -38,6 +38,10 @@ namespace {
 
 constexpr int kRomThreads = 256;
 constexpr int kRomWarps = kRomThreads / 32;
+// rank-1 cluster kernel: 16 warps, so that at k = 256 over 16 CTAs every warp owns one
+// velocity row and one stress row (no serial rows per warp on the latency-bound path)
+constexpr int kR1Threads = 512;
+constexpr int kR1Warps = kR1Threads / 32;
 
 // ---- double-float (hi + lo FP32) arithmetic ------------------------------------
 struct df {
@@ -160,7 +164,7 @@ struct Arith<true> {
 
 // One persistent launch for nsteps ROM rank-1 leapfrog steps (one cluster).
 template <bool MIXED>
-__global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs a) {
+__global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a) {
   using A = Arith<MIXED>;
   using T = typename A::T;
   cg::cluster_group cluster = cg::this_cluster();
@@ -177,13 +181,13 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
   const uint32_t s0 = min(a.ks, crank * a.rows_s), s1 = min(a.ks, s0 + a.rows_s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  for (uint32_t k = threadIdx.x; k < a.kv; k += kRomThreads) xv[k] = A::load(a.xv[k]);
-  for (uint32_t k = threadIdx.x; k < a.ks; k += kRomThreads) xs[k] = A::load(a.xs[k]);
-  for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kRomThreads)
+  for (uint32_t k = threadIdx.x; k < a.kv; k += kR1Threads) xv[k] = A::load(a.xv[k]);
+  for (uint32_t k = threadIdx.x; k < a.ks; k += kR1Threads) xs[k] = A::load(a.xs[k]);
+  for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kR1Threads)
     Av[e] = A::load(a.Av[(size_t)v0 * a.ks + e]);
-  for (size_t e = threadIdx.x; e < (size_t)(s1 - s0) * a.kv; e += kRomThreads)
+  for (size_t e = threadIdx.x; e < (size_t)(s1 - s0) * a.kv; e += kR1Threads)
     As[e] = A::load(a.As[(size_t)s0 * a.kv + e]);
-  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) bv[r - v0] = A::load(a.b[r]);
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) bv[r - v0] = A::load(a.b[r]);
   cluster.sync();
 
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
@@ -192,7 +196,7 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
     // (RankOneForcing keeps the whole signal time series too: forcing_rank_one.hpp:169-178)
     const double fdt = a.fdt[it];
     // 1. velocity rows of this CTA
-    for (uint32_t r = v0 + warp; r < v1; r += kRomWarps) {
+    for (uint32_t r = v0 + warp; r < v1; r += kR1Warps) {
       const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
       const T xold = xv[r];
       __syncwarp();  // every lane has read the old row before one of them overwrites the local copy
@@ -208,7 +212,7 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
     cluster.sync();
     // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185)
     if (a.fseis && n % a.fseis == 0) {
-      for (uint32_t r = crank * kRomWarps + warp; r < a.R; r += csize * kRomWarps) {
+      for (uint32_t r = crank * kR1Warps + warp; r < a.R; r += csize * kR1Warps) {
         // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
         const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
         const T s = A::dot(prow, xv, a.kv, lane);
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
       }
     }
     // 2. stress rows of this CTA
-    for (uint32_t r = s0 + warp; r < s1; r += kRomWarps) {
+    for (uint32_t r = s0 + warp; r < s1; r += kR1Warps) {
       const T y = A::dot(As + (size_t)(r - s0) * a.kv, xv, a.kv, lane);
       const T xold = xs[r];
       __syncwarp();
@@ -230,8 +234,8 @@ __global__ void __launch_bounds__(kRomThreads) rom_rank1_cluster_kernel(RomArgs 
     }
     cluster.sync();
   }
-  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kRomThreads) a.xv[r] = A::value(xv[r]);
-  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kRomThreads) a.xs[r] = A::value(xs[r]);
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) a.xv[r] = A::value(xv[r]);
+  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xs[r]);
 }
 
 __global__ void rom_split_df_kernel(const double* in, df* out, size_t n) {
@@ -366,7 +370,7 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(h->cluster);
-  cfg.blockDim = dim3(kRomThreads);
+  cfg.blockDim = dim3(kR1Threads);
   cfg.dynamicSmemBytes = h->smem;
   cfg.stream = h->stream;
   cudaLaunchAttribute attr[1];
