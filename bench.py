@@ -585,7 +585,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    if not args.no_extra:
+    if world == 1 and not args.no_extra:  # the other configurations: single-GPU runs only
         line["other_configs"] = extra_workloads(np, torch, shaw)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(np).items() if k in
