@@ -260,6 +260,7 @@ def extra_workloads(np, torch, shaw):
                              "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
                              "seismogram_max_abs": float(np.max(np.abs(res[shaw.FP64][1]))),
                              "forcing": {"depth_km": depth, "period_s": period, "delay_s": 180.0},
+                             "cpu_oracle": rom_cpu_oracle(np, av, as_, b, 2000, dt, period),
                              "basis": basis["info"]}
     # config 4: ROM rank-2, k = 512, M = 4096 forcings; FP64 (DGEMM) vs tensor-core forms
     k, M, n = 512, 4096, 100
@@ -290,10 +291,27 @@ def extra_workloads(np, torch, shaw):
         "seismogram_rel_err_ozaki": _relerr(np, res[shaw.MIXED_OZAKI_BF16][1], res[shaw.FP64][1]),
         "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
+        "cpu_oracle": rom_cpu_oracle(np, av, as_, b[:, :64], 60, dt, periods[:64]),
         "basis": "leading 512 modes of the POD basis of config 3"}
     out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
     out["fom_rank2_2000x4000_M64"] = fom_fp64_vs_fp32(np, torch, shaw)
     return out
+
+
+def rom_cpu_oracle(np, av, as_, b, nsteps, dt, periods):
+    """The oracle's ROM leapfrog (the reference's GEMV / GEMM loop restated, FP64, all host
+    threads) on a bounded sample: forcing-steps/s on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    oracle_lib.build()
+    b = np.asfortranarray(np.asarray(b, np.float64).reshape(av.shape[0], -1, order="F"))
+    M = b.shape[1]
+    periods = np.broadcast_to(np.asarray(periods, np.float64), (M,))
+    t0 = time.perf_counter()
+    oracle_lib.rom_run(av, as_, b, nsteps, dt, [2] * M, periods, [180.0] * M)
+    el = time.perf_counter() - t0
+    return {"value": M * nsteps / el, "unit": "forcing-steps/s", "cores": oracle_lib.lib().orc_num_threads(0),
+            "kind": "port", "sample": "%d steps of %d forcing column(s) (%.2f s)" % (nsteps, M, el)}
 
 
 def fom_fp64_vs_fp32(np, torch, shaw, nth=2000, nr=4000, M=64, n_time=20, n_err=1000):
