@@ -204,8 +204,11 @@ int shaw_rom_set_signals(shaw_rom_t h, const int32_t* kind, const double* period
 int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t freq_vp, uint64_t freq_sp, uint64_t nsteps, double* host_vp,
                            double* host_sp);
 /* In-loop ROM seismogram S(r, t, j) = PhiVp[gid_r, :] . xv(:, j) at every freq
- * steps (reconstructSeismogram, main_reconstruct_seismo.cc:157-185); phi_rows is
- * R x kv row-major (the basis rows of the receivers' vp gids). */
+ * steps (reconstructSeismogram, main_reconstruct_seismo.cc:157-185, whose rank-2 form
+ * the reference leaves unimplemented at :187-190); phi_rows is R x kv row-major (the
+ * basis rows of the receivers' vp gids).  FP64 and rank-1 mixed: FP64 / double-float
+ * dots; SHAW_MIXED_OZAKI_BF16: an exact sliced product on the tensor cores inside the
+ * persistent kernel; SHAW_MIXED_TF32X3: SHAW_ERR_UNSUPPORTED (use snapshots). */
 int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t num_receivers, uint64_t freq,
                            uint64_t nsteps);
 int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps);

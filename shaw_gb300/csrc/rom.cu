@@ -566,14 +566,26 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   if (h->phi_rcv_df) { cudaFree(h->phi_rcv_df); h->phi_rcv_df = nullptr; }
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
+  if (h->oz)
+    if (int rc = shaw::oz::set_receivers(h->oz, 0, nullptr, 0, nullptr, 0, 0, h->stream)) return rc;
   if (R == 0) return SHAW_OK;
-  if (h->persistent2())
+  if (h->tc)
     return shaw::fail(SHAW_ERR_UNSUPPORTED,
-                      "the tensor-core rank-2 ROM records snapshots; form the seismogram from them");
+                      "the TF32x3 rank-2 ROM records snapshots; form the seismogram from them");
   if (!phi_rows) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver rows");
   if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
   if (nsteps % freq) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Seismogram sampling frequency not a divisor of steps");
   const uint64_t T = nsteps / freq;
+  if (h->oz) {
+    // the tensor-core kernel forms the seismogram in the loop, as an exact (Ozaki) product
+    // of the sliced receiver rows with the sliced velocity state
+    if (h->kv > 65535 || freq > 0xFFFFFFFFull) return shaw::fail(SHAW_ERR_UNSUPPORTED, "receiver setup too large");
+    SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
+    SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
+    if (int rc = shaw::oz::set_receivers(h->oz, 0, phi_rows, R, h->seis, T, (uint32_t)freq, h->stream)) return rc;
+    h->R = R; h->fseis = freq; h->seis_T = T; h->seis_nsteps = nsteps;
+    return SHAW_OK;
+  }
   SHAW_CUDA(cudaMalloc(&h->phi_rcv, (size_t)R * h->kv * sizeof(double)));
   SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
   SHAW_CUDA(cudaMemcpyAsync(h->phi_rcv, phi_rows, (size_t)R * h->kv * sizeof(double), cudaMemcpyHostToDevice,

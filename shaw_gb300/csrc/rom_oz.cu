@@ -99,6 +99,12 @@ struct OzInst {
   uint32_t fvp, fsp;
   int* expo;  // [3][Mp]: per column, the exponent of the current XS slices and the predicted
               // exponents of the next XV and XS slicing (kept across launches)
+  // receivers: rows PhiVp[gid_r, :] sliced like an operator, seismogram R x T x M (device)
+  const uint8_t* Ar;  // [Rp/128][kvp/32][slice][8 KB]
+  const int* alpha_r;
+  double* seis;
+  unsigned long long Tseis;
+  uint32_t fseis, R, Rp;
   uint32_t kv, ks, kvp, ksp, M, Mp;
 };
 
@@ -529,6 +535,29 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       if (__syncthreads_or(sh->abort != 0)) break;
+      // ---------------- seismogram on sample steps: S(:, t, cols) = PhiRcv XV ----------------
+      // (main_reconstruct_seismo.cc:157-185 in the loop; the XV slices of the stress GEMM
+      // are its B operand, so the product is exact like the leapfrog's)
+      if (in.seis && in.fseis && n % in.fseis == 0) {
+        const unsigned long long tcnt = n / in.fseis - 1;
+        gemm_phase(stages, sh, in.Ar, bvt, in.Rp / 128, n_kc_s, nb, it, uses, a.error,
+                   [&](uint32_t mt, uint32_t tcols) {
+                     const uint32_t r = mt * 128 + q * 32 + lane;
+                     const int alpha = in.alpha_r[r];
+                     for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+                       float yh[8], yl[8];
+                       load_combine8(tcols, nb, q, j0, yh, yl);
+#pragma unroll
+                       for (int jj = 0; jj < 8; ++jj) {
+                         const uint32_t col = col0 + j0 + jj;
+                         if (r < in.R && col < in.M)
+                           in.seis[r + (size_t)in.R * (tcnt + in.Tseis * col)] =
+                               ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]);
+                       }
+                     }
+                   });
+        if (__syncthreads_or(sh->abort != 0)) break;
+      }
       // ---------------- stress: XS += dt As XV ----------------
       gemm_phase(stages, sh, in.As, bvt, n_mt_s, n_kc_s, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
         const uint32_t row = mt * 128 + q * 32 + lane;
@@ -842,6 +871,37 @@ int set_snapshots(Batch* p, uint32_t i, double* snap_vp, double* snap_sp, unsign
   return SHAW_OK;
 }
 
+int set_receivers(Batch* p, uint32_t i, const double* rows, uint32_t R, double* d_seis, unsigned long long T,
+                  uint32_t freq, cudaStream_t s) {
+  if (!p || i >= p->inst.size()) return fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  OzInst& in = p->inst[i];
+  SHAW_CUDA(cudaStreamSynchronize(s));
+  if (in.Ar) cudaFree((void*)in.Ar);
+  if (in.alpha_r) cudaFree((void*)in.alpha_r);
+  in.Ar = nullptr; in.alpha_r = nullptr; in.seis = nullptr; in.R = in.Rp = in.fseis = 0; in.Tseis = 0;
+  p->table_dirty = true;
+  if (R == 0) return SHAW_OK;
+  const uint32_t Rp = round_up(R, 128);
+  std::vector<uint16_t> sl;
+  std::vector<int> al;
+  slice_operator(rows, R, in.kv, Rp, in.kvp, sl, al);
+  uint8_t* dA = nullptr;
+  int* dal = nullptr;
+  SHAW_CUDA(cudaMalloc(&dA, sl.size() * 2));
+  cudaError_t e = cudaMalloc(&dal, Rp * sizeof(int));
+  if (e != cudaSuccess) {
+    cudaFree(dA);
+    return cuda_fail(e, "cudaMalloc (receiver exponents)");
+  }
+  in.Ar = dA;
+  in.alpha_r = dal;
+  SHAW_CUDA(cudaMemcpyAsync(dA, sl.data(), sl.size() * 2, cudaMemcpyHostToDevice, s));
+  SHAW_CUDA(cudaMemcpyAsync(dal, al.data(), Rp * sizeof(int), cudaMemcpyHostToDevice, s));
+  SHAW_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  in.seis = d_seis; in.R = R; in.Rp = Rp; in.Tseis = T; in.fseis = freq;
+  return SHAW_OK;
+}
+
 int reset(Batch* p, cudaStream_t s) {
   for (const OzInst& in : p->inst) {
     const size_t nv = (size_t)in.Mp * in.kvp, ns = (size_t)in.Mp * in.ksp;
@@ -972,6 +1032,10 @@ uint32_t num_ctas(const Batch* p) { return p->ctas; }
 void destroy(Batch* p) {
   if (!p) return;
   for (void* b : p->owned) cudaFree(b);
+  for (OzInst& in : p->inst) {
+    if (in.Ar) cudaFree((void*)in.Ar);
+    if (in.alpha_r) cudaFree((void*)in.alpha_r);
+  }
   void* bufs[] = {p->d_inst, p->d_tiles, p->d_order, p->d_begin, p->bvt, p->bst, p->error, p->tile_ns};
   for (void* b : bufs)
     if (b) cudaFree(b);

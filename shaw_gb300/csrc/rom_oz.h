@@ -27,6 +27,11 @@ int set_signals(Batch* p, uint32_t i, const int* kind, const double* period, con
 // Device snapshot buffers of instance i (k x T x M LayoutLeft), or nullptr / frequency 0.
 int set_snapshots(Batch* p, uint32_t i, double* snap_vp, double* snap_sp, unsigned long long Tvp,
                   unsigned long long Tsp, uint32_t fvp, uint32_t fsp);
+// Receivers of instance i: rows = PhiVp[gid_r, :] (host, R x kv row-major); on every step n
+// with n % freq == 0 the kernel writes S(r, n/freq - 1, j) = rows[r, :] . XV[:, j] into the
+// device seismogram d_seis (R x T x M LayoutLeft).  R = 0 removes them.
+int set_receivers(Batch* p, uint32_t i, const double* rows, uint32_t R, double* d_seis, unsigned long long T,
+                  uint32_t freq, cudaStream_t s);
 int reset(Batch* p, cudaStream_t s);
 // nsteps leapfrog steps of every instance, starting after step step0: one persistent launch.
 int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsigned long long nsteps);

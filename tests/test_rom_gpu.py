@@ -230,3 +230,46 @@ def test_rank2_ozaki_advance_in_pieces(shaw):
     r.synchronize()
     part = r.get_state()
     assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
+
+
+@pytest.mark.parametrize("R,freq", [(5, 1), (181, 2)])
+def test_rank2_ozaki_in_loop_seismogram(shaw, R, freq):
+    """Receivers on the tensor-core path: the seismogram formed inside the persistent
+    kernel (exact sliced product of the receiver rows with the velocity state) against
+    the FP64 path's DGEMM seismogram; a run in pieces gives the same samples."""
+    kv, ks, M, n, dt = 200, 160, 70, 400, 0.5
+    av, as_, _ = stable_system(ks, 21)
+    big_v = np.zeros((kv, ks))
+    big_v[:ks, :ks] = av * 0.2
+    big_s = np.zeros((ks, kv))
+    big_s[:ks, :ks] = as_ * 0.2
+    rng = np.random.default_rng(R)
+    b = rng.standard_normal((kv, M)) * 1e-3
+    rows = rng.standard_normal((R, kv)) / np.sqrt(kv)
+    periods = rng.uniform(30, 90, M)
+    out = {}
+    for p in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
+        r = shaw.Rom(big_v, big_s, b, rank=2, precision=p)
+        r.set_signals("gaussDer", periods, 40.0)
+        r.set_receivers(rows, freq, n)
+        r.run(dt, n)
+        out[p] = r.seismogram()
+        if p == shaw.MIXED_OZAKI_BF16:
+            r.reset()
+            r.advance(dt, 100)
+            r.advance(dt, n - 100)
+            r.synchronize()
+            assert np.array_equal(r.seismogram(), out[p])
+        r.close()
+    assert out[shaw.FP64].shape == (R, n // freq, M)
+    assert np.max(np.abs(out[shaw.FP64])) > 0
+    assert relerr(out[shaw.MIXED_OZAKI_BF16], out[shaw.FP64]) <= 1e-8
+
+
+def test_rank2_tf32x3_receivers_unsupported(shaw):
+    av, as_, _ = stable_system(128, 3)
+    r = shaw.Rom(av * 0.2, as_ * 0.2, np.ones((128, 4)) * 1e-3, rank=2, precision=shaw.MIXED_TF32X3)
+    with pytest.raises(shaw.ShawError) as e:
+        r.set_receivers(np.ones((3, 128)), 1, 10)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    r.close()
