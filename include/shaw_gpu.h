@@ -253,6 +253,12 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
  * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */
 int shaw_rom_batch_set_snapshots(shaw_rom_batch_t h, uint32_t i, uint64_t freq_vp, uint64_t freq_sp,
                                  uint64_t nsteps, double* host_vp, double* host_sp);
+/* In-loop seismogram of instance i (shaw_rom_set_receivers semantics): phi_rows R x kv
+ * row-major; the seismogram R x (nsteps/freq) x M (LayoutLeft) is read back with
+ * shaw_rom_batch_get_seismogram. */
+int shaw_rom_batch_set_receivers(shaw_rom_batch_t h, uint32_t i, const double* phi_rows, uint32_t num_receivers,
+                                 uint64_t freq, uint64_t nsteps);
+int shaw_rom_batch_get_seismogram(shaw_rom_batch_t h, uint32_t i, double* out);
 int shaw_rom_batch_reset(shaw_rom_batch_t h);
 int shaw_rom_batch_advance(shaw_rom_batch_t h, double dt, uint64_t nsteps);
 int shaw_rom_batch_run(shaw_rom_batch_t h, double dt, uint64_t nsteps);

@@ -96,6 +96,9 @@ SIGNATURES = [
     ("shaw_rom_batch_tune", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_size_t]),
     ("shaw_rom_batch_set_snapshots", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                                     ctypes.c_uint64, _dp, _dp]),
+    ("shaw_rom_batch_set_receivers", ctypes.c_int, [_vp, ctypes.c_uint32, _dp, ctypes.c_uint32, ctypes.c_uint64,
+                                                    ctypes.c_uint64]),
+    ("shaw_rom_batch_get_seismogram", ctypes.c_int, [_vp, ctypes.c_uint32, _dp]),
     ("shaw_rom_batch_reset", ctypes.c_int, [_vp]),
     ("shaw_rom_batch_advance", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     ("shaw_rom_batch_run", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
@@ -397,6 +400,7 @@ class RomBatch:
         self.h = h
         self._keep = []
         self._snaps = {}
+        self._seis = {}
 
     def close(self):
         if getattr(self, "h", None):
@@ -425,6 +429,17 @@ class RomBatch:
 
     def snapshots(self, i):
         return self._snaps[i]
+
+    def set_receivers(self, i, phi_rows, freq, nsteps):
+        pr = np.ascontiguousarray(phi_rows, np.float64)
+        _check(lib().shaw_rom_batch_set_receivers(self.h, i, _p(pr, _dp), pr.shape[0], freq, nsteps))
+        self._seis[i] = (pr.shape[0], nsteps // freq)
+
+    def seismogram(self, i):
+        R, T = self._seis[i]
+        out = np.zeros((R, T, self.shapes[i][2]), order="F")
+        _check(lib().shaw_rom_batch_get_seismogram(self.h, i, _p(out, _dp)))
+        return out
 
     def reset(self):
         _check(lib().shaw_rom_batch_reset(self.h))

@@ -32,6 +32,10 @@ struct BInst {
   // reduced-state snapshots (device, k x T x M) and the caller's host arrays
   uint64_t fvp = 0, fsp = 0, snap_nsteps = 0;
   double *snap_vp = nullptr, *snap_sp = nullptr, *host_vp = nullptr, *host_sp = nullptr;
+  // receivers: rows PhiVp[gid_r, :] (device, FP64 path) and the seismogram R x T x M (device)
+  uint32_t R = 0;
+  uint64_t fseis = 0, seis_T = 0, seis_nsteps = 0;
+  double *phi_rcv = nullptr, *seis = nullptr;
 };
 
 // Column c of the batch (over all instances) -> its instance data, for the FP64 forcing kernel.
@@ -84,6 +88,15 @@ int fp64_step(BH* h, double dt, uint64_t n) {
   SHAW_CUDA(cudaGetLastError());
   h->launches += h->inst.size() + 1;
   for (BInst& in : h->inst) {
+    if (in.fseis && n % in.fseis == 0) {
+      // S(:, t, :) = PhiRcv (R x kv) XV (kv x M)  (main_reconstruct_seismo.cc:157-185)
+      const double one1 = 1.0, zero = 0.0;
+      if (cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)in.R, (int)in.M, (int)in.kv, &one1, in.phi_rcv,
+                      (int)in.kv, in.xv, (int)in.kv, &zero, in.seis + (size_t)in.R * (n / in.fseis - 1),
+                      (int)(in.R * in.seis_T)) != CUBLAS_STATUS_SUCCESS)
+        return shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (seismogram) failed");
+      h->launches++;
+    }
     if (in.fvp && n % in.fvp == 0) {
       const uint64_t T = in.snap_nsteps / in.fvp;
       SHAW_CUDA(cudaMemcpy2DAsync(in.snap_vp + in.kv * (n / in.fvp - 1), in.kv * T * sizeof(double), in.xv,
@@ -114,7 +127,8 @@ void shaw_rom_batch_destroy(shaw_rom_batch_t h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->oz) shaw::oz::destroy(h->oz);
   for (BInst& in : h->inst) {
-    void* bufs[] = {in.Av, in.As, in.b, in.xv, in.xs, in.kind, in.period, in.delay, in.snap_vp, in.snap_sp};
+    void* bufs[] = {in.Av, in.As, in.b, in.xv, in.xs, in.kind, in.period, in.delay, in.snap_vp, in.snap_sp,
+                    in.phi_rcv, in.seis};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -216,6 +230,7 @@ int shaw_rom_batch_reset(shaw_rom_batch_t h) {
     }
   }
   for (BInst& in : h->inst) {
+    if (in.seis) SHAW_CUDA(cudaMemsetAsync(in.seis, 0, (size_t)in.R * in.seis_T * in.M * 8, h->stream));
     if (in.snap_vp) SHAW_CUDA(cudaMemsetAsync(in.snap_vp, 0, in.kv * (in.snap_nsteps / in.fvp) * in.M * 8, h->stream));
     if (in.snap_sp) SHAW_CUDA(cudaMemsetAsync(in.snap_sp, 0, in.ks * (in.snap_nsteps / in.fsp) * in.M * 8, h->stream));
   }
@@ -249,6 +264,47 @@ int shaw_rom_batch_set_snapshots(shaw_rom_batch_t h, uint32_t i, uint64_t fvp, u
   return SHAW_OK;
 }
 
+int shaw_rom_batch_set_receivers(shaw_rom_batch_t h, uint32_t i, const double* phi_rows, uint32_t R, uint64_t freq,
+                                 uint64_t nsteps) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (i >= h->inst.size()) return shaw::fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  BInst& in = h->inst[i];
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (in.phi_rcv) { cudaFree(in.phi_rcv); in.phi_rcv = nullptr; }
+  if (in.seis) { cudaFree(in.seis); in.seis = nullptr; }
+  in.R = 0; in.fseis = in.seis_T = in.seis_nsteps = 0;
+  if (h->oz)
+    if (int rc = shaw::oz::set_receivers(h->oz, i, nullptr, 0, nullptr, 0, 0, h->stream)) return rc;
+  if (R == 0) return SHAW_OK;
+  if (!phi_rows) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver rows");
+  if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
+  if (nsteps % freq) return shaw::fail(SHAW_ERR_FREQ_DIVISOR, "Seismogram sampling frequency not a divisor of steps");
+  if (freq > 0xFFFFFFFFull) return shaw::fail(SHAW_ERR_UNSUPPORTED, "seismogram frequency too large");
+  const uint64_t T = nsteps / freq;
+  SHAW_CUDA(cudaMalloc(&in.seis, std::max<size_t>(1, (size_t)R * T * in.M) * sizeof(double)));
+  SHAW_CUDA(cudaMemsetAsync(in.seis, 0, (size_t)R * T * in.M * sizeof(double), h->stream));
+  if (h->oz) {
+    if (int rc = shaw::oz::set_receivers(h->oz, i, phi_rows, R, in.seis, T, (uint32_t)freq, h->stream)) return rc;
+  } else {
+    SHAW_CUDA(cudaMalloc(&in.phi_rcv, (size_t)R * in.kv * sizeof(double)));
+    SHAW_CUDA(cudaMemcpyAsync(in.phi_rcv, phi_rows, (size_t)R * in.kv * sizeof(double), cudaMemcpyHostToDevice,
+                              h->stream));
+  }
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  in.R = R; in.fseis = freq; in.seis_T = T; in.seis_nsteps = nsteps;
+  return SHAW_OK;
+}
+
+int shaw_rom_batch_get_seismogram(shaw_rom_batch_t h, uint32_t i, double* out) {
+  if (!h || !out) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
+  if (i >= h->inst.size()) return shaw::fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
+  const BInst& in = h->inst[i];
+  if (!in.seis) return shaw::fail(SHAW_ERR_STATE, "no receivers set");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  SHAW_CUDA(cudaMemcpy(out, in.seis, (size_t)in.R * in.seis_T * in.M * sizeof(double), cudaMemcpyDeviceToHost));
+  return SHAW_OK;
+}
+
 int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, char* report, size_t cap) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
@@ -271,9 +327,12 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
 int shaw_rom_batch_advance(shaw_rom_batch_t h, double dt, uint64_t nsteps) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
-  for (const BInst& in : h->inst)
+  for (const BInst& in : h->inst) {
     if (in.fvp && h->step + nsteps > in.snap_nsteps)
       return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
+    if (in.fseis && h->step + nsteps > in.seis_nsteps)
+      return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the seismogram was sized for");
+  }
   if (nsteps == 0) return SHAW_OK;
   if (h->oz) {
     if (int rc = shaw::oz::advance(h->oz, h->stream, dt, h->step, nsteps)) return rc;

@@ -140,3 +140,32 @@ def test_batch_errors(shaw):
     bt.set_snapshots(0, 2, 2, 10)
     with pytest.raises(shaw.ShawError):
         bt.advance(0.5, 11)
+
+
+def test_batch_seismograms(shaw):
+    """Per-instance receivers: the FP64 batch equals the single-system FP64 path, the
+    tensor-core batch (seismogram formed inside the persistent kernel) is within 1e-8."""
+    insts = _instances(7)
+    n, dt = 200, 0.5
+    rng = np.random.default_rng(8)
+    rows = [rng.standard_normal((R, d["rom_jvp"].shape[0])) for R, d in zip((3, 130, 1, 7, 20), insts)]
+    freqs = (1, 2, 4, 1, 5)
+    seis = {}
+    for p in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
+        bt = shaw.RomBatch(insts, precision=p)
+        for i in range(len(insts)):
+            bt.set_receivers(i, rows[i], freqs[i], n)
+        bt.run(dt, n)
+        seis[p] = [bt.seismogram(i) for i in range(len(insts))]
+        bt.close()
+    for i, d in enumerate(insts):
+        r = shaw.Rom(d["rom_jvp"], d["rom_jsp"], d["b"], rank=2)
+        r.set_signals(d["kind"], d["period"], d["delay"])
+        r.set_receivers(rows[i], freqs[i], n)
+        r.run(dt, n)
+        single = r.seismogram()
+        r.close()
+        assert seis[shaw.FP64][i].shape == single.shape
+        assert np.max(np.abs(single)) > 0
+        assert relerr(seis[shaw.FP64][i], single) <= 1e-14
+        assert relerr(seis[shaw.MIXED_OZAKI_BF16][i], single) <= 1e-8
