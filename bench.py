@@ -228,6 +228,20 @@ def extra_workloads(np, torch, shaw):
     out["fom_rank1_101x201"] = {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t,
                                 "steps": n, "us_per_step": t / n * 1e6}
     f.close()
+    # the same job on the reference's fixture orientation (tests/fullMesh101x201: 201 theta x 101 r)
+    fx = shaw.Mesh.generate(201, 101)
+    fx.set_material("unilayer", MATERIAL)
+    dtx = 0.25 * min(fx.info[5], fx.info[4] * fx.info[2]) / (2.0 ** 0.5 * 7300.0)
+    f = shaw.Fom(fx, 1, 1)
+    f.set_sources([fx.map_source(640.0, 0.0)], "gaussDer", 60.0, 180.0)
+    f.set_receivers([fx.map_receiver(float(a)) for a in range(181)], 1, n)
+    f.run(dtx, n)
+    f.reset()
+    t = _timed(torch, f.stream, lambda: f.advance(dtx, n))
+    f.synchronize()
+    out["fom_rank1_fixture_201x101"] = {"metric": "FOM DOF-updates/s", "value": (fx.nvp + fx.nsp) * n / t,
+                                        "steps": n, "us_per_step": t / n * 1e6}
+    f.close()
     basis = pod_basis(np, shaw, mesh, dt)
     rcv = [mesh.map_receiver(float(a)) for a in range(181)]
     rho_inv = mesh.arrays()["rho_inv_vp"]

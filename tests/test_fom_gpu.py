@@ -224,3 +224,31 @@ def test_error_paths(shaw, oracle):
     with pytest.raises(shaw.ShawError) as e:
         f.synchronize()
     assert e.value.code == shaw.ERR_NONFINITE
+
+
+def test_config1_both_orientations_match_oracle(shaw, oracle, tmp_path):
+    """Config 1 as worded (101 theta x 201 r) and the reference fixture's orientation
+    (tests/fullMesh101x201: 201 theta x 101 r), axis source at 640 km, receivers every
+    degree: GPU rank-1 run against the oracle."""
+    for nth, nr in ((101, 201), (201, 101)):
+        m = shaw.Mesh.generate(nth, nr)
+        m.set_material("unilayer", CFG_MATERIAL)
+        d = str(tmp_path / ("m%dx%d" % (nth, nr)))
+        os.makedirs(d)
+        m.write(d)
+        om = oracle.OracleMesh(d)
+        om.set_material("unilayer", [(CFG_MATERIAL[0:3], CFG_MATERIAL[3:6])])
+        dt = 0.25 * min(m.info[5], m.info[4] * m.info[2]) / (np.sqrt(2.0) * 7300.0)
+        n = 300
+        src = m.map_source(640.0, 0.0)
+        assert src == om.map_source(640.0, 0.0)
+        rcv = [m.map_receiver(float(a)) for a in range(181)]
+        f = shaw.Fom(m, 1, 1)
+        f.set_sources([src], "gaussDer", 60.0, 20.0)
+        f.set_receivers(rcv, 1, n)
+        f.run(dt, n)
+        ref = om.fom_run(1, n, dt, [src], [2], [60.0], [20.0], rcv, 1, 0, 0)
+        vp, sp = f.get_state()
+        assert relerr(vp, ref["final_vp"]) <= RTOL and relerr(sp, ref["final_sp"]) <= RTOL
+        assert relerr(f.seismogram(), ref["seis"]) <= RTOL
+        f.close()
