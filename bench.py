@@ -46,8 +46,9 @@ def parse():
     p.add_argument("--forcings", type=int, default=M)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the other configurations' lines")
-    p.add_argument("--profile-rom", default=None, choices=["ozaki", "tf32x3", "fp64"],
-                   help="only run the rank-2 ROM (k=512, M=4096) for --steps steps, for profiler captures")
+    p.add_argument("--profile-rom", default=None, choices=["ozaki", "tf32x3", "fp64", "rank1-fp64", "rank1-mixed"],
+                   help="only run the rank-2 ROM (k=512, M=4096) or the rank-1 ROM (k=256, 181 receivers) "
+                        "for --steps steps, for profiler captures")
     p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32"],
                    help="only run the FOM on the 1000x2000 grid with --forcings columns for --steps steps")
     return p.parse_args()
@@ -637,11 +638,19 @@ def main():
         import numpy as np
         import shaw_gb300 as shaw
         shaw.build()
-        prec = {"ozaki": shaw.MIXED_OZAKI_BF16, "tf32x3": shaw.MIXED_TF32X3, "fp64": shaw.FP64}[args.profile_rom]
-        av, as_ = stable_rom(np, 512, 7, 0.004, 0.2)
-        rng = np.random.default_rng(8)
-        r = shaw.Rom(av, as_, rng.standard_normal((512, 4096)) * 1e-3, rank=2, precision=prec)
-        r.set_signals("gaussDer", rng.uniform(30.0, 90.0, 4096), 180.0)
+        if args.profile_rom.startswith("rank1"):
+            av, as_ = stable_rom(np, 256, 3, 0.004, 0.2)
+            rng = np.random.default_rng(4)
+            prec = shaw.FP64 if args.profile_rom == "rank1-fp64" else shaw.MIXED_FP32
+            r = shaw.Rom(av, as_, rng.standard_normal(256) * 1e-3, rank=1, precision=prec)
+            r.set_signals("gaussDer", 60.0, 180.0)
+            r.set_receivers(rng.standard_normal((181, 256)) / 16.0, 1, args.steps)
+        else:
+            prec = {"ozaki": shaw.MIXED_OZAKI_BF16, "tf32x3": shaw.MIXED_TF32X3, "fp64": shaw.FP64}[args.profile_rom]
+            av, as_ = stable_rom(np, 512, 7, 0.004, 0.2)
+            rng = np.random.default_rng(8)
+            r = shaw.Rom(av, as_, rng.standard_normal((512, 4096)) * 1e-3, rank=2, precision=prec)
+            r.set_signals("gaussDer", rng.uniform(30.0, 90.0, 4096), 180.0)
         r.run(0.5, args.steps)
         print(json.dumps({"profile_rom": args.profile_rom, "steps": args.steps, "launches": r.kernel_launches}))
         r.close()

@@ -143,8 +143,8 @@ struct Arith<false> {
     return warp_sum(acc);
   }
   // x + dt*y, then + fdt*b when b != null: KokkosBlas::gemv then axpy roundings
-  __device__ static T update(T x, T y, double dt) { return __dadd_rn(x, __dmul_rn(dt, y)); }
-  __device__ static T axpy(T x, double a, T b) { return __dadd_rn(x, __dmul_rn(a, b)); }
+  __device__ static T update(T x, T y, T dt) { return __dadd_rn(x, __dmul_rn(dt, y)); }
+  __device__ static T axpy(T x, T a, T b) { return __dadd_rn(x, __dmul_rn(a, b)); }
 };
 
 template <>
@@ -158,8 +158,9 @@ struct Arith<true> {
     warp_sum_df(s, c);
     return df_norm(s, c);
   }
-  __device__ static T update(T x, T y, double dt) { return df_add(x, df_mul(df_split(dt), y)); }
-  __device__ static T axpy(T x, double a, T b) { return df_add(x, df_mul(df_split(a), b)); }
+  // dt and a arrive already split (once per launch / per step, not per row)
+  __device__ static T update(T x, T y, T dt) { return df_add(x, df_mul(dt, y)); }
+  __device__ static T axpy(T x, T a, T b) { return df_add(x, df_mul(a, b)); }
 };
 
 // One persistent launch for nsteps ROM rank-1 leapfrog steps (one cluster).
@@ -190,28 +191,32 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) bv[r - v0] = A::load(a.b[r]);
   cluster.sync();
 
+  const T dtT = A::load(a.dt);
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
     const unsigned long long n = a.step0 + it + 1;
     // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt, from the table filled before the launch
     // (RankOneForcing keeps the whole signal time series too: forcing_rank_one.hpp:169-178)
-    const double fdt = a.fdt[it];
+    const T fdt = A::load(a.fdt[it]);
+    // sample steps of the observers, decided once per step
+    const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
+    const bool seis_now = a.fseis && n % a.fseis == 0;
     // 1. velocity rows of this CTA
     for (uint32_t r = v0 + warp; r < v1; r += kR1Warps) {
       const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
       const T xold = xv[r];
       __syncwarp();  // every lane has read the old row before one of them overwrites the local copy
       if (lane < (int)csize) {
-        T x = A::update(xold, y, a.dt);
+        T x = A::update(xold, y, dtT);
         x = A::axpy(x, fdt, bv[r - v0]);
         T* dst = cluster.map_shared_rank(xv + r, lane);
         *dst = x;
-        if (lane == 0 && a.fvp && n % a.fvp == 0)
+        if (lane == 0 && snap_v)
           a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
       }
     }
     cluster.sync();
     // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185)
-    if (a.fseis && n % a.fseis == 0) {
+    if (seis_now) {
       for (uint32_t r = crank * kR1Warps + warp; r < a.R; r += csize * kR1Warps) {
         // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
         const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
@@ -225,10 +230,10 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
       const T xold = xs[r];
       __syncwarp();
       if (lane < (int)csize) {
-        const T x = A::update(xold, y, a.dt);
+        const T x = A::update(xold, y, dtT);
         T* dst = cluster.map_shared_rank(xs + r, lane);
         *dst = x;
-        if (lane == 0 && a.fsp && n % a.fsp == 0)
+        if (lane == 0 && snap_s)
           a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
       }
     }
