@@ -249,6 +249,11 @@ void shaw_rom_batch_destroy(shaw_rom_batch_t h);
  * steps; keeps the fastest and leaves the batch reset.  A report of the candidates
  * goes to report[cap] (may be NULL). */
 int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, char* report, size_t cap);
+/* Fixed tiling of a tensor-core batch (e.g. one the autotuner chose before): tiles of
+ * width 16, 32 or 64 forcing columns; paired != 0 splits every tile's rows across two
+ * co-resident CTAs (needs >= 256 modes per dof and 2 x tiles <= SMs, else
+ * SHAW_ERR_UNSUPPORTED).  SHAW_ERR_UNSUPPORTED on FP64 batches. */
+int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired);
 /* Reduced-state snapshots of instance i: kv x (nsteps/freq_vp) x M and
  * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */
 int shaw_rom_batch_set_snapshots(shaw_rom_batch_t h, uint32_t i, uint64_t freq_vp, uint64_t freq_sp,

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("shaw_rom_batch_create", ctypes.c_int, [ctypes.c_uint32, _vp, ctypes.c_int, ctypes.POINTER(_vp)]),
     ("shaw_rom_batch_destroy", None, [_vp]),
     ("shaw_rom_batch_tune", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_size_t]),
+    ("shaw_rom_batch_set_tiling", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_int]),
     ("shaw_rom_batch_set_snapshots", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                                     ctypes.c_uint64, _dp, _dp]),
     ("shaw_rom_batch_set_receivers", ctypes.c_int, [_vp, ctypes.c_uint32, _dp, ctypes.c_uint32, ctypes.c_uint64,
@@ -414,6 +415,11 @@ class RomBatch:
         buf = ctypes.create_string_buffer(4096)
         _check(lib().shaw_rom_batch_tune(self.h, dt, trial_steps, buf, len(buf)))
         return buf.value.decode()
+
+    def set_tiling(self, width, paired=False):
+        """Fixed tensor-core tiling: `width` forcing columns per tile (16, 32, 64), each
+        tile optionally split across two co-resident CTAs."""
+        _check(lib().shaw_rom_batch_set_tiling(self.h, width, int(bool(paired))))
 
     def describe(self):
         buf = ctypes.create_string_buffer(512)

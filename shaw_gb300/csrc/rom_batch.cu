@@ -310,8 +310,10 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
   if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
   std::string rep;
   if (h->oz) {
-    if (int rc = shaw::oz::tune(h->oz, h->stream, dt, trial_steps, rep)) return rc;
-    h->launches += 1 + 6;  // warm-up + two timings per candidate width
+    unsigned long long n = 0;
+    const int rc = shaw::oz::tune(h->oz, h->stream, dt, trial_steps, rep, n);
+    h->launches += n;
+    if (rc) return rc;
   } else {
     rep = "FP64: cuBLAS DGEMM per instance, nothing to tune\n";
   }
@@ -322,6 +324,12 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
     report[cap - 1] = '\0';
   }
   return SHAW_OK;
+}
+
+int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (!h->oz) return shaw::fail(SHAW_ERR_UNSUPPORTED, "FP64 batches have no tiling");
+  return shaw::oz::set_tiling(h->oz, width, paired != 0);
 }
 
 int shaw_rom_batch_advance(shaw_rom_batch_t h, double dt, uint64_t nsteps) {

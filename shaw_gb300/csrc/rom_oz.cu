@@ -108,8 +108,11 @@ struct OzInst {
   uint32_t kv, ks, kvp, ksp, M, Mp;
 };
 
+// pinfo: bit 0 = part (0 or 1), bit 1 = paired, bits 2.. = pair slot.  A paired tile is
+// advanced by two co-resident CTAs that split its 128-row M-tiles between them and share
+// the B slices (global memory), the column maxima and a step barrier (pair_sync).
 struct OzTile {
-  uint32_t inst, col0, nb, pad;
+  uint32_t inst, col0, nb, pinfo;
 };
 
 struct OzArgs {
@@ -124,6 +127,8 @@ struct OzArgs {
   unsigned long long step0, nsteps;
   unsigned int* error;
   unsigned long long* tile_ns;  // per tile: device time of its last run
+  unsigned int* pair_sync;      // per pair slot: arrival counter (zeroed before each launch)
+  unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima (zeroed before each launch)
 };
 
 struct Shared {
@@ -163,7 +168,7 @@ __device__ __forceinline__ void acc_next(uint32_t nbuf, uint32_t (&uses)[2], uin
 // 4..11 while the MMAs of the next M-tile fill the other set.
 template <typename Epi>
 __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const uint8_t* Aop, const uint8_t* Bop,
-                                           uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
+                                           uint32_t mt0, uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
                                            uint32_t (&uses)[2], unsigned int* err, Epi epi) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb), nbuf = acc_buffers(nb);
@@ -174,7 +179,7 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
       const uint32_t mt = q / n_kc, c = q - mt * n_kc;
       uint8_t* st = stages + (size_t)s * kStageBytes;
       mbar_expect_tx(&sh->full[s], kABytes + bbytes);
-      bulk_g2s(st, Aop + ((size_t)mt * n_kc + c) * kABytes, kABytes, &sh->full[s]);
+      bulk_g2s(st, Aop + ((size_t)(mt0 + mt) * n_kc + c) * kABytes, kABytes, &sh->full[s]);
       bulk_g2s(st + kABytes, Bop + (size_t)c * bbytes, bbytes, &sh->full[s]);
     }
   } else if (warp == 1 && lane == 0) {
@@ -229,7 +234,7 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
       acc_next(nbuf, lu, buf, par);
       if (!mbar_wait(&sh->acc_full[buf], par)) { raise(sh, err, 8u); break; }
       tc_fence_after();
-      if (!sh->abort) epi(mt, sh->tmem + buf * 256u);
+      if (!sh->abort) epi(mt0 + mt, sh->tmem + buf * 256u);
       tc_fence_before();
       mbar_arrive(&sh->acc_empty[buf]);
     }
@@ -279,18 +284,19 @@ __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q
 // Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
 // into the BF16 B tiles with per-column exponents beta[j] (|x| < 2^beta).
 __device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t nb,
-                                            const int* beta, uint8_t* tiles, unsigned long long mask) {
+                                            const int* beta, uint8_t* tiles, unsigned long long mask, uint32_t r0,
+                                            uint32_t r1) {
   const uint32_t t = threadIdx.x - 128;
   const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);
-  const uint32_t n = kp * nb;
+  const uint32_t nr = r1 - r0, n = nr * nb;
   for (uint32_t e0 = t; e0 < n; e0 += 4 * kEpiThreads) {
     float vh[4], vl[4];
     uint32_t jj[4], rr[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const uint32_t e = e0 + u * kEpiThreads;
-      jj[u] = e / kp;
-      rr[u] = e - jj[u] * kp;
+      jj[u] = e / (nr ? nr : 1);
+      rr[u] = r0 + (e - jj[u] * nr);
       if (e < n && ((mask >> jj[u]) & 1ull)) {
         vh[u] = xh[(size_t)jj[u] * kp + rr[u]];
         vl[u] = xl[(size_t)jj[u] * kp + rr[u]];
@@ -388,6 +394,31 @@ __device__ __forceinline__ void note_max8(Shared* sh, uint32_t j0, const float* 
 
 __device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
+// Step barrier of the two CTAs of a paired tile (block-wide call).  Thread 0 publishes this
+// CTA's global writes (release), counts its arrival and waits, bounded, until the peer has
+// arrived as often; then it acquires the peer's writes for the generic and the bulk-copy
+// (async) proxies.  A wait that runs out raises the error flag.
+__device__ __forceinline__ void pair_sync(Shared* sh, unsigned int* ctr, uint32_t& nsync, unsigned int* err) {
+  __syncthreads();
+  ++nsync;
+  if (threadIdx.x == 0 && !sh->abort) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    bool ok = false;
+    for (unsigned long long i = 0; i < kWaitLimit; ++i) {
+      if (*reinterpret_cast<volatile unsigned int*>(ctr) >= 2u * nsync) {
+        ok = true;
+        break;
+      }
+      __nanosleep(64);
+    }
+    if (!ok) raise(sh, err, 32u);
+    __threadfence();
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* stages = smem;
@@ -395,8 +426,6 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ew = warp - 4;  // >= 0 on the epilogue warps
   const int q = warp & 3;   // TMEM lane quarter of this warp
-  uint8_t* bvt = a.bvt + (size_t)blockIdx.x * a.bscratch;
-  uint8_t* bst = a.bst + (size_t)blockIdx.x * a.bscratch;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -436,6 +465,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     if (__syncthreads_or(sh->abort != 0)) break;
     const OzInst& in = sh->in;
     const uint32_t nb = sh->tile.nb, col0 = sh->tile.col0;
+    const bool paired = (sh->tile.pinfo & 2u) != 0u;
+    const uint32_t part = sh->tile.pinfo & 1u, slot = sh->tile.pinfo >> 2;
     const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
     const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);             // B-tile geometry
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
@@ -445,15 +476,50 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     float* const xsl = in.xsl + (size_t)col0 * in.ksp;
     const float* const bh = in.bh + (size_t)col0 * in.kvp;
     const float* const bl = in.bl + (size_t)col0 * in.kvp;
+    // M-tiles of this CTA: all of them, or its half of a paired tile (part 0 the first
+    // ceil(n/2), part 1 the rest); the B slices are then one buffer per pair
+    auto half = [&](uint32_t n, uint32_t& m0, uint32_t& m1) {
+      m0 = (paired && part) ? (n + 1) / 2 : 0u;
+      m1 = (paired && !part) ? (n + 1) / 2 : n;
+    };
+    uint32_t mv0, mv1, ms0, ms1, mr0, mr1;
+    half(n_mt_v, mv0, mv1);
+    half(n_mt_s, ms0, ms1);
+    half(in.Rp / 128, mr0, mr1);
+    uint8_t* const bvt = a.bvt + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
+    uint8_t* const bst = a.bst + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
+    unsigned int* const pctr = paired ? a.pair_sync + slot : nullptr;
+    unsigned int* const pcol = paired ? a.pair_colmax + (size_t)slot * 4 * kMaxNb : nullptr;  // [parity][part][nb]
+    uint32_t nsync = 0, nx = 0;
+    // Paired: combine the column maxima of both parts (block-wide call).  Each part
+    // stores its own maxima, both pass the step barrier, each folds in the peer's; the
+    // buffers alternate between exchanges, so a part never overwrites maxima the peer
+    // has yet to read (it would first have to pass the next barrier).
+    auto exchange = [&]() {
+      const uint32_t t = threadIdx.x - 128;
+      unsigned int* const xb = pcol + (size_t)(nx & 1u) * 2 * kMaxNb;
+      ++nx;
+      if (ew >= 0) {
+        asm volatile("fence.proxy.async.global;" ::: "memory");  // slices written in the phase, for the peer's TMA
+        epi_barrier();
+        if (t < nb) __stcg(xb + part * kMaxNb + t, sh->colmax[t]);
+      }
+      pair_sync(sh, pctr, nsync, a.error);
+      if (ew >= 0 && t < nb) sh->colmax[t] = max(sh->colmax[t], __ldcg(xb + (part ^ 1u) * kMaxNb + t));
+    };
 
     // B tiles of the current XS (the state may be non-zero when advancing in pieces):
     // with the exponents the previous launch left (so a run in pieces slices exactly
     // as an uninterrupted run), or exact exponents for a fresh state
     if (ew >= 0) {
-      for (uint32_t e = threadIdx.x - 128; e < in.ksp * nb; e += kEpiThreads) {
-        const uint32_t j = e / in.ksp, row = e - j * in.ksp;
+      const uint32_t nr = (ms1 - ms0) * 128;
+      for (uint32_t e = threadIdx.x - 128; e < nr * nb; e += kEpiThreads) {
+        const uint32_t j = e / nr, row = ms0 * 128 + (e - j * nr);
         atomicMax(&sh->colmax[j], __float_as_uint(fabsf(xsh[(size_t)j * in.ksp + row])));
       }
+    }
+    if (paired) exchange();
+    if (ew >= 0) {
       epi_barrier();
       column_exponents(sh, nb, sh->beta_s, sh->pred_s);
       const uint32_t t = threadIdx.x - 128;
@@ -466,9 +532,10 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
       }
       epi_barrier();
-      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull);
+      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
+    if (paired) pair_sync(sh, pctr, nsync, a.error);  // both halves of the XS slices written
     if (__syncthreads_or(sh->abort != 0)) break;
 
     for (unsigned long long st = 0; st < a.nsteps; ++st) {
@@ -490,7 +557,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
       const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
       // ---------------- velocity: XV += dt Av XS + fdt b ----------------
-      gemm_phase(stages, sh, in.Av, bst, n_mt_v, n_kc_v, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+      gemm_phase(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row];
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
@@ -526,21 +593,25 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           note_max8(sh, j0, ph);
         }
       });
+      if (paired) exchange();
       if (ew >= 0) {
         epi_barrier();
         settle_exponents(sh, nb, sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s);
         epi_barrier();
         const unsigned long long redo = sh->reslice_v;
-        if (redo && !sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo);
+        if (redo && !sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
+      // paired: the re-sliced rows of both parts must land before either reads them (the
+      // mask is the same in both parts, so both take this barrier or neither)
+      if (paired && __syncthreads_or(ew >= 0 && sh->reslice_v != 0ull)) pair_sync(sh, pctr, nsync, a.error);
       if (__syncthreads_or(sh->abort != 0)) break;
       // ---------------- seismogram on sample steps: S(:, t, cols) = PhiRcv XV ----------------
       // (main_reconstruct_seismo.cc:157-185 in the loop; the XV slices of the stress GEMM
       // are its B operand, so the product is exact like the leapfrog's)
       if (in.seis && in.fseis && n % in.fseis == 0) {
         const unsigned long long tcnt = n / in.fseis - 1;
-        gemm_phase(stages, sh, in.Ar, bvt, in.Rp / 128, n_kc_s, nb, it, uses, a.error,
+        gemm_phase(stages, sh, in.Ar, bvt, mr0, mr1 - mr0, n_kc_s, nb, it, uses, a.error,
                    [&](uint32_t mt, uint32_t tcols) {
                      const uint32_t r = mt * 128 + q * 32 + lane;
                      const int alpha = in.alpha_r[r];
@@ -559,7 +630,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         if (__syncthreads_or(sh->abort != 0)) break;
       }
       // ---------------- stress: XS += dt As XV ----------------
-      gemm_phase(stages, sh, in.As, bvt, n_mt_s, n_kc_s, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+      gemm_phase(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row];
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
@@ -592,17 +663,19 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           note_max8(sh, j0, ph);
         }
       });
+      if (paired) exchange();
       if (ew >= 0) {
         epi_barrier();
         settle_exponents(sh, nb, sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v);
         epi_barrier();
         const unsigned long long redo = sh->reslice_s;
-        if (redo && !sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo);
+        if (redo && !sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
+      if (paired && __syncthreads_or(ew >= 0 && sh->reslice_s != 0ull)) pair_sync(sh, pctr, nsync, a.error);
       if (__syncthreads_or(sh->abort != 0)) break;
     }
-    if (ew >= 0 && threadIdx.x - 128 < nb) {  // exponents for the next launch
+    if (ew >= 0 && threadIdx.x - 128 < nb && part == 0u) {  // exponents for the next launch
       const uint32_t t = threadIdx.x - 128;
       in.expo[col0 + t] = sh->beta_s[t];
       in.expo[in.Mp + col0 + t] = sh->pred_v[t];
@@ -705,6 +778,7 @@ struct Batch {
   std::vector<void*> owned;  // device buffers of the instances
   // tiling
   uint32_t width = 32;
+  bool paired = false;  // every tile split over two co-resident CTAs (one tile part per CTA)
   std::string sched_source = "model";
   std::vector<OzTile> tiles;
   std::vector<uint32_t> order, begin;
@@ -716,6 +790,7 @@ struct Batch {
   size_t bscratch = 0;
   unsigned int* error = nullptr;
   unsigned long long* tile_ns = nullptr;
+  unsigned int *pair_sync = nullptr, *pair_colmax = nullptr;
   size_t smem = 0;
   int sms = 0;
   bool table_dirty = true, tiles_dirty = true;
@@ -735,14 +810,46 @@ double tile_model_cost(const OzInst& in, uint32_t nb) {
   return (double)nb * ((double)in.kvp * in.ksp * 21.0 / 2048.0 + 15.0 * (in.kvp + in.ksp)) + 2000.0;
 }
 
-void build_tiles(Batch* p, uint32_t W) {
+// Paired tiling is possible when every instance has at least two M-tiles per phase and the
+// tile parts fit one per SM (the two parts of a pair wait on each other, so all CTAs must
+// be resident at once: the launch is cooperative).
+bool pairing_fits(const Batch* p, uint32_t W) {
+  uint32_t n = 0;
+  for (const OzInst& in : p->inst) {
+    if (in.kvp < 256 || in.ksp < 256) return false;
+    const uint32_t nb = tile_width_for(in.M, W);
+    n += (in.M + nb - 1) / nb;
+  }
+  return 2 * n <= (uint32_t)p->sms;
+}
+
+void build_tiles(Batch* p, uint32_t W, bool paired = false) {
   p->width = W;
+  p->paired = paired;
   p->tiles.clear();
+  uint32_t slot = 0;
   for (uint32_t i = 0; i < (uint32_t)p->inst.size(); ++i) {
     const uint32_t nb = tile_width_for(p->inst[i].M, W);
-    for (uint32_t c = 0; c < p->inst[i].M; c += nb) p->tiles.push_back({i, c, nb, 0u});
+    for (uint32_t c = 0; c < p->inst[i].M; c += nb, ++slot) {
+      if (!paired) {
+        p->tiles.push_back({i, c, nb, 0u});
+      } else {
+        p->tiles.push_back({i, c, nb, (slot << 2) | 2u});
+        p->tiles.push_back({i, c, nb, (slot << 2) | 3u});
+      }
+    }
   }
   p->ctas = std::min<uint32_t>((uint32_t)p->tiles.size(), (uint32_t)p->sms);
+  if (paired) {  // one tile part per CTA
+    p->order.resize(p->tiles.size());
+    std::iota(p->order.begin(), p->order.end(), 0u);
+    p->begin.resize(p->ctas + 1);
+    std::iota(p->begin.begin(), p->begin.end(), 0u);
+    p->model_makespan = tile_model_cost(p->inst[0], p->tiles[0].nb) / 2;
+    p->sched_source = "paired";
+    p->tiles_dirty = true;
+    return;
+  }
   std::vector<double> cost(p->tiles.size());
   for (size_t t = 0; t < p->tiles.size(); ++t) cost[t] = tile_model_cost(p->inst[p->tiles[t].inst], p->tiles[t].nb);
   lpt_schedule(cost, p->ctas, p->order, p->begin, p->model_makespan);
@@ -795,7 +902,7 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
     in.kv = d[i].kv; in.ks = d[i].ks; in.M = d[i].M;
     in.kvp = round_up(in.kv, 128); in.ksp = round_up(in.ks, 128); in.Mp = round_up(in.M, kMaxNb);
     kmax_p = std::max(kmax_p, std::max(in.kvp, in.ksp));
-    b->max_tiles += (in.M + 15) / 16;
+    b->max_tiles += 2 * ((in.M + 15) / 16);
     std::vector<uint16_t> sv, ss;
     std::vector<int> av, as;
     slice_operator(d[i].Av, in.kv, in.ks, in.kvp, in.ksp, sv, av);
@@ -842,10 +949,24 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
   OZ_TRY(cudaMalloc(&b->bst, (size_t)b->sms * b->bscratch));
   OZ_TRY(cudaMalloc(&b->error, sizeof(unsigned int)));
   OZ_TRY(cudaMalloc(&b->tile_ns, b->max_tiles * sizeof(unsigned long long)));
+  OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)b->sms * sizeof(unsigned int)));
+  OZ_TRY(cudaMalloc(&b->pair_colmax, (size_t)b->sms * 4 * kMaxNb * sizeof(unsigned int)));
 #undef OZ_TRY
   b->smem = (size_t)kStages * kStageBytes + sizeof(Shared);
-  // default tiling: 32-column tiles (64 when a single wide system fills every SM twice)
-  build_tiles(b, (n == 1 && d[0].M >= 64u * (uint32_t)b->sms) ? 64u : 32u);
+  // default tiling: tiles split across CTA pairs where they fit (the widest tiles that
+  // still occupy half the SMs, else the narrowest); otherwise 32-column tiles (64 when a
+  // single wide system fills every SM twice)
+  uint32_t pw = 0;
+  for (uint32_t W : {16u, 32u, 64u}) {
+    if (!pairing_fits(b, W)) continue;
+    uint32_t parts = 0;
+    for (const OzInst& in : b->inst) parts += 2 * ((in.M + tile_width_for(in.M, W) - 1) / tile_width_for(in.M, W));
+    if (pw == 0 || 2 * parts >= (uint32_t)b->sms) pw = W;
+  }
+  if (pw)
+    build_tiles(b, pw, true);
+  else
+    build_tiles(b, (n == 1 && d[0].M >= 64u * (uint32_t)b->sms) ? 64u : 32u);
   p = b;
   return reset(p, s);
 }
@@ -924,8 +1045,16 @@ int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsig
   a.inst = p->d_inst; a.tiles = p->d_tiles; a.order = p->d_order; a.cta_begin = p->d_begin;
   a.bvt = p->bvt; a.bst = p->bst; a.bscratch = p->bscratch;
   a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error; a.tile_ns = p->tile_ns;
+  a.pair_sync = p->pair_sync; a.pair_colmax = p->pair_colmax;
   SHAW_CUDA(cudaFuncSetAttribute(rom_rank2_ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
-  rom_rank2_ozaki_kernel<<<p->ctas, kThreads, p->smem, s>>>(a);
+  if (p->paired) {  // the parts of a pair wait on each other: all CTAs resident (cooperative launch)
+    SHAW_CUDA(cudaMemsetAsync(p->pair_sync, 0, p->ctas / 2 * sizeof(unsigned int), s));
+    void* args[] = {&a};
+    SHAW_CUDA(cudaLaunchCooperativeKernel((const void*)rom_rank2_ozaki_kernel, dim3(p->ctas), dim3(kThreads), args,
+                                          p->smem, s));
+  } else {
+    rom_rank2_ozaki_kernel<<<p->ctas, kThreads, p->smem, s>>>(a);
+  }
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
 }
@@ -949,8 +1078,18 @@ int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs) {
   return SHAW_OK;
 }
 
-int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report) {
+int set_tiling(Batch* p, uint32_t width, bool paired) {
+  if (width != 16 && width != 32 && width != 64) return fail(SHAW_ERR_INVALID_ARG, "tile width must be 16, 32 or 64");
+  if (paired && !pairing_fits(p, width))
+    return fail(SHAW_ERR_UNSUPPORTED, "paired tiles need >= 256 modes per dof and two CTAs per tile on the SMs");
+  build_tiles(p, width, paired);
+  return SHAW_OK;
+}
+
+int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report,
+         unsigned long long& launches) {
   if (trial_steps == 0) trial_steps = 1;
+  launches = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   SHAW_CUDA(cudaEventCreate(&e0));
   SHAW_CUDA(cudaEventCreate(&e1));
@@ -960,6 +1099,7 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
     if (int r = upload(p, s)) return r;
     SHAW_CUDA(cudaEventRecord(e0, s));
     if (int r = advance(p, s, dt, 0, trial_steps)) return r;
+    ++launches;
     SHAW_CUDA(cudaEventRecord(e1, s));
     if (int r = check(p, s)) return r;
     SHAW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -968,6 +1108,7 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
   struct Best {
     float ms = 1e30f;
     uint32_t width = 32;
+    bool paired = false;
     std::vector<OzTile> tiles;
     std::vector<uint32_t> order, begin;
     uint32_t ctas = 0;
@@ -990,7 +1131,7 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
       std::snprintf(line, sizeof(line), "width %u: %zu tiles on %u CTAs, model schedule %.3f ms", W,
                     p->tiles.size(), p->ctas, ms_model);
       report += line;
-      if (ms_model < best.ms) best = {ms_model, W, p->tiles, p->order, p->begin, p->ctas, "model"};
+      if (ms_model < best.ms) best = {ms_model, W, false, p->tiles, p->order, p->begin, p->ctas, "model"};
       // schedule from the measured tile times
       std::vector<double> cost(ns.begin(), ns.end());
       double mk = 0.0;
@@ -1001,13 +1142,25 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
       if ((rc = timed(ms_meas))) break;
       std::snprintf(line, sizeof(line), ", measured schedule %.3f ms\n", ms_meas);
       report += line;
-      if (ms_meas < best.ms) best = {ms_meas, W, p->tiles, p->order, p->begin, p->ctas, "measured"};
+      if (ms_meas < best.ms) best = {ms_meas, W, false, p->tiles, p->order, p->begin, p->ctas, "measured"};
+    }
+    if (rc) break;
+    for (uint32_t W : {16u, 32u, 64u}) {  // tiles split over CTA pairs, where they fit
+      if (!pairing_fits(p, W)) continue;
+      build_tiles(p, W, true);
+      float ms_pair = 0.f;
+      if ((rc = timed(ms_pair))) break;
+      std::snprintf(line, sizeof(line), "width %u paired: %zu tile parts on %u CTAs, %.3f ms\n", W, p->tiles.size(),
+                    p->ctas, ms_pair);
+      report += line;
+      if (ms_pair < best.ms) best = {ms_pair, W, true, p->tiles, p->order, p->begin, p->ctas, "paired"};
     }
   } while (false);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
   p->width = best.width;
+  p->paired = best.paired;
   p->tiles = best.tiles;
   p->order = best.order;
   p->begin = best.begin;
@@ -1022,8 +1175,8 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
 
 std::string describe(const Batch* p) {
   char buf[256];
-  std::snprintf(buf, sizeof(buf), "tile width %u, %zu tiles, %u CTAs, %s schedule", p->width, p->tiles.size(),
-                p->ctas, p->sched_source.c_str());
+  std::snprintf(buf, sizeof(buf), "tile width %u%s, %zu tiles, %u CTAs, %s schedule", p->width,
+                p->paired ? " (each tile on a CTA pair)" : "", p->tiles.size(), p->ctas, p->sched_source.c_str());
   return buf;
 }
 
@@ -1036,7 +1189,8 @@ void destroy(Batch* p) {
     if (in.Ar) cudaFree((void*)in.Ar);
     if (in.alpha_r) cudaFree((void*)in.alpha_r);
   }
-  void* bufs[] = {p->d_inst, p->d_tiles, p->d_order, p->d_begin, p->bvt, p->bst, p->error, p->tile_ns};
+  void* bufs[] = {p->d_inst,  p->d_tiles, p->d_order,   p->d_begin,    p->bvt,
+                  p->bst,     p->error,   p->tile_ns,   p->pair_sync,  p->pair_colmax};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete p;

@@ -40,9 +40,15 @@ int check(Batch* p, cudaStream_t s);
 // FP64 copy of instance i's states (device buffers kv x M and ks x M, LayoutLeft).
 int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs);
 // Autotuner: times every tile width in {16, 32, 64} with a model-cost LPT schedule and a
-// schedule rebuilt from the measured per-tile times, keeps the fastest, and leaves all
-// states reset to zero.  `report` receives one line per candidate.
-int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report);
+// schedule rebuilt from the measured per-tile times, and every width whose tiles fit
+// the SMs twice over split across CTA pairs; keeps the fastest and leaves all states
+// reset to zero.  `report` receives one line per candidate, `launches` the number of
+// kernel launches made.
+int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, std::string& report,
+         unsigned long long& launches);
+// Fixed tiling: tiles of `width` forcing columns (16, 32 or 64), optionally each split
+// across two co-resident CTAs (SHAW_ERR_UNSUPPORTED where the pairs do not fit).
+int set_tiling(Batch* p, uint32_t width, bool paired);
 // The current tiling in words (width, tiles, CTAs, schedule source).
 std::string describe(const Batch* p);
 uint32_t num_ctas(const Batch* p);

@@ -169,3 +169,49 @@ def test_batch_seismograms(shaw):
         assert np.max(np.abs(single)) > 0
         assert relerr(seis[shaw.FP64][i], single) <= 1e-14
         assert relerr(seis[shaw.MIXED_OZAKI_BF16][i], single) <= 1e-8
+
+
+def test_batch_ozaki_paired_tiles_bitwise(shaw):
+    """Tiles split across CTA pairs (each CTA half of the 128-row blocks, shared slices,
+    a step barrier) give the same numbers as whole tiles: states, snapshots and
+    seismograms bit for bit, also when advanced in pieces and with an odd number of
+    row blocks (384 modes) or a part without receiver rows (3 receivers)."""
+    insts = _instances(9, shapes=[(384, 256, 100), (512, 512, 33), (256, 384, 20)])
+    n, dt = 60, 0.5
+    rng = np.random.default_rng(10)
+    rows = [rng.standard_normal((R, d["rom_jvp"].shape[0])) for R, d in zip((130, 3, 7), insts)]
+    out = {}
+    for paired in (False, True):
+        bt = shaw.RomBatch(insts, precision=shaw.MIXED_OZAKI_BF16)
+        bt.set_tiling(16, paired=paired)
+        assert ("pair" in bt.describe()) == paired
+        for i in range(len(insts)):
+            bt.set_snapshots(i, 7, 5, n)
+            bt.set_receivers(i, rows[i], 3, n)
+        bt.advance(dt, 25)
+        bt.advance(dt, n - 25)
+        bt.synchronize()
+        out[paired] = [(bt.get_state(i), bt.snapshots(i), bt.seismogram(i)) for i in range(len(insts))]
+        bt.close()
+    for i in range(len(insts)):
+        (xa, sa, ga), (xb, sb, gb) = out[False][i], out[True][i]
+        for u, v in zip(xa + sa + (ga,), xb + sb + (gb,)):
+            assert np.array_equal(u, v), i
+        assert np.max(np.abs(ga)) > 0
+
+
+def test_batch_tiling_errors(shaw):
+    small = _instances(11, shapes=[(128, 256, 40)])
+    bt = shaw.RomBatch(small, precision=shaw.MIXED_OZAKI_BF16)
+    with pytest.raises(shaw.ShawError) as e:
+        bt.set_tiling(32, paired=True)  # one 128-row block per velocity phase: nothing to split
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    with pytest.raises(shaw.ShawError) as e:
+        bt.set_tiling(48)
+    assert e.value.code == shaw.ERR_INVALID_ARG
+    bt.close()
+    bt = shaw.RomBatch(small, precision=shaw.FP64)
+    with pytest.raises(shaw.ShawError) as e:
+        bt.set_tiling(32)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    bt.close()
