@@ -70,9 +70,10 @@ constexpr uint32_t kABytes = kSlices * kATile;
 constexpr uint32_t kMaxNb = 64;
 constexpr uint32_t kStageBytes = kABytes + kSlices * kMaxNb * kRowBytes;  // 72 KB
 constexpr int kStages = 3;
-constexpr uint32_t kTmemCols = 512;           // two accumulator sets at columns 0 and 256 when 6 nb <= 256
+// TMEM: two accumulator sets at columns 0 and 256 when 6 nb <= 256; otherwise one set at
+// column 0 and the staging of its combined values at column 6 nb
+constexpr uint32_t kTmemCols = 512;
 
-__host__ __device__ constexpr uint32_t btile_bytes(uint32_t nb) { return nb * kRowBytes; }
 __host__ __device__ constexpr uint32_t bstage_bytes(uint32_t nb) { return kSlices * nb * kRowBytes; }
 __host__ __device__ constexpr uint32_t acc_buffers(uint32_t nb) { return (kDiags * nb <= 256) ? 2u : 1u; }
 
@@ -80,6 +81,26 @@ __host__ __device__ constexpr uint32_t acc_buffers(uint32_t nb) { return (kDiags
 // core matrices of 8 rows x 16 bytes, K-direction stride 128 B, 8-row-group stride 512 B.
 __host__ __device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k) {
   return (((r >> 3) * 4u + (k >> 3)) << 7) + ((r & 7u) << 4) + ((k & 7u) << 1);
+}
+
+// Byte offset of (slice s, column j, K-row k) in one pipeline stage of state slices (the
+// B operand, MN-major, no swizzle): the 6 slices are stacked along N (n = s*nb + j); a
+// core matrix is 8 K-rows x 16 bytes (8 consecutive n); N-direction stride 128 B,
+// K-direction stride 96*nb B (all 6*nb columns of one 8-row K group).  Eight
+// consecutive columns of one row are 16 contiguous bytes.
+__host__ __device__ __forceinline__ uint32_t bslice_off(uint32_t nb, uint32_t s, uint32_t j, uint32_t k) {
+  const uint32_t n = s * nb + j;
+  return (k >> 3) * (96u * nb) + ((n >> 3) << 7) + ((k & 7u) << 4) + ((n & 7u) << 1);
+}
+
+// Global stores as inline PTX without a memory clobber: the epilogue's stores go to
+// global memory only, so shared-memory values read around them need no reload.
+__device__ __forceinline__ void st_f32(float* p, float v) { asm volatile("st.global.f32 [%0], %1;" ::"l"(p), "f"(v)); }
+__device__ __forceinline__ void st_f64(double* p, double v) {
+  asm volatile("st.global.f64 [%0], %1;" ::"l"(p), "d"(v));
+}
+__device__ __forceinline__ void st_v4(void* p, const uint32_t (&w)[4]) {
+  asm volatile("st.global.v4.b32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]));
 }
 
 // One reduced system on the device.
@@ -163,6 +184,9 @@ __device__ __forceinline__ void acc_next(uint32_t nbuf, uint32_t (&uses)[2], uin
   uses[buf]++;
 }
 
+// Instruction-descriptor bit: B operand MN-major ("transpose B").
+constexpr uint32_t kIdescBMnMajor = 1u << 16;
+
 // One GEMM phase: for every 128-row M-tile, D_d = sum over K of the slice pairs on
 // diagonal d into an accumulator set; the epilogue `epi(mt, tmem_cols)` runs on warps
 // 4..11 while the MMAs of the next M-tile fill the other set.
@@ -171,7 +195,7 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
                                            uint32_t mt0, uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
                                            uint32_t (&uses)[2], unsigned int* err, Epi epi) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb), nbuf = acc_buffers(nb);
+  const uint32_t bbytes = bstage_bytes(nb), nbuf = acc_buffers(nb);
   if (warp == 0 && lane == 0) {
     for (uint32_t q = 0; q < n_mt * n_kc && !sh->abort; ++q) {
       const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
@@ -199,7 +223,7 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
         // descriptors of the stage's first A / B slice; the others differ only in the
         // start-address field (16-byte units, no carry: shared addresses < 256 KB)
         const uint64_t adesc0 = smem_desc(abase, 128, 512);
-        const uint64_t bdesc0 = smem_desc(abase + kABytes, 128, 512);
+        const uint64_t bdesc0 = smem_desc(abase + kABytes, 96u * nb, 128);  // MN-major state slices
         // The B slices of a stage are stacked along N (slice t = rows t*nb ..), and the
         // diagonal accumulators along TMEM columns (diagonal d = columns d*nb ..), so
         // operator slice sa times the state slices tb = 0 .. 5-sa is ONE MMA of
@@ -216,8 +240,8 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
             uint32_t tb = 0, left = (uint32_t)(kSlices - sa);
             while (left) {
               const uint32_t take = min(left, 256u / nb);
-              const uint64_t bdesc = bdesc0 + ((tb * btile + k * 256) >> 4);
-              mma_f16(dcol + (sa + tb) * nb, adesc, bdesc, idesc_bf16(take * nb), acc);
+              const uint64_t bdesc = bdesc0 + ((tb * 16u * nb + k * 192u * nb) >> 4);
+              mma_f16(dcol + (sa + tb) * nb, adesc, bdesc, idesc_bf16(take * nb) | kIdescBMnMajor, acc);
               tb += take;
               left -= take;
             }
@@ -234,9 +258,12 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
       acc_next(nbuf, lu, buf, par);
       if (!mbar_wait(&sh->acc_full[buf], par)) { raise(sh, err, 8u); break; }
       tc_fence_after();
-      if (!sh->abort) epi(mt0 + mt, sh->tmem + buf * 256u);
-      tc_fence_before();
-      mbar_arrive(&sh->acc_empty[buf]);
+      // the epilogue may hand the accumulator back early (returns true once it has)
+      const bool released = !sh->abort && epi(mt0 + mt, sh->tmem + buf * 256u, &sh->acc_empty[buf]);
+      if (!released) {
+        tc_fence_before();
+        mbar_arrive(&sh->acc_empty[buf]);
+      }
     }
   }
   // every thread advances the counters the same way
@@ -281,13 +308,43 @@ __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q
   }
 }
 
+// With a single accumulator set (6 nb > 256, i.e. nb = 64) the TMEM columns after it,
+// [6 nb, 8 nb), stage the combined values of one M-tile: the epilogue drains the
+// accumulator into them (hi at +j, lo at +nb+j), hands it back to the MMA issuer, and
+// finishes the state update while the next M-tile's MMAs run.
+__device__ __forceinline__ bool stage_accumulator(uint32_t tcols, uint32_t spare, uint32_t nb, int q, uint32_t jbeg,
+                                                  uint32_t jend, uint64_t* acc_empty) {
+  for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+    float yh[8], yl[8];
+    load_combine8(tcols, nb, q, j0, yh, yl);
+    tmem_st8(spare + j0, yh);
+    tmem_st8(spare + nb + j0, yl);
+  }
+  tmem_wait_st();
+  tc_fence_before();
+  mbar_arrive(acc_empty);
+  return true;
+}
+
+// Combined values of 8 columns: from the accumulator, or from the staging columns.
+__device__ __forceinline__ void fetch_combined8(bool staged, uint32_t tcols, uint32_t spare, uint32_t nb, int q,
+                                                uint32_t j0, float* yh, float* yl) {
+  if (staged) {
+    tmem_ld8(spare + j0, yh);
+    tmem_ld8(spare + nb + j0, yl);
+    tmem_wait_ld();
+  } else {
+    load_combine8(tcols, nb, q, j0, yh, yl);
+  }
+}
+
 // Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
 // into the BF16 B tiles with per-column exponents beta[j] (|x| < 2^beta).
 __device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t nb,
                                             const int* beta, uint8_t* tiles, unsigned long long mask, uint32_t r0,
                                             uint32_t r1) {
   const uint32_t t = threadIdx.x - 128;
-  const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);
+  const uint32_t bbytes = bstage_bytes(nb);
   const uint32_t nr = r1 - r0, n = nr * nb;
   for (uint32_t e0 = t; e0 < n; e0 += 4 * kEpiThreads) {
     float vh[4], vl[4];
@@ -307,33 +364,44 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
       if (e0 + u * kEpiThreads >= n) break;
       if (!((mask >> jj[u]) & 1ull)) continue;
       float h = ldexpf(vh[u], -beta[jj[u]]), l = ldexpf(vl[u], -beta[jj[u]]);
-      uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + tile_off(jj[u], rr[u] % kKc);
+      uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + bslice_off(nb, 0, jj[u], rr[u] % kKc);
 #pragma unroll
       for (int s = 0; s < kSlices; ++s) {
         const float th = h * 64.f, tl = l * 64.f;
         float a = rintf(th);
         a = fminf(64.f, fmaxf(-64.f, a));
         two_sum(th - a, tl, h, l);
-        *reinterpret_cast<__nv_bfloat16*>(base + s * btile) = __float2bfloat16_rn(a);
+        *reinterpret_cast<__nv_bfloat16*>(base + s * 16u * nb) = __float2bfloat16_rn(a);
       }
     }
   }
 }
 
-// Slice one state value (row, column j) into the B tiles with exponent beta (the
-// stacked-slice layout of slice_state).  Values at or above 2^beta are clamped; the
-// caller detects that from the column maximum and re-slices exactly.
-__device__ __forceinline__ void slice_value(float xh, float xl, int beta, uint32_t row, uint32_t j, uint32_t bbytes,
-                                            uint32_t btile, uint8_t* tiles) {
-  float h = ldexpf(xh, -beta), l = ldexpf(xl, -beta);
-  uint8_t* base = tiles + (size_t)(row / kKc) * bbytes + tile_off(j, row % kKc);
+// Slice 8 state values of one row (columns j0 .. j0+7) into the B tiles with exponents
+// e[jj] (the layout of slice_state): per slice one 16-byte store at dst + s*16*nb, dst =
+// the (row, j0) byte of slice 0.  Values at or above 2^e are clamped; the caller
+// detects that from the column maximum and re-slices exactly.
+__device__ __forceinline__ void slice_value8(const float* xh, const float* xl, const int* e, uint8_t* dst,
+                                             uint32_t nb) {
+  float h[8], l[8];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    h[jj] = ldexpf(xh[jj], -e[jj]);
+    l[jj] = ldexpf(xl[jj], -e[jj]);
+  }
 #pragma unroll
   for (int s = 0; s < kSlices; ++s) {
-    const float th = h * 64.f, tl = l * 64.f;
-    float a = rintf(th);
-    a = fminf(64.f, fmaxf(-64.f, a));
-    two_sum(th - a, tl, h, l);
-    *reinterpret_cast<__nv_bfloat16*>(base + s * btile) = __float2bfloat16_rn(a);
+    uint32_t w[4];
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      const float th = h[jj] * 64.f, tl = l[jj] * 64.f;
+      float a = rintf(th);
+      a = fminf(64.f, fmaxf(-64.f, a));
+      two_sum(th - a, tl, h[jj], l[jj]);
+      const uint32_t bits = __bfloat16_as_ushort(__float2bfloat16_rn(a));
+      w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
+    }
+    st_v4(dst + s * 16u * nb, w);
   }
 }
 
@@ -468,7 +536,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const bool paired = (sh->tile.pinfo & 2u) != 0u;
     const uint32_t part = sh->tile.pinfo & 1u, slot = sh->tile.pinfo >> 2;
     const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
-    const uint32_t bbytes = bstage_bytes(nb), btile = btile_bytes(nb);             // B-tile geometry
+    const uint32_t bbytes = bstage_bytes(nb);                                      // B stage bytes
+    const bool stage = acc_buffers(nb) == 1;  // single accumulator set: stage it in TMEM
+    const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + kDiags * nb;
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
     float* const xvh = in.xvh + (size_t)col0 * in.kvp;
     float* const xvl = in.xvl + (size_t)col0 * in.kvp;
@@ -557,11 +627,15 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
       const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
       // ---------------- velocity: XV += dt Av XS + fdt b ----------------
-      gemm_phase(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+      gemm_phase(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
+                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row];
+        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off(nb, 0, 0, row % kKc);
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
           float ph[8], pl[8], qh[8], ql[8];
+          int pe[8];
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
             const size_t si = (size_t)(j0 + jj) * in.kvp + row;
@@ -571,7 +645,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             ql[jj] = bl[si];
           }
           float yh[8], yl[8];
-          load_combine8(tcols, nb, q, j0, yh, yl);
+          fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
@@ -582,16 +656,21 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             pow2_pair(e, s1, s2);
             df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
             df_fma(xh, xl, sh->fdt_h[j], sh->fdt_l[j], qh[jj], ql[jj]);
-            xvh[si] = xh;
-            xvl[si] = xl;
+            st_f32(xvh + si, xh);
+            st_f32(xvl + si, xl);
             ph[jj] = xh;
+            pl[jj] = xl;
+            // a column without a prediction is sliced with any exponent: it is re-sliced
+            // exactly after the phase
             const int pv = sh->pred_v[j];
-            if (pv != kNoPrediction) slice_value(xh, xl, pv, row, j, bbytes, btile, bvt);
+            pe[jj] = pv != kNoPrediction ? pv : 0;
             if (snap_v && row < in.kv && col < in.M)
-              in.snap_vp[row + (size_t)in.kv * (tv + in.Tvp * col)] = (double)xh + (double)xl;
+              st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), (double)xh + (double)xl);
           }
+          slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
           note_max8(sh, j0, ph);
         }
+        return staged;
       });
       if (paired) exchange();
       if (ew >= 0) {
@@ -612,7 +691,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       if (in.seis && in.fseis && n % in.fseis == 0) {
         const unsigned long long tcnt = n / in.fseis - 1;
         gemm_phase(stages, sh, in.Ar, bvt, mr0, mr1 - mr0, n_kc_s, nb, it, uses, a.error,
-                   [&](uint32_t mt, uint32_t tcols) {
+                   [&](uint32_t mt, uint32_t tcols, uint64_t*) {
                      const uint32_t r = mt * 128 + q * 32 + lane;
                      const int alpha = in.alpha_r[r];
                      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
@@ -622,19 +701,24 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
                        for (int jj = 0; jj < 8; ++jj) {
                          const uint32_t col = col0 + j0 + jj;
                          if (r < in.R && col < in.M)
-                           in.seis[r + (size_t)in.R * (tcnt + in.Tseis * col)] =
-                               ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]);
+                           st_f64(in.seis + r + (size_t)in.R * (tcnt + in.Tseis * col),
+                                  ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]));
                        }
                      }
+                     return false;
                    });
         if (__syncthreads_or(sh->abort != 0)) break;
       }
       // ---------------- stress: XS += dt As XV ----------------
-      gemm_phase(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error, [&](uint32_t mt, uint32_t tcols) {
+      gemm_phase(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
+                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row];
+        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off(nb, 0, 0, row % kKc);
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
           float ph[8], pl[8];
+          int pe[8];
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const size_t si = (size_t)(j0 + jj) * in.ksp + row;
@@ -642,7 +726,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             pl[jj] = xsl[si];
           }
           float yh[8], yl[8];
-          load_combine8(tcols, nb, q, j0, yh, yl);
+          fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
@@ -652,16 +736,19 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             float s1, s2;
             pow2_pair(e, s1, s2);
             df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-            xsh[si] = xh;
-            xsl[si] = xl;
+            st_f32(xsh + si, xh);
+            st_f32(xsl + si, xl);
             ph[jj] = xh;
+            pl[jj] = xl;
             const int ps = sh->pred_s[j];
-            if (ps != kNoPrediction) slice_value(xh, xl, ps, row, j, bbytes, btile, bst);
+            pe[jj] = ps != kNoPrediction ? ps : 0;
             if (snap_s && row < in.ks && col < in.M)
-              in.snap_sp[row + (size_t)in.ks * (ts + in.Tsp * col)] = (double)xh + (double)xl;
+              st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), (double)xh + (double)xl);
           }
+          slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
           note_max8(sh, j0, ph);
         }
+        return staged;
       });
       if (paired) exchange();
       if (ew >= 0) {
