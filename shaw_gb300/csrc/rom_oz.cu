@@ -379,15 +379,22 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
 
 // Slice 8 state values of one row (columns j0 .. j0+7) into the B tiles with exponents
 // e[jj] (the layout of slice_state): per slice one 16-byte store at dst + s*16*nb, dst =
-// the (row, j0) byte of slice 0.  Values at or above 2^e are clamped; the caller
-// detects that from the column maximum and re-slices exactly.
+// the (row, j0) byte of slice 0.  A value at or above 2^e gives meaningless slices (no
+// clamp): the caller detects it from the column maximum and re-slices that column
+// exactly.  Below 2^e the first slice is in [-64, 64] and every slice is exact in BF16.
 __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, const int* e, uint8_t* dst,
                                              uint32_t nb) {
   float h[8], l[8];
 #pragma unroll
   for (int jj = 0; jj < 8; ++jj) {
-    h[jj] = ldexpf(xh[jj], -e[jj]);
-    l[jj] = ldexpf(xl[jj], -e[jj]);
+    if (e[jj] >= -126 && e[jj] <= 126) {  // 2^-e is a normal FP32: one exact (or once-rounded) product
+      const float f = __int_as_float((127 - e[jj]) << 23);
+      h[jj] = xh[jj] * f;
+      l[jj] = xl[jj] * f;
+    } else {
+      h[jj] = ldexpf(xh[jj], -e[jj]);
+      l[jj] = ldexpf(xl[jj], -e[jj]);
+    }
   }
 #pragma unroll
   for (int s = 0; s < kSlices; ++s) {
@@ -395,8 +402,7 @@ __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, c
 #pragma unroll
     for (int jj = 0; jj < 8; ++jj) {
       const float th = h[jj] * 64.f, tl = l[jj] * 64.f;
-      float a = rintf(th);
-      a = fminf(64.f, fmaxf(-64.f, a));
+      const float a = rintf(th);
       two_sum(th - a, tl, h[jj], l[jj]);
       const uint32_t bits = __bfloat16_as_ushort(__float2bfloat16_rn(a));
       w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
