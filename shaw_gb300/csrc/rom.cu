@@ -108,11 +108,17 @@ struct RomArgs {
 };
 
 // Dynamic shared memory of the rank-1 kernel, in elements of T (double or df):
-//   xv_full[kv] | xs_full[ks] | Av rows [rows_v x ks] | As rows [rows_s x kv] | b rows [rows_v]
+//   xv_full[2][kv] (alternating by step) | xs_full[ks] | Av rows [rows_v x ks] |
+//   As rows [rows_s x kv] | b rows [rows_v]
 template <typename T>
 size_t rank1_smem_bytes(uint32_t kv, uint32_t ks, uint32_t rv, uint32_t rs) {
-  return sizeof(T) * ((size_t)kv + ks + (size_t)rv * ks + (size_t)rs * kv + rv);
+  return sizeof(T) * (2 * (size_t)kv + ks + (size_t)rv * ks + (size_t)rs * kv + rv);
 }
+
+// The two halves of a cluster barrier (release on arrival, acquire on the wait), so that
+// work that touches no exchanged row can run in between.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -172,8 +178,11 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   const uint32_t crank = cluster.block_rank();
   const uint32_t csize = cluster.num_blocks();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* xv = reinterpret_cast<T*>(smem_raw);
-  T* xs = xv + a.kv;
+  // XV alternates between two full copies: step it reads copy it % 2 and writes its new
+  // rows into copy (it + 1) % 2 of every CTA, so the seismogram of a step can read its
+  // copy while other CTAs already write the next one
+  T* const xvb = reinterpret_cast<T*>(smem_raw);
+  T* xs = xvb + 2 * (size_t)a.kv;
   T* Av = xs + a.ks;
   T* As = Av + (size_t)a.rows_v * a.ks;
   T* bv = As + (size_t)a.rows_s * a.kv;
@@ -182,7 +191,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   const uint32_t s0 = min(a.ks, crank * a.rows_s), s1 = min(a.ks, s0 + a.rows_s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  for (uint32_t k = threadIdx.x; k < a.kv; k += kR1Threads) xv[k] = A::load(a.xv[k]);
+  for (uint32_t k = threadIdx.x; k < a.kv; k += kR1Threads) xvb[k] = A::load(a.xv[k]);
   for (uint32_t k = threadIdx.x; k < a.ks; k += kR1Threads) xs[k] = A::load(a.xs[k]);
   for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kR1Threads)
     Av[e] = A::load(a.Av[(size_t)v0 * a.ks + e]);
@@ -200,13 +209,13 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
     // sample steps of the observers, decided once per step
     const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
     const bool seis_now = a.fseis && n % a.fseis == 0;
+    const T* const xcur = xvb + (size_t)(it & 1) * a.kv;
+    T* const xv = xvb + (size_t)((it + 1) & 1) * a.kv;  // the new velocity state
     // 1. velocity rows of this CTA
     for (uint32_t r = v0 + warp; r < v1; r += kR1Warps) {
       const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
-      const T xold = xv[r];
-      __syncwarp();  // every lane has read the old row before one of them overwrites the local copy
       if (lane < (int)csize) {
-        T x = A::update(xold, y, dtT);
+        T x = A::update(xcur[r], y, dtT);
         x = A::axpy(x, fdt, bv[r - v0]);
         T* dst = cluster.map_shared_rank(xv + r, lane);
         *dst = x;
@@ -214,16 +223,8 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
           a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
       }
     }
-    cluster.sync();
-    // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185)
-    if (seis_now) {
-      for (uint32_t r = crank * kR1Warps + warp; r < a.R; r += csize * kR1Warps) {
-        // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
-        const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
-        const T s = A::dot(prow, xv, a.kv, lane);
-        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = A::value(s);
-      }
-    }
+    cluster_arrive();
+    cluster_wait();
     // 2. stress rows of this CTA
     for (uint32_t r = s0 + warp; r < s1; r += kR1Warps) {
       const T y = A::dot(As + (size_t)(r - s0) * a.kv, xv, a.kv, lane);
@@ -237,9 +238,23 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
           a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
       }
     }
-    cluster.sync();
+    cluster_arrive();
+    // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185),
+    // inside the barrier: it reads only this step's XV copy, which nobody writes until
+    // every CTA has arrived here
+    if (seis_now) {
+      // receiver r on CTA r % csize: the rows spread evenly over the cluster
+      for (uint32_t r = crank + csize * warp; r < a.R; r += csize * kR1Warps) {
+        // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
+        const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
+        const T s = A::dot(prow, xv, a.kv, lane);
+        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = A::value(s);
+      }
+    }
+    cluster_wait();
   }
-  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) a.xv[r] = A::value(xv[r]);
+  const T* const xfin = xvb + (size_t)(a.nsteps & 1) * a.kv;
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) a.xv[r] = A::value(xfin[r]);
   for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xs[r]);
 }
 
