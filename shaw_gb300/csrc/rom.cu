@@ -92,7 +92,7 @@ struct RomArgs {
   const double* b;    // kv (rank-1 forcing vector)
   double* xv;         // kv  (initial state in, final state out)
   double* xs;         // ks
-  const double* fdt;  // [nsteps]: f(t_{n-1}) * dt of the launch's steps
+  const void* fdt_t;  // [nsteps]: f(t_{n-1}) * dt of the launch's steps, as the kernel's element type
   double dt;
   uint32_t kv, ks, rows_v, rows_s;  // rows per CTA
   unsigned long long step0, nsteps;
@@ -151,6 +151,8 @@ struct Arith<false> {
   // x + dt*y, then + fdt*b when b != null: KokkosBlas::gemv then axpy roundings
   __device__ static T update(T x, T y, T dt) { return __dadd_rn(x, __dmul_rn(dt, y)); }
   __device__ static T axpy(T x, T a, T b) { return __dadd_rn(x, __dmul_rn(a, b)); }
+  // an output sample (seismogram): the value itself
+  __device__ static void store_sample(double* p, T x) { *p = x; }
 };
 
 template <>
@@ -167,6 +169,9 @@ struct Arith<true> {
   // dt and a arrive already split (once per launch / per step, not per row)
   __device__ static T update(T x, T y, T dt) { return df_add(x, df_mul(dt, y)); }
   __device__ static T axpy(T x, T a, T b) { return df_add(x, df_mul(a, b)); }
+  // an output sample: the FP32 pair in the double's 8 bytes, widened to FP64 after the
+  // launch (rom_samples_to_fp64_kernel), so the time loop issues no FP64 instruction
+  __device__ static void store_sample(double* p, T x) { *reinterpret_cast<df*>(p) = x; }
 };
 
 // One persistent launch for nsteps ROM rank-1 leapfrog steps (one cluster).
@@ -205,7 +210,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
     const unsigned long long n = a.step0 + it + 1;
     // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt, from the table filled before the launch
     // (RankOneForcing keeps the whole signal time series too: forcing_rank_one.hpp:169-178)
-    const T fdt = A::load(a.fdt[it]);
+    const T fdt = static_cast<const T*>(a.fdt_t)[it];
     // sample steps of the observers, decided once per step
     const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
     const bool seis_now = a.fseis && n % a.fseis == 0;
@@ -248,7 +253,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
         // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
         const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
         const T s = A::dot(prow, xv, a.kv, lane);
-        if (lane == 0) a.seis[r + (size_t)a.R * (n / a.fseis - 1)] = A::value(s);
+        if (lane == 0) A::store_sample(a.seis + r + (size_t)a.R * (n / a.fseis - 1), s);
       }
     }
     cluster_wait();
@@ -258,9 +263,21 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xs[r]);
 }
 
+// FP64 -> FP32 hi + lo; in and out may be the same array (each element is read before
+// it is overwritten, by the same thread).
 __global__ void rom_split_df_kernel(const double* in, df* out, size_t n) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
-    out[e] = df_split(in[e]);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double v = in[e];
+    out[e] = df_split(v);
+  }
+}
+
+// Samples stored as FP32 hi + lo pairs in place of doubles -> FP64, in place.
+__global__ void rom_samples_to_fp64_kernel(double* p, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const df v = *reinterpret_cast<const df*>(p + e);
+    p[e] = df_val(v);
+  }
 }
 
 // table[s] = f(t) * dt at t = (step0 + s) * dt: the forcing of step step0 + s + 1.
@@ -378,7 +395,13 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
       h->h_kind[0], h->h_delay[0], h->h_period[0], dt, h->step, nsteps, h->fdt);
   h->launches++;
   SHAW_CUDA(cudaGetLastError());
-  a.fdt = h->fdt; a.dt = dt;
+  if (MIXED) {  // the forcing table as FP32 hi + lo, in place
+    rom_split_df_kernel<<<(unsigned)((nsteps + 255) / 256), 256, 0, h->stream>>>(h->fdt, reinterpret_cast<df*>(h->fdt),
+                                                                                  nsteps);
+    h->launches++;
+    SHAW_CUDA(cudaGetLastError());
+  }
+  a.fdt_t = h->fdt; a.dt = dt;
   a.kv = (uint32_t)h->kv; a.ks = (uint32_t)h->ks; a.rows_v = h->rows_v; a.rows_s = h->rows_s;
   a.step0 = h->step; a.nsteps = nsteps;
   a.fvp = (uint32_t)h->fvp; a.fsp = (uint32_t)h->fsp; a.snap_vp = h->snap_vp; a.snap_sp = h->snap_sp;
@@ -402,6 +425,16 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   cfg.numAttrs = 1;
   SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
   h->launches++;
+  if (MIXED && h->seis && h->fseis) {  // this launch's seismogram samples -> FP64
+    const uint64_t t0 = h->step / h->fseis, t1 = (h->step + nsteps) / h->fseis;
+    if (t1 > t0) {
+      const size_t cnt = (size_t)h->R * (t1 - t0);
+      rom_samples_to_fp64_kernel<<<(unsigned)std::min<size_t>((cnt + 255) / 256, 1024), 256, 0, h->stream>>>(
+          h->seis + (size_t)h->R * t0, cnt);
+      h->launches++;
+      SHAW_CUDA(cudaGetLastError());
+    }
+  }
   return SHAW_OK;
 }
 

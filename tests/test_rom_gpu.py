@@ -121,6 +121,29 @@ def test_rank1_advance_in_pieces(shaw, setup):
     assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_rank1_seismogram_in_pieces(shaw, prec):
+    """Seismogram samples (every 3 steps) of a run advanced in uneven pieces equal those
+    of one uninterrupted run bit for bit, in both precisions (the mixed form widens each
+    launch's samples to FP64 after the launch)."""
+    k, n = 96, 300
+    av, as_, b = stable_system(k, 12)
+    rows = np.random.default_rng(13).standard_normal((9, k)) / np.sqrt(k)
+    p = shaw.FP64 if prec == "fp64" else shaw.MIXED_FP32
+    r = shaw.Rom(av * 0.5, as_ * 0.5, b, rank=1, precision=p)
+    r.set_signals("gaussDer", 40.0, 30.0)
+    r.set_receivers(rows, 3, n)
+    r.run(0.5, n)
+    whole = r.seismogram().copy()
+    r.reset()
+    for m in (1, 98, 2, 199):
+        r.advance(0.5, m)
+    r.synchronize()
+    assert np.max(np.abs(whole)) > 0
+    assert np.array_equal(r.seismogram(), whole)
+    r.close()
+
+
 @pytest.mark.parametrize("M", [1, 5, 16])
 def test_rank2_fp64_matches_oracle(shaw, oracle, setup, M):
     rng = np.random.default_rng(M)
