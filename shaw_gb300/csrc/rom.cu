@@ -9,8 +9,9 @@
 // bound.  It runs as ONE persistent launch on a thread-block cluster: each CTA
 // keeps its slice of operator rows in shared memory and a full copy of both
 // reduced states; after each half-step every CTA pushes its new rows into all
-// CTAs' copies through distributed shared memory and the cluster barrier
-// (barrier.cluster, hardware) orders the exchange.  Two arithmetics:
+// CTAs' copies of the next state with asynchronous distributed-shared-memory stores
+// that complete on the receiving CTA's mbarrier (st.async ... complete_tx), and each
+// CTA waits (bounded) on its own mbarrier for the full vector.  Two arithmetics:
 //   SHAW_FP64        FP64 products and state (the oracle-parity path);
 //   SHAW_MIXED_FP32  "double-float": operators and states split into FP32 hi+lo,
 //                    error-free products (FMA) with compensated FP32 sums
@@ -105,20 +106,59 @@ struct RomArgs {
   const void* phi_rcv_t;  // the same rows as the kernel's element type (double, or df for the mixed form)
   double* seis;           // R x Tseis
   unsigned long long Tseis;
+  unsigned int* error;    // set when an exchange wait runs out
 };
 
 // Dynamic shared memory of the rank-1 kernel, in elements of T (double or df):
-//   xv_full[2][kv] (alternating by step) | xs_full[ks] | Av rows [rows_v x ks] |
+//   xv_full[2][kv] | xs_full[2][ks] (both alternating by step) | Av rows [rows_v x ks] |
 //   As rows [rows_s x kv] | b rows [rows_v]
 template <typename T>
 size_t rank1_smem_bytes(uint32_t kv, uint32_t ks, uint32_t rv, uint32_t rs) {
-  return sizeof(T) * (2 * (size_t)kv + ks + (size_t)rv * ks + (size_t)rs * kv + rv);
+  return sizeof(T) * (2 * (size_t)kv + 2 * (size_t)ks + (size_t)rv * ks + (size_t)rs * kv + rv);
 }
 
-// The two halves of a cluster barrier (release on arrival, acquire on the wait), so that
-// work that touches no exchanged row can run in between.
-__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
-__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+// ---- cluster exchange: st.async into the peers' shared memory, completing on their mbarrier
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t peer_addr(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_async8(uint32_t raddr, uint64_t v, uint32_t rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(raddr), "l"(v),
+               "r"(rbar)
+               : "memory");
+}
+__device__ __forceinline__ void xbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)));
+}
+// this CTA's single arrival of the phase, announcing the bytes the peers will deliver
+__device__ __forceinline__ void xbar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase with the given parity (acquire at cluster scope: the
+// peers' stores are visible afterwards).  False when the limit ran out.
+__device__ __forceinline__ bool xbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (unsigned long long i = 0; i < (1ull << 24); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+template <typename T>
+__device__ __forceinline__ uint64_t bits8(T x) {
+  static_assert(sizeof(T) == 8, "8-byte state elements");
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return u;
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -183,12 +223,15 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   const uint32_t crank = cluster.block_rank();
   const uint32_t csize = cluster.num_blocks();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // XV alternates between two full copies: step it reads copy it % 2 and writes its new
-  // rows into copy (it + 1) % 2 of every CTA, so the seismogram of a step can read its
-  // copy while other CTAs already write the next one
+  // Both states alternate between two full copies: step it reads copy it % 2 and writes
+  // its new rows into copy (it + 1) % 2 of every CTA.  A CTA reaches the step that
+  // overwrites a copy only after every peer has sent the rows of the step in between,
+  // i.e. after every peer has finished reading that copy.
   T* const xvb = reinterpret_cast<T*>(smem_raw);
-  T* xs = xvb + 2 * (size_t)a.kv;
-  T* Av = xs + a.ks;
+  T* const xsb = xvb + 2 * (size_t)a.kv;
+  T* Av = xsb + 2 * (size_t)a.ks;
+  // xbar[c]: the XV copy c is complete; xbar[2 + c]: the XS copy c is complete
+  __shared__ __align__(8) uint64_t xbar[4];
   T* As = Av + (size_t)a.rows_v * a.ks;
   T* bv = As + (size_t)a.rows_s * a.kv;
   // row slices of this CTA (empty for trailing ranks when the rows do not divide evenly)
@@ -196,8 +239,12 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   const uint32_t s0 = min(a.ks, crank * a.rows_s), s1 = min(a.ks, s0 + a.rows_s);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 4; ++i) xbar_init(&xbar[i]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   for (uint32_t k = threadIdx.x; k < a.kv; k += kR1Threads) xvb[k] = A::load(a.xv[k]);
-  for (uint32_t k = threadIdx.x; k < a.ks; k += kR1Threads) xs[k] = A::load(a.xs[k]);
+  for (uint32_t k = threadIdx.x; k < a.ks; k += kR1Threads) xsb[k] = A::load(a.xs[k]);
   for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kR1Threads)
     Av[e] = A::load(a.Av[(size_t)v0 * a.ks + e]);
   for (size_t e = threadIdx.x; e < (size_t)(s1 - s0) * a.kv; e += kR1Threads)
@@ -205,6 +252,17 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) bv[r - v0] = A::load(a.b[r]);
   cluster.sync();
 
+  // ROM seismogram S(r) = PhiVp[gid_r, :] . XV after step nn, on its sample steps
+  // (main_reconstruct_seismo.cc:157-185); receiver r on CTA r % csize, so the rows
+  // spread evenly over the cluster; receiver rows in the kernel's own arithmetic
+  auto seismogram = [&](const T* x, unsigned long long nn) {
+    if (!a.fseis || nn % a.fseis != 0) return;
+    for (uint32_t r = crank + csize * warp; r < a.R; r += csize * kR1Warps) {
+      const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
+      const T s = A::dot(prow, x, a.kv, lane);
+      if (lane == 0) A::store_sample(a.seis + r + (size_t)a.R * (nn / a.fseis - 1), s);
+    }
+  };
   const T dtT = A::load(a.dt);
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
     const unsigned long long n = a.step0 + it + 1;
@@ -213,54 +271,53 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
     const T fdt = static_cast<const T*>(a.fdt_t)[it];
     // sample steps of the observers, decided once per step
     const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
-    const bool seis_now = a.fseis && n % a.fseis == 0;
-    const T* const xcur = xvb + (size_t)(it & 1) * a.kv;
-    T* const xv = xvb + (size_t)((it + 1) & 1) * a.kv;  // the new velocity state
-    // 1. velocity rows of this CTA
+    const uint32_t cur = (uint32_t)(it & 1), nxt = cur ^ 1u, par = (uint32_t)((it >> 1) & 1);
+    const T* const xvc = xvb + (size_t)cur * a.kv;
+    const T* const xsc = xsb + (size_t)cur * a.ks;
+    T* const xv = xvb + (size_t)nxt * a.kv;  // the new states
+    T* const xs = xsb + (size_t)nxt * a.ks;
+    // 1. velocity rows of this CTA, sent to copy nxt of every CTA (lane l -> CTA l)
+    if (threadIdx.x == 0) xbar_expect(&xbar[nxt], a.kv * (uint32_t)sizeof(T));
     for (uint32_t r = v0 + warp; r < v1; r += kR1Warps) {
-      const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
+      const T y = A::dot(Av + (size_t)(r - v0) * a.ks, xsc, a.ks, lane);
       if (lane < (int)csize) {
-        T x = A::update(xcur[r], y, dtT);
+        T x = A::update(xvc[r], y, dtT);
         x = A::axpy(x, fdt, bv[r - v0]);
-        T* dst = cluster.map_shared_rank(xv + r, lane);
-        *dst = x;
+        st_async8(peer_addr(smem_addr(xv + r), lane), bits8(x), peer_addr(smem_addr(&xbar[nxt]), lane));
         if (lane == 0 && snap_v)
           a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
       }
     }
-    cluster_arrive();
-    cluster_wait();
+    bool ok = xbar_wait(&xbar[nxt], par);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(a.error, 1u);
+      break;
+    }
     // 2. stress rows of this CTA
+    if (threadIdx.x == 0) xbar_expect(&xbar[2 + nxt], a.ks * (uint32_t)sizeof(T));
     for (uint32_t r = s0 + warp; r < s1; r += kR1Warps) {
       const T y = A::dot(As + (size_t)(r - s0) * a.kv, xv, a.kv, lane);
-      const T xold = xs[r];
-      __syncwarp();
       if (lane < (int)csize) {
-        const T x = A::update(xold, y, dtT);
-        T* dst = cluster.map_shared_rank(xs + r, lane);
-        *dst = x;
+        const T x = A::update(xsc[r], y, dtT);
+        st_async8(peer_addr(smem_addr(xs + r), lane), bits8(x), peer_addr(smem_addr(&xbar[2 + nxt]), lane));
         if (lane == 0 && snap_s)
           a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
       }
     }
-    cluster_arrive();
-    // ROM seismogram S(r) = PhiVp[gid_r, :] . xv  (main_reconstruct_seismo.cc:157-185),
-    // inside the barrier: it reads only this step's XV copy, which nobody writes until
-    // every CTA has arrived here
-    if (seis_now) {
-      // receiver r on CTA r % csize: the rows spread evenly over the cluster
-      for (uint32_t r = crank + csize * warp; r < a.R; r += csize * kR1Warps) {
-        // receiver rows in the kernel's own arithmetic (FP64, or FP32 hi + lo)
-        const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
-        const T s = A::dot(prow, xv, a.kv, lane);
-        if (lane == 0) A::store_sample(a.seis + r + (size_t)a.R * (n / a.fseis - 1), s);
-      }
+    // the seismogram while the stress rows travel: it reads only this step's XV copy
+    seismogram(xv, n);
+    ok = xbar_wait(&xbar[2 + nxt], par);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(a.error, 2u);
+      break;
     }
-    cluster_wait();
   }
-  const T* const xfin = xvb + (size_t)(a.nsteps & 1) * a.kv;
-  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) a.xv[r] = A::value(xfin[r]);
-  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xs[r]);
+  const T* const xvf = xvb + (size_t)(a.nsteps & 1) * a.kv;
+  const T* const xsf = xsb + (size_t)(a.nsteps & 1) * a.ks;
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) a.xv[r] = A::value(xvf[r]);
+  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xsf[r]);
+  // no CTA leaves while a peer may still deliver rows into its shared memory
+  cluster.sync();
 }
 
 // FP64 -> FP32 hi + lo; in and out may be the same array (each element is read before
@@ -346,6 +403,7 @@ struct shaw_rom_s {
   void* phi_rcv_df = nullptr;  // receiver rows split into FP32 hi + lo (rank-1 mixed form)
   double* fdt = nullptr;  // rank-1 forcing table of the current launch
   uint64_t fdt_cap = 0;
+  unsigned int* r1_err = nullptr;  // rank-1 kernel: an exchange wait ran out
   // rank-1 cluster launch shape
   uint32_t cluster = 1, rows_v = 0, rows_s = 0;
   size_t smem = 0;
@@ -370,7 +428,7 @@ int rank1_configure(RH* h) {
     if (bytes <= budget) {
       // prefer the smallest cluster whose per-CTA row slice keeps the warps busy
       // FP64 GEMV rows are the cost on GB300's narrow FP64 pipe: spread them over up
-      // to 16 CTAs (the cluster barrier costs less than the extra rows per CTA)
+      // to 16 CTAs (the cluster exchange costs less than the extra rows per CTA)
       if (rv > 16 && c < 16) continue;
       h->cluster = c; h->rows_v = rv; h->rows_s = rs; h->smem = bytes;
       return SHAW_OK;
@@ -401,6 +459,11 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
     h->launches++;
     SHAW_CUDA(cudaGetLastError());
   }
+  if (!h->r1_err) {
+    SHAW_CUDA(cudaMalloc(&h->r1_err, sizeof(unsigned int)));
+    SHAW_CUDA(cudaMemsetAsync(h->r1_err, 0, sizeof(unsigned int), h->stream));
+  }
+  a.error = h->r1_err;
   a.fdt_t = h->fdt; a.dt = dt;
   a.kv = (uint32_t)h->kv; a.ks = (uint32_t)h->ks; a.rows_v = h->rows_v; a.rows_s = h->rows_s;
   a.step0 = h->step; a.nsteps = nsteps;
@@ -550,7 +613,7 @@ void shaw_rom_destroy(shaw_rom_t h) {
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
   void* bufs[] = {h->Av, h->As, h->b, h->xv, h->xs, h->kind, h->period, h->delay,
-                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->phi_rcv_df};
+                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->phi_rcv_df, h->r1_err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -661,6 +724,7 @@ int shaw_rom_reset(shaw_rom_t h) {
   SHAW_CUDA(cudaMemsetAsync(h->xv, 0, h->kv * h->M * sizeof(double), h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->xs, 0, h->ks * h->M * sizeof(double), h->stream));
   if (h->seis) SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)h->R * h->seis_T * h->M * sizeof(double), h->stream));
+  if (h->r1_err) SHAW_CUDA(cudaMemsetAsync(h->r1_err, 0, sizeof(unsigned int), h->stream));
   if (h->tc || h->oz) {
     const int rc = h->tc ? shaw::tc::reset(h->tc, h->stream) : shaw::oz::reset(h->oz, h->stream);
     if (rc) return rc;
@@ -709,6 +773,13 @@ int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
 int shaw_rom_synchronize(shaw_rom_t h) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->rank == 1 && h->r1_err) {
+    unsigned int err = 0;
+    SHAW_CUDA(cudaMemcpy(&err, h->r1_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err)
+      return shaw::fail(SHAW_ERR_CUDA, "rank-1 ROM kernel: a cluster exchange wait ran out (code " +
+                                           std::to_string(err) + ")");
+  }
   if (h->rank == 1 && h->fvp) {
     // rank-1 snapshots are collected on the device; copy what the run produced
     const uint64_t Tv = std::min<uint64_t>(h->step / h->fvp, h->snap_nsteps / h->fvp);
