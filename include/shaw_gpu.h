@@ -70,7 +70,10 @@ extern "C" {
 #define SHAW_MIXED_FP32       3  /* ROM rank 1: FP32 hi+lo arithmetic; FOM: FP32 state     */
 #define SHAW_MIXED_OZAKI_BF16 4  /* ROM rank 2: BF16 tensor cores, 6 six-bit slices per
                                     operand (Ozaki scheme), exact FP32 accumulation,
-                                    compensated FP32 state: FP64-grade GEMMs              */
+                                    compensated FP32 state (~2^-36 products)             */
+#define SHAW_OZAKI_FP64       5  /* ROM rank 2: BF16 tensor cores, 9 six-bit slices per
+                                    operand, exact FP32 accumulation, FP64 state:
+                                    FP64-grade results at tensor-core speed               */
 
 const char* shaw_last_error(void);
 const char* shaw_version(void);
@@ -193,7 +196,8 @@ int shaw_rom_project_noalloc(shaw_fom_t fom, const double* d_phi_vp, uint64_t kv
  * rom_jvp kv x ks and rom_jsp ks x kv row-major; b kv x M LayoutLeft with
  * b[:,j] = rhoInv[src_j] * PhiVp[src_j, :] (rom_problem_rank_one.hpp:137-147).
  * precision: SHAW_FP64, or SHAW_MIXED_FP32 (rank 1: FP32 hi+lo operators and
- * state, error-free products and compensated sums). */
+ * state, error-free products and compensated sums); rank 2 also SHAW_MIXED_TF32X3,
+ * SHAW_MIXED_OZAKI_BF16 and SHAW_OZAKI_FP64 (tensor cores, one persistent launch). */
 int shaw_rom_create(uint64_t kv, uint64_t ks, const double* rom_jvp, const double* rom_jsp, int rank,
                     uint32_t num_forcings, const double* b, int precision, shaw_rom_t* out);
 void shaw_rom_destroy(shaw_rom_t h);
@@ -207,8 +211,9 @@ int shaw_rom_set_snapshots(shaw_rom_t h, uint64_t freq_vp, uint64_t freq_sp, uin
  * steps (reconstructSeismogram, main_reconstruct_seismo.cc:157-185, whose rank-2 form
  * the reference leaves unimplemented at :187-190); phi_rows is R x kv row-major (the
  * basis rows of the receivers' vp gids).  FP64 and rank-1 mixed: FP64 / double-float
- * dots; SHAW_MIXED_OZAKI_BF16: an exact sliced product on the tensor cores inside the
- * persistent kernel; SHAW_MIXED_TF32X3: SHAW_ERR_UNSUPPORTED (use snapshots). */
+ * dots; SHAW_MIXED_OZAKI_BF16 / SHAW_OZAKI_FP64: an exact sliced product on the tensor
+ * cores inside the persistent kernel; SHAW_MIXED_TF32X3: SHAW_ERR_UNSUPPORTED (use
+ * snapshots). */
 int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t num_receivers, uint64_t freq,
                            uint64_t nsteps);
 int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps);
@@ -228,8 +233,8 @@ uint64_t shaw_rom_kernel_launches(shaw_rom_t h);
  * Every instance is that system with its own kv, ks, operators, forcing vectors b
  * (kv x M LayoutLeft, column j = rhoInv[src_j] PhiVp[src_j, :]) and per-column
  * signals; all advance with one dt.  precision: SHAW_FP64 (cuBLAS DGEMMs per
- * instance) or SHAW_MIXED_OZAKI_BF16 (all instances, all steps, one persistent
- * tensor-core launch; kv, ks <= 1024). */
+ * instance), or SHAW_MIXED_OZAKI_BF16 / SHAW_OZAKI_FP64 (all instances, all steps, one
+ * persistent tensor-core launch; kv, ks <= 1024). */
 typedef struct shaw_rom_batch_s* shaw_rom_batch_t;
 typedef struct {
   uint64_t kv, ks;

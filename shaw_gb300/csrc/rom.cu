@@ -554,9 +554,11 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
   if (rank == 1 && M != 1) return shaw::fail(SHAW_ERR_INVALID_ARG, "the rank-1 form has exactly one forcing");
   if (rank == 1 && precision != SHAW_FP64 && precision != SHAW_MIXED_FP32)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "rank-1 ROM precision must be SHAW_FP64 or SHAW_MIXED_FP32");
-  if (rank == 2 && precision != SHAW_FP64 && precision != SHAW_MIXED_TF32X3 && precision != SHAW_MIXED_OZAKI_BF16)
+  if (rank == 2 && precision != SHAW_FP64 && precision != SHAW_MIXED_TF32X3 && precision != SHAW_MIXED_OZAKI_BF16 &&
+      precision != SHAW_OZAKI_FP64)
     return shaw::fail(SHAW_ERR_UNSUPPORTED,
-                      "rank-2 ROM precision must be SHAW_FP64, SHAW_MIXED_TF32X3 or SHAW_MIXED_OZAKI_BF16");
+                      "rank-2 ROM precision must be SHAW_FP64, SHAW_MIXED_TF32X3, SHAW_MIXED_OZAKI_BF16 or "
+                      "SHAW_OZAKI_FP64");
   RH* h = new RH();
   h->kv = kv; h->ks = ks; h->M = M; h->rank = rank; h->precision = precision;
   auto bail = [&](int rc) { shaw_rom_destroy(h); return rc; };
@@ -585,10 +587,10 @@ int shaw_rom_create(uint64_t kv, uint64_t ks, const double* Av, const double* As
     rc = shaw::tc::create(h->tc, (uint32_t)kv, (uint32_t)ks, h->Av, h->As, M, h->b, h->stream);
     if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = shaw::fail(SHAW_ERR_CUDA, "tensor-core ROM setup failed");
-  } else if (precision == SHAW_MIXED_OZAKI_BF16) {
+  } else if (precision == SHAW_MIXED_OZAKI_BF16 || precision == SHAW_OZAKI_FP64) {
     shaw::oz::InstanceDesc d;
     d.kv = (uint32_t)kv; d.ks = (uint32_t)ks; d.M = M; d.Av = Av; d.As = As; d.b = b;
-    rc = shaw::oz::create(h->oz, 1, &d, h->stream);
+    rc = shaw::oz::create(h->oz, 1, &d, h->stream, precision == SHAW_OZAKI_FP64 ? 9 : 6);
     if (rc == SHAW_OK) rc = shaw::oz::set_signals(h->oz, 0, h->kind, h->period, h->delay);
     if (rc == SHAW_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = shaw::fail(SHAW_ERR_CUDA, "Ozaki tensor-core ROM setup failed");

@@ -142,8 +142,9 @@ int shaw_rom_batch_create(uint32_t n, const shaw_rom_instance_desc* desc, int pr
   if (!out || !desc) return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
   *out = nullptr;
   if (n == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "a batch needs at least one instance");
-  if (precision != SHAW_FP64 && precision != SHAW_MIXED_OZAKI_BF16)
-    return shaw::fail(SHAW_ERR_UNSUPPORTED, "batched ROM precision must be SHAW_FP64 or SHAW_MIXED_OZAKI_BF16");
+  if (precision != SHAW_FP64 && precision != SHAW_MIXED_OZAKI_BF16 && precision != SHAW_OZAKI_FP64)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED,
+                      "batched ROM precision must be SHAW_FP64, SHAW_MIXED_OZAKI_BF16 or SHAW_OZAKI_FP64");
   for (uint32_t i = 0; i < n; ++i) {
     const shaw_rom_instance_desc& d = desc[i];
     const std::string who = "instance " + std::to_string(i) + ": ";
@@ -206,7 +207,7 @@ int shaw_rom_batch_create(uint32_t n, const shaw_rom_instance_desc* desc, int pr
       od[i].kv = (uint32_t)desc[i].kv; od[i].ks = (uint32_t)desc[i].ks; od[i].M = desc[i].num_forcings;
       od[i].Av = desc[i].rom_jvp; od[i].As = desc[i].rom_jsp; od[i].b = desc[i].b;
     }
-    int rc = shaw::oz::create(h->oz, n, od.data(), h->stream);
+    int rc = shaw::oz::create(h->oz, n, od.data(), h->stream, precision == SHAW_OZAKI_FP64 ? 9 : 6);
     for (uint32_t i = 0; rc == SHAW_OK && i < n; ++i)
       rc = shaw::oz::set_signals(h->oz, i, h->inst[i].kind, h->inst[i].period, h->inst[i].delay);
     if (rc) return bail(rc);

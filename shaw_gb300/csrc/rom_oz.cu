@@ -61,21 +61,30 @@ namespace {
 // (two groups of four: warp w reads TMEM lanes 32*(w%4).., each group half the columns)
 constexpr int kThreads = 384;
 constexpr int kEpiThreads = 256;
-constexpr int kSlices = 6;
-constexpr int kDiags = 6;                     // d = s + t in [0, 5]
 constexpr int kKc = 32;                       // BF16 K-elements per pipeline stage (64 bytes per row)
 constexpr uint32_t kRowBytes = kKc * 2;
 constexpr uint32_t kATile = 128 * kRowBytes;  // one slice of a 128 x 32 operator tile: 8 KB
-constexpr uint32_t kABytes = kSlices * kATile;
-constexpr uint32_t kMaxNb = 64;
-constexpr uint32_t kStageBytes = kABytes + kSlices * kMaxNb * kRowBytes;  // 72 KB
-constexpr int kStages = 3;
-// TMEM: two accumulator sets at columns 0 and 256 when 6 nb <= 256; otherwise one set at
-// column 0 and the staging of its combined values at column 6 nb
+constexpr uint32_t kMaxNb = 64;               // widest tile of either form
+constexpr int kMaxStages = 3;
+// TMEM: two accumulator sets at columns 0 and 256 when S nb <= 256; otherwise one set at
+// column 0 and the staging of its combined values at column S nb
 constexpr uint32_t kTmemCols = 512;
 
-__host__ __device__ constexpr uint32_t bstage_bytes(uint32_t nb) { return kSlices * nb * kRowBytes; }
-__host__ __device__ constexpr uint32_t acc_buffers(uint32_t nb) { return (kDiags * nb <= 256) ? 2u : 1u; }
+// The two forms of the scheme, by slice count S (the diagonals d = s + t <= S - 1 kept):
+//   S = 6: 36-bit slicing, FP32 hi + lo state (SHAW_MIXED_OZAKI_BF16);
+//   S = 9: 54-bit slicing, FP64 state: FP64-grade results (SHAW_OZAKI_FP64).
+// Exactness of the FP32 accumulators (K <= 1024): a diagonal d holds at most d + 1 slice
+// pairs; the first slice of either operand is in [-64, 64], the others in [-32, 32], so
+// d = 8 sums below 2 * 64 * 32 * 1024 + 7 * 32 * 32 * 1024 = 11 * 2^20 < 2^24.
+template <int S>
+struct Geo {
+  static constexpr uint32_t kABytes = S * kATile;                              // 48 / 72 KB
+  static constexpr uint32_t kMaxNb = S == 6 ? 64u : 16u;
+  static constexpr uint32_t kStageBytes = kABytes + S * kMaxNb * kRowBytes;  // 72 / 81 KB
+  static constexpr int kStages = S == 6 ? 3 : 2;
+  __host__ __device__ static constexpr uint32_t bstage_bytes(uint32_t nb) { return S * nb * kRowBytes; }
+  __host__ __device__ static constexpr uint32_t acc_buffers(uint32_t nb) { return (S * nb <= 256) ? 2u : 1u; }
+};
 
 // Byte offset of (row r, k) in a K-major, no-swizzle BF16 tile of 32 K-elements:
 // core matrices of 8 rows x 16 bytes, K-direction stride 128 B, 8-row-group stride 512 B.
@@ -84,13 +93,15 @@ __host__ __device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k) {
 }
 
 // Byte offset of (slice s, column j, K-row k) in one pipeline stage of state slices (the
-// B operand, MN-major, no swizzle): the 6 slices are stacked along N (n = s*nb + j); a
+// B operand, MN-major, no swizzle): the S slices are stacked along N (n = s*nb + j); a
 // core matrix is 8 K-rows x 16 bytes (8 consecutive n); N-direction stride 128 B,
-// K-direction stride 96*nb B (all 6*nb columns of one 8-row K group).  Eight
-// consecutive columns of one row are 16 contiguous bytes.
+// K-direction stride 16*S*nb B (all S*nb columns of one 8-row K group).  Eight
+// consecutive columns of one row are 16 contiguous bytes; slice s starts 16*nb*s bytes
+// after slice 0.
+template <int S>
 __host__ __device__ __forceinline__ uint32_t bslice_off(uint32_t nb, uint32_t s, uint32_t j, uint32_t k) {
   const uint32_t n = s * nb + j;
-  return (k >> 3) * (96u * nb) + ((n >> 3) << 7) + ((k & 7u) << 4) + ((n & 7u) << 1);
+  return (k >> 3) * (16u * S * nb) + ((n >> 3) << 7) + ((k & 7u) << 4) + ((n & 7u) << 1);
 }
 
 // Global stores as inline PTX without a memory clobber: the epilogue's stores go to
@@ -111,7 +122,9 @@ struct OzInst {
   const int* alpha_s;
   const float* bh;
   const float* bl;  // [Mp][kvp]
-  float *xvh, *xvl, *xsh, *xsl;
+  float *xvh, *xvl, *xsh, *xsl;  // 6-slice form: states as FP32 hi + lo, [Mp][kp]
+  const double* b64;              // 9-slice form: forcing vectors and states in FP64
+  double *xv64, *xs64;
   const int* kind;
   const double* period;
   const double* delay;
@@ -153,7 +166,7 @@ struct OzArgs {
 };
 
 struct Shared {
-  uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], drain;
+  uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], drain;
   uint32_t tmem;
   int abort;
   int beta_v[kMaxNb], beta_s[kMaxNb];   // exponents the current B tiles were sliced with
@@ -161,6 +174,7 @@ struct Shared {
   unsigned int colmax[kMaxNb];
   unsigned long long reslice_v, reslice_s;  // columns to re-slice exactly after a phase
   float fdt_h[kMaxNb], fdt_l[kMaxNb];  // f_j(t_{n-1}) * dt of the current step, as FP32 hi + lo
+  double fdt64[kMaxNb];                 // the same in FP64 (9-slice form)
   OzInst in;
   OzTile tile;
 };
@@ -190,12 +204,15 @@ constexpr uint32_t kIdescBMnMajor = 1u << 16;
 // One GEMM phase: for every 128-row M-tile, D_d = sum over K of the slice pairs on
 // diagonal d into an accumulator set; the epilogue `epi(mt, tmem_cols)` runs on warps
 // 4..11 while the MMAs of the next M-tile fill the other set.
-template <typename Epi>
+template <int S, typename Epi>
 __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const uint8_t* Aop, const uint8_t* Bop,
                                            uint32_t mt0, uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
                                            uint32_t (&uses)[2], unsigned int* err, Epi epi) {
+  using G = Geo<S>;
+  constexpr int kStages = G::kStages;
+  constexpr uint32_t kStageBytes = G::kStageBytes, kABytes = G::kABytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t bbytes = bstage_bytes(nb), nbuf = acc_buffers(nb);
+  const uint32_t bbytes = G::bstage_bytes(nb), nbuf = G::acc_buffers(nb);
   if (warp == 0 && lane == 0) {
     for (uint32_t q = 0; q < n_mt * n_kc && !sh->abort; ++q) {
       const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
@@ -223,24 +240,24 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
         // descriptors of the stage's first A / B slice; the others differ only in the
         // start-address field (16-byte units, no carry: shared addresses < 256 KB)
         const uint64_t adesc0 = smem_desc(abase, 128, 512);
-        const uint64_t bdesc0 = smem_desc(abase + kABytes, 96u * nb, 128);  // MN-major state slices
+        const uint64_t bdesc0 = smem_desc(abase + kABytes, 16u * S * nb, 128);  // MN-major state slices
         // The B slices of a stage are stacked along N (slice t = rows t*nb ..), and the
         // diagonal accumulators along TMEM columns (diagonal d = columns d*nb ..), so
-        // operator slice sa times the state slices tb = 0 .. 5-sa is ONE MMA of
-        // N = (6-sa)*nb whose output columns start at diagonal sa: 6 MMAs per K-step
-        // instead of 21 pair MMAs, each A slice read from shared memory once.  N is
-        // capped at 256 (split into two MMAs for nb = 64).  The first MMA of a tile
+        // operator slice sa times the state slices tb = 0 .. S-1-sa is ONE MMA of
+        // N = (S-sa)*nb whose output columns start at diagonal sa: S MMAs per K-step
+        // instead of S(S+1)/2 pair MMAs, each A slice read from shared memory once.  N
+        // is capped at 256 (split into two MMAs where needed).  The first MMA of a tile
         // (sa = 0 covers every diagonal) starts the accumulation.
 #pragma unroll
         for (uint32_t k = 0; k < kKc / 16; ++k) {
 #pragma unroll
-          for (int sa = 0; sa < kSlices; ++sa) {
+          for (int sa = 0; sa < S; ++sa) {
             const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
             const uint32_t acc = (c > 0 || k > 0 || sa > 0) ? 1u : 0u;
-            uint32_t tb = 0, left = (uint32_t)(kSlices - sa);
+            uint32_t tb = 0, left = (uint32_t)(S - sa);
             while (left) {
               const uint32_t take = min(left, 256u / nb);
-              const uint64_t bdesc = bdesc0 + ((tb * 16u * nb + k * 192u * nb) >> 4);
+              const uint64_t bdesc = bdesc0 + ((tb * 16u * nb + k * 32u * S * nb) >> 4);
               mma_f16(dcol + (sa + tb) * nb, adesc, bdesc, idesc_bf16(take * nb) | kIdescBMnMajor, acc);
               tb += take;
               left -= take;
@@ -288,6 +305,7 @@ __device__ __forceinline__ void pow2_pair(int e, float& f1, float& f2) {
 // y = Y * 2^-42 (before the row / column scaling).  No integer or 64-bit conversions.
 __device__ __forceinline__ void load_combine8(uint32_t tcols, uint32_t nb, int q, uint32_t j0, float* yh,
                                               float* yl) {
+  constexpr int kDiags = 6;
   float D[kDiags][8];
 #pragma unroll
   for (int d = 0; d < kDiags; ++d) tmem_ld8(tcols + ((uint32_t)(q * 32) << 16) + d * nb + j0, D[d]);
@@ -344,7 +362,7 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
                                             const int* beta, uint8_t* tiles, unsigned long long mask, uint32_t r0,
                                             uint32_t r1) {
   const uint32_t t = threadIdx.x - 128;
-  const uint32_t bbytes = bstage_bytes(nb);
+  const uint32_t bbytes = Geo<6>::bstage_bytes(nb);
   const uint32_t nr = r1 - r0, n = nr * nb;
   for (uint32_t e0 = t; e0 < n; e0 += 4 * kEpiThreads) {
     float vh[4], vl[4];
@@ -364,9 +382,9 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
       if (e0 + u * kEpiThreads >= n) break;
       if (!((mask >> jj[u]) & 1ull)) continue;
       float h = ldexpf(vh[u], -beta[jj[u]]), l = ldexpf(vl[u], -beta[jj[u]]);
-      uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + bslice_off(nb, 0, jj[u], rr[u] % kKc);
+      uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + bslice_off<6>(nb, 0, jj[u], rr[u] % kKc);
 #pragma unroll
-      for (int s = 0; s < kSlices; ++s) {
+      for (int s = 0; s < 6; ++s) {
         const float th = h * 64.f, tl = l * 64.f;
         float a = rintf(th);
         a = fminf(64.f, fmaxf(-64.f, a));
@@ -397,7 +415,7 @@ __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, c
     }
   }
 #pragma unroll
-  for (int s = 0; s < kSlices; ++s) {
+  for (int s = 0; s < 6; ++s) {
     uint32_t w[4];
 #pragma unroll
     for (int jj = 0; jj < 8; ++jj) {
@@ -411,6 +429,137 @@ __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, c
   }
 }
 
+// ---- 9-slice form: FP64 state, integer combination and slicing -------------------
+
+// v * 2^e for a power-of-two scaling, exact: an add to the exponent field when the
+// result stays normal, ldexp otherwise.
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7FF) + e;
+  if (v != 0.0 && ex > 0 && ex < 2047 && ((b >> 52) & 0x7FF) != 0) return __longlong_as_double(b + ((long long)e << 52));
+  return ldexp(v, e);
+}
+
+// Read the 9 diagonal accumulators of 8 columns for this thread's row and combine them
+// exactly in integers: D_d < 2^24 (integers held by FP32), Y = sum_d D_d 2^(6(8-d)) =
+// H 2^36 + L with H = D_0 2^12 + D_1 2^6 + D_2 (|H| < 2^36) and L = sum_{d>=3} D_d
+// 2^(6(8-d)) (|L| < 2^54); y = Y * 2^-60 before the row / column scaling.  Returned as
+// the FP64 pair (H exact, L rounded once).
+__device__ __forceinline__ void load_combine8_fp64(uint32_t tcols, uint32_t nb, int q, uint32_t j0, double* yH,
+                                                   double* yL) {
+  float D[9][8];
+#pragma unroll
+  for (int d = 0; d < 9; ++d) tmem_ld8(tcols + ((uint32_t)(q * 32) << 16) + d * nb + j0, D[d]);
+  tmem_wait_ld();
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    long long H = __float2int_rn(D[0][jj]);
+    H = H * 64 + __float2int_rn(D[1][jj]);
+    H = H * 64 + __float2int_rn(D[2][jj]);
+    long long L = __float2int_rn(D[3][jj]);
+#pragma unroll
+    for (int d = 4; d < 9; ++d) L = L * 64 + __float2int_rn(D[d][jj]);
+    yH[jj] = (double)H;
+    yL[jj] = (double)L;
+  }
+}
+
+// x * 2^(54 - beta) rounded to an integer, from the bits of x (no FP64 arithmetic): the
+// 54-bit fixed-point value of x / 2^beta for |x| < 2^beta.  Values at or above 2^beta
+// give meaningless results; the caller re-slices such columns exactly.
+__device__ __forceinline__ long long fixed54(double x, int beta) {
+  const long long bits = __double_as_longlong(x);
+  int e = (int)((bits >> 52) & 0x7FF);
+  long long m = bits & 0xFFFFFFFFFFFFFLL;
+  if (e == 0)
+    e = 1;  // subnormal: no implicit bit
+  else
+    m |= 1LL << 52;
+  const int sh = e - 1075 + 54 - beta;  // x / 2^beta * 2^54 = m * 2^sh
+  long long v;
+  if (sh >= 0)
+    v = sh <= 9 ? (m << sh) : 0;
+  else if (sh > -63)
+    v = (m + (1LL << (-sh - 1))) >> (-sh);
+  else
+    v = 0;
+  return bits < 0 ? -v : v;
+}
+
+// BF16 bits of a small integer (|a| <= 256 exactly): a + 1.5 * 2^23 as FP32 bits, back to
+// the float a, whose low 16 bits are zero.
+__device__ __forceinline__ uint32_t bf16_of_int(int a) {
+  return __float_as_uint(__int_as_float(0x4B400000 + a) - 12582912.0f) >> 16;
+}
+
+// Balanced base-64 digit s (most significant first) of a 54-bit fixed-point value v;
+// v keeps the remainder.  Digit 0 is in [-64, 64], the others in [-32, 32).
+template <int s>
+__device__ __forceinline__ int take_digit(long long& v) {
+  if constexpr (s == 8) {
+    return (int)v;
+  } else {
+    constexpr int b = 6 * (8 - s);
+    const long long a = (v + (1LL << (b - 1))) >> b;
+    v -= a << b;
+    return (int)a;
+  }
+}
+
+template <int s>
+__device__ __forceinline__ void slice9_step(long long (&v)[8], uint8_t* dst, uint32_t nb) {
+  uint32_t w[4];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) {
+    const uint32_t bits = bf16_of_int(take_digit<s>(v[jj]));
+    w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
+  }
+  st_v4(dst + s * 16u * nb, w);
+  if constexpr (s < 8) slice9_step<s + 1>(v, dst, nb);
+}
+
+// 9-slice form of slice_value8: 8 FP64 values of one row into the B tiles.
+__device__ __forceinline__ void slice_value8_fp64(const double* x, const int* e, uint8_t* dst, uint32_t nb) {
+  long long v[8];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) v[jj] = fixed54(x[jj], e[jj]);
+  slice9_step<0>(v, dst, nb);
+}
+
+// 9-slice form of slice_state: rows [r0, r1) x nb of an FP64 state block.
+__device__ __forceinline__ void slice_state_fp64(const double* x, uint32_t kp, uint32_t nb, const int* beta,
+                                                 uint8_t* tiles, unsigned long long mask, uint32_t r0, uint32_t r1) {
+  const uint32_t t = threadIdx.x - 128;
+  const uint32_t bbytes = Geo<9>::bstage_bytes(nb);
+  const uint32_t nr = r1 - r0, n = nr * nb;
+  for (uint32_t e = t; e < n; e += kEpiThreads) {
+    const uint32_t j = e / (nr ? nr : 1), r = r0 + (e - j * nr);
+    if (!((mask >> j) & 1ull)) continue;
+    long long v = fixed54(x[(size_t)j * kp + r], beta[j]);
+    uint8_t* base = tiles + (size_t)(r / kKc) * bbytes + bslice_off<9>(nb, 0, j, r % kKc);
+    int a[9];
+    a[0] = take_digit<0>(v); a[1] = take_digit<1>(v); a[2] = take_digit<2>(v);
+    a[3] = take_digit<3>(v); a[4] = take_digit<4>(v); a[5] = take_digit<5>(v);
+    a[6] = take_digit<6>(v); a[7] = take_digit<7>(v); a[8] = take_digit<8>(v);
+#pragma unroll
+    for (int s = 0; s < 9; ++s) *reinterpret_cast<uint16_t*>(base + s * 16u * nb) = (uint16_t)bf16_of_int(a[s]);
+  }
+}
+
+// Column-maximum key of an FP64 value: the upper 32 bits of |x| (monotonic in |x|).
+__device__ __forceinline__ unsigned int max_key64(double x) {
+  return (unsigned int)((__double_as_longlong(x) >> 32) & 0x7FFFFFFF);
+}
+
+// floor(log2 m) of a column maximum key (FP32 bits of |x| for S = 6, max_key64 for S = 9).
+template <int S>
+__device__ __forceinline__ int key_ilogb(unsigned int m) {
+  if constexpr (S == 6)
+    return ilogbf(__uint_as_float(m));
+  else
+    return (int)(m >> 20) - 1023;
+}
+
 // "no exponent yet": the int whose four bytes are 0x80 (what a byte-wise memset writes)
 constexpr int kNoPrediction = (int)0x80808080;
 
@@ -420,20 +569,21 @@ constexpr int kNoPrediction = (int)0x80808080;
 // *mask for an exact re-slice with beta = ilogb(m) + 1.  The next prediction is
 // ilogb(m) + 2 (one bit of headroom).  Epilogue threads t < nb; colmax is consumed;
 // *other (the other phase's mask, no longer read) is cleared.
+template <int S>
 __device__ __forceinline__ void settle_exponents(Shared* sh, uint32_t nb, int* beta, int* pred,
                                                  unsigned long long* mask, unsigned long long* other) {
   const uint32_t t = threadIdx.x - 128;
   if (t == 0) *other = 0ull;
   if (t < nb) {
-    const float m = __uint_as_float(sh->colmax[t]);
+    const unsigned int m = sh->colmax[t];
     sh->colmax[t] = 0u;
     const int p = pred[t];
     bool ok;
-    if (m == 0.f) {  // an all-zero column: its slices are zeros with any exponent
+    if (m == 0u) {  // an all-zero column: its slices are zeros with any exponent
       ok = p != kNoPrediction;
       beta[t] = ok ? p : 0;
     } else {
-      const int e = ilogbf(m);  // 2^e <= m < 2^(e+1)
+      const int e = key_ilogb<S>(m);  // 2^e <= m < 2^(e+1)
       ok = p != kNoPrediction && e + 1 <= p && p <= e + 3;
       beta[t] = ok ? p : e + 1;
       pred[t] = e + 2;
@@ -443,27 +593,35 @@ __device__ __forceinline__ void settle_exponents(Shared* sh, uint32_t nb, int* b
 }
 
 // Column exponents from the maxima gathered in colmax: |x| < 2^beta.
+template <int S>
 __device__ __forceinline__ void column_exponents(Shared* sh, uint32_t nb, int* beta, int* pred) {
   const uint32_t t = threadIdx.x - 128;
   if (t < nb) {
-    const float m = __uint_as_float(sh->colmax[t]);
-    beta[t] = (m > 0.f) ? ilogbf(m) + 1 : 0;
-    if (m > 0.f) pred[t] = beta[t] + 1;
+    const unsigned int m = sh->colmax[t];
+    beta[t] = (m != 0u) ? key_ilogb<S>(m) + 1 : 0;
+    if (m != 0u) pred[t] = beta[t] + 1;
     sh->colmax[t] = 0u;
   }
 }
 
-// Column maxima of |x| over the warp's 32 rows for 8 columns j0 .. j0+7: eight warp
-// reductions, then lane jj publishes column j0+jj with one shared atomic.
-__device__ __forceinline__ void note_max8(Shared* sh, uint32_t j0, const float* xh) {
+// Column maxima over the warp's 32 rows for 8 columns j0 .. j0+7 of monotonic keys of
+// |x|: eight warp reductions, then lane jj publishes column j0+jj with one shared atomic.
+__device__ __forceinline__ void note_max8_keys(Shared* sh, uint32_t j0, const unsigned int* key) {
   const int lane = threadIdx.x & 31;
   unsigned int mine = 0u;
 #pragma unroll
   for (int jj = 0; jj < 8; ++jj) {
-    const unsigned int m = __reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(xh[jj])));
+    const unsigned int m = __reduce_max_sync(0xffffffffu, key[jj]);
     if (lane == jj) mine = m;
   }
   if (lane < 8) atomicMax(&sh->colmax[j0 + lane], mine);
+}
+// keys of FP32 values: the bits of |x|
+__device__ __forceinline__ void note_max8(Shared* sh, uint32_t j0, const float* xh) {
+  unsigned int key[8];
+#pragma unroll
+  for (int jj = 0; jj < 8; ++jj) key[jj] = __float_as_uint(fabsf(xh[jj]));
+  note_max8_keys(sh, j0, key);
 }
 
 __device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
@@ -493,10 +651,14 @@ __device__ __forceinline__ void pair_sync(Shared* sh, unsigned int* ctr, uint32_
   __syncthreads();
 }
 
+// S = 6: FP32 hi + lo state (SHAW_MIXED_OZAKI_BF16); S = 9: FP64 state (SHAW_OZAKI_FP64).
+template <int S>
 __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) {
+  using G = Geo<S>;
+  constexpr int kStages = G::kStages;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* stages = smem;
-  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * kStageBytes);
+  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * G::kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ew = warp - 4;  // >= 0 on the epilogue warps
   const int q = warp & 3;   // TMEM lane quarter of this warp
@@ -542,16 +704,21 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const bool paired = (sh->tile.pinfo & 2u) != 0u;
     const uint32_t part = sh->tile.pinfo & 1u, slot = sh->tile.pinfo >> 2;
     const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
-    const uint32_t bbytes = bstage_bytes(nb);                                      // B stage bytes
-    const bool stage = acc_buffers(nb) == 1;  // single accumulator set: stage it in TMEM
-    const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + kDiags * nb;
+    const uint32_t bbytes = G::bstage_bytes(nb);                                   // B stage bytes
+    // single accumulator set: stage it in TMEM (6-slice form, nb = 64; the 9-slice form
+    // keeps tiles of 16 columns and two sets)
+    const bool stage = S == 6 && G::acc_buffers(nb) == 1;
+    const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + S * nb;
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
-    float* const xvh = in.xvh + (size_t)col0 * in.kvp;
-    float* const xvl = in.xvl + (size_t)col0 * in.kvp;
-    float* const xsh = in.xsh + (size_t)col0 * in.ksp;
-    float* const xsl = in.xsl + (size_t)col0 * in.ksp;
-    const float* const bh = in.bh + (size_t)col0 * in.kvp;
-    const float* const bl = in.bl + (size_t)col0 * in.kvp;
+    float* const xvh = S == 6 ? in.xvh + (size_t)col0 * in.kvp : nullptr;
+    float* const xvl = S == 6 ? in.xvl + (size_t)col0 * in.kvp : nullptr;
+    float* const xsh = S == 6 ? in.xsh + (size_t)col0 * in.ksp : nullptr;
+    float* const xsl = S == 6 ? in.xsl + (size_t)col0 * in.ksp : nullptr;
+    const float* const bh = S == 6 ? in.bh + (size_t)col0 * in.kvp : nullptr;
+    const float* const bl = S == 6 ? in.bl + (size_t)col0 * in.kvp : nullptr;
+    double* const xv64 = S == 9 ? in.xv64 + (size_t)col0 * in.kvp : nullptr;
+    double* const xs64 = S == 9 ? in.xs64 + (size_t)col0 * in.ksp : nullptr;
+    const double* const b64 = S == 9 ? in.b64 + (size_t)col0 * in.kvp : nullptr;
     // M-tiles of this CTA: all of them, or its half of a paired tile (part 0 the first
     // ceil(n/2), part 1 the rest); the B slices are then one buffer per pair
     auto half = [&](uint32_t n, uint32_t& m0, uint32_t& m1) {
@@ -591,13 +758,14 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       const uint32_t nr = (ms1 - ms0) * 128;
       for (uint32_t e = threadIdx.x - 128; e < nr * nb; e += kEpiThreads) {
         const uint32_t j = e / nr, row = ms0 * 128 + (e - j * nr);
-        atomicMax(&sh->colmax[j], __float_as_uint(fabsf(xsh[(size_t)j * in.ksp + row])));
+        const size_t si = (size_t)j * in.ksp + row;
+        atomicMax(&sh->colmax[j], S == 6 ? __float_as_uint(fabsf(xsh[si])) : max_key64(xs64[si]));
       }
     }
     if (paired) exchange();
     if (ew >= 0) {
       epi_barrier();
-      column_exponents(sh, nb, sh->beta_s, sh->pred_s);
+      column_exponents<S>(sh, nb, sh->beta_s, sh->pred_s);
       const uint32_t t = threadIdx.x - 128;
       if (t < nb) {
         const int bs = in.expo[col0 + t];
@@ -608,7 +776,10 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
       }
       epi_barrier();
-      slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
+      if constexpr (S == 6)
+        slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
+      else
+        slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
       asm volatile("fence.proxy.async.global;" ::: "memory");
     }
     if (paired) pair_sync(sh, pctr, nsync, a.error);  // both halves of the XS slices written
@@ -625,6 +796,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
                          : 0.0;
           sh->fdt_h[t] = (float)f;
           sh->fdt_l[t] = (float)(f - (double)sh->fdt_h[t]);
+          sh->fdt64[t] = f;
         }
         epi_barrier();
       }
@@ -633,12 +805,13 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
       const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
       // ---------------- velocity: XV += dt Av XS + fdt b ----------------
-      gemm_phase(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
+      if constexpr (S == 6) {
+      gemm_phase<S>(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
                  [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row];
-        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off(nb, 0, 0, row % kKc);
+        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
           float ph[8], pl[8], qh[8], ql[8];
           int pe[8];
@@ -678,13 +851,57 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
+      } else {
+      gemm_phase<S>(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
+                 [&](uint32_t mt, uint32_t tcols, uint64_t*) {
+        const uint32_t row = mt * 128 + q * 32 + lane;
+        const int alpha = in.alpha_v[row] - 60;
+        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+          double x[8], f[8];
+          int pe[8];
+          unsigned int key[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
+            const size_t si = (size_t)(j0 + jj) * in.kvp + row;
+            x[jj] = xv64[si];
+            f[jj] = b64[si];
+          }
+          double yH[8], yL[8];
+          load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const uint32_t j = j0 + jj, col = col0 + j;
+            const int e = alpha + sh->beta_s[j];
+            // x += dt * y with y = (yH 2^36 + yL) 2^e, then x += fdt * b
+            double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
+            xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
+            xn = fma(sh->fdt64[j], f[jj], xn);
+            st_f64(xv64 + (size_t)j * in.kvp + row, xn);
+            x[jj] = xn;
+            key[jj] = max_key64(xn);
+            const int pv = sh->pred_v[j];
+            pe[jj] = pv != kNoPrediction ? pv : 0;
+            if (snap_v && row < in.kv && col < in.M) st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), xn);
+          }
+          slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
+          note_max8_keys(sh, j0, key);
+        }
+        return false;
+      });
+      }
       if (paired) exchange();
       if (ew >= 0) {
         epi_barrier();
-        settle_exponents(sh, nb, sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s);
+        settle_exponents<S>(sh, nb, sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s);
         epi_barrier();
         const unsigned long long redo = sh->reslice_v;
-        if (redo && !sh->abort) slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
+        if (redo && !sh->abort) {
+          if constexpr (S == 6)
+            slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
+          else
+            slice_state_fp64(xv64, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
+        }
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       // paired: the re-sliced rows of both parts must land before either reads them (the
@@ -696,19 +913,31 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       // are its B operand, so the product is exact like the leapfrog's)
       if (in.seis && in.fseis && n % in.fseis == 0) {
         const unsigned long long tcnt = n / in.fseis - 1;
-        gemm_phase(stages, sh, in.Ar, bvt, mr0, mr1 - mr0, n_kc_s, nb, it, uses, a.error,
+        gemm_phase<S>(stages, sh, in.Ar, bvt, mr0, mr1 - mr0, n_kc_s, nb, it, uses, a.error,
                    [&](uint32_t mt, uint32_t tcols, uint64_t*) {
                      const uint32_t r = mt * 128 + q * 32 + lane;
                      const int alpha = in.alpha_r[r];
                      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-                       float yh[8], yl[8];
-                       load_combine8(tcols, nb, q, j0, yh, yl);
+                       double v[8];
+                       if constexpr (S == 6) {
+                         float yh[8], yl[8];
+                         load_combine8(tcols, nb, q, j0, yh, yl);
+#pragma unroll
+                         for (int jj = 0; jj < 8; ++jj)
+                           v[jj] = ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]);
+                       } else {
+                         double yH[8], yL[8];
+                         load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+#pragma unroll
+                         for (int jj = 0; jj < 8; ++jj) {
+                           const int e = alpha + sh->beta_v[j0 + jj] - 60;
+                           v[jj] = fma(scale_pow2(1.0, e + 36), yH[jj], scale_pow2(yL[jj], e));
+                         }
+                       }
 #pragma unroll
                        for (int jj = 0; jj < 8; ++jj) {
                          const uint32_t col = col0 + j0 + jj;
-                         if (r < in.R && col < in.M)
-                           st_f64(in.seis + r + (size_t)in.R * (tcnt + in.Tseis * col),
-                                  ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]));
+                         if (r < in.R && col < in.M) st_f64(in.seis + r + (size_t)in.R * (tcnt + in.Tseis * col), v[jj]);
                        }
                      }
                      return false;
@@ -716,12 +945,13 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         if (__syncthreads_or(sh->abort != 0)) break;
       }
       // ---------------- stress: XS += dt As XV ----------------
-      gemm_phase(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
+      if constexpr (S == 6) {
+      gemm_phase<S>(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
                  [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row];
-        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off(nb, 0, 0, row % kKc);
+        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
         for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
           float ph[8], pl[8];
           int pe[8];
@@ -756,13 +986,51 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
+      } else {
+      gemm_phase<S>(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
+                 [&](uint32_t mt, uint32_t tcols, uint64_t*) {
+        const uint32_t row = mt * 128 + q * 32 + lane;
+        const int alpha = in.alpha_s[row] - 60;
+        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+          double x[8];
+          int pe[8];
+          unsigned int key[8];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) x[jj] = xs64[(size_t)(j0 + jj) * in.ksp + row];
+          double yH[8], yL[8];
+          load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) {
+            const uint32_t j = j0 + jj, col = col0 + j;
+            const int e = alpha + sh->beta_v[j];
+            double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
+            xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
+            st_f64(xs64 + (size_t)j * in.ksp + row, xn);
+            x[jj] = xn;
+            key[jj] = max_key64(xn);
+            const int ps = sh->pred_s[j];
+            pe[jj] = ps != kNoPrediction ? ps : 0;
+            if (snap_s && row < in.ks && col < in.M) st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), xn);
+          }
+          slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
+          note_max8_keys(sh, j0, key);
+        }
+        return false;
+      });
+      }
       if (paired) exchange();
       if (ew >= 0) {
         epi_barrier();
-        settle_exponents(sh, nb, sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v);
+        settle_exponents<S>(sh, nb, sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v);
         epi_barrier();
         const unsigned long long redo = sh->reslice_s;
-        if (redo && !sh->abort) slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
+        if (redo && !sh->abort) {
+          if constexpr (S == 6)
+            slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
+          else
+            slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
+        }
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       if (paired && __syncthreads_or(ew >= 0 && sh->reslice_s != 0ull)) pair_sync(sh, pctr, nsync, a.error);
@@ -798,6 +1066,15 @@ __global__ void oz_gather_state_kernel(const float* h, const float* l, uint32_t 
   }
 }
 
+// FP64 state ([Mp][kp]) -> LayoutLeft k x M
+__global__ void oz_gather_state64_kernel(const double* x, uint32_t k, uint32_t M, uint32_t kp, double* out) {
+  const size_t n = (size_t)k * M;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t col = (uint32_t)(e / k), row = (uint32_t)(e % k);
+    out[e] = x[(size_t)col * kp + row];
+  }
+}
+
 uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
 
 uint16_t bf16_bits_of_int(double a) {
@@ -807,9 +1084,10 @@ uint16_t bf16_bits_of_int(double a) {
   return (uint16_t)(u >> 16);
 }
 
-// Row-scaled 6-bit slices of a row-major FP64 operator (rows x cols), padded, tiled
-// as [rows_p/128][cols_p/32][slice][128 x 32 BF16 tile]; alpha[r] = row exponent.
-void slice_operator(const double* A, uint32_t rows, uint32_t cols, uint32_t rows_p, uint32_t cols_p,
+// Row-scaled 6-bit slices (S of them) of a row-major FP64 operator (rows x cols),
+// padded, tiled as [rows_p/128][cols_p/32][slice][128 x 32 BF16 tile]; alpha[r] = row
+// exponent.
+void slice_operator(const double* A, uint32_t rows, uint32_t cols, uint32_t rows_p, uint32_t cols_p, int kSlices,
                     std::vector<uint16_t>& out, std::vector<int>& alpha) {
   const uint32_t n_kc = cols_p / kKc;
   out.assign((size_t)rows_p * cols_p * kSlices, 0);
@@ -870,6 +1148,8 @@ struct Batch {
   OzInst* d_inst = nullptr;
   std::vector<void*> owned;  // device buffers of the instances
   // tiling
+  int slices = 6;        // 6: FP32 hi + lo state; 9: FP64 state
+  uint32_t max_nb = 64;  // widest tile of the form
   uint32_t width = 32;
   bool paired = false;  // every tile split over two co-resident CTAs (one tile part per CTA)
   std::string sched_source = "model";
@@ -897,10 +1177,10 @@ uint32_t tile_width_for(uint32_t M, uint32_t W) {
   return nb;
 }
 
-// Modelled cost of one tile per step (arbitrary units): the 2 x 21 slice-pair MMAs of
-// 128 x nb x 16 and the per-element epilogue and re-slicing work.
-double tile_model_cost(const OzInst& in, uint32_t nb) {
-  return (double)nb * ((double)in.kvp * in.ksp * 21.0 / 2048.0 + 15.0 * (in.kvp + in.ksp)) + 2000.0;
+// Modelled cost of one tile per step (arbitrary units): the 2 x S(S+1)/2 slice-pair MMAs
+// of 128 x nb x 16 and the per-element epilogue and re-slicing work.
+double tile_model_cost(const OzInst& in, uint32_t nb, int S) {
+  return (double)nb * ((double)in.kvp * in.ksp * (S * (S + 1) / 2) / 2048.0 + 15.0 * (in.kvp + in.ksp)) + 2000.0;
 }
 
 // Paired tiling is possible when every instance has at least two M-tiles per phase and the
@@ -938,13 +1218,14 @@ void build_tiles(Batch* p, uint32_t W, bool paired = false) {
     std::iota(p->order.begin(), p->order.end(), 0u);
     p->begin.resize(p->ctas + 1);
     std::iota(p->begin.begin(), p->begin.end(), 0u);
-    p->model_makespan = tile_model_cost(p->inst[0], p->tiles[0].nb) / 2;
+    p->model_makespan = tile_model_cost(p->inst[0], p->tiles[0].nb, p->slices) / 2;
     p->sched_source = "paired";
     p->tiles_dirty = true;
     return;
   }
   std::vector<double> cost(p->tiles.size());
-  for (size_t t = 0; t < p->tiles.size(); ++t) cost[t] = tile_model_cost(p->inst[p->tiles[t].inst], p->tiles[t].nb);
+  for (size_t t = 0; t < p->tiles.size(); ++t)
+    cost[t] = tile_model_cost(p->inst[p->tiles[t].inst], p->tiles[t].nb, p->slices);
   lpt_schedule(cost, p->ctas, p->order, p->begin, p->model_makespan);
   p->sched_source = "model";
   p->tiles_dirty = true;
@@ -968,8 +1249,9 @@ int upload(Batch* p, cudaStream_t s) {
 
 }  // namespace
 
-int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
+int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s, int slices) {
   p = nullptr;
+  if (slices != 6 && slices != 9) return fail(SHAW_ERR_INVALID_ARG, "slice count must be 6 or 9");
   if (n == 0 || !d) return fail(SHAW_ERR_INVALID_ARG, "empty batch");
   for (uint32_t i = 0; i < n; ++i) {
     if (d[i].kv == 0 || d[i].ks == 0 || d[i].M == 0 || !d[i].Av || !d[i].As || !d[i].b)
@@ -978,6 +1260,8 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
       return fail(SHAW_ERR_UNSUPPORTED, "the Ozaki tensor-core ROM supports at most 1024 modes per dof");
   }
   Batch* b = new Batch();
+  b->slices = slices;
+  b->max_nb = slices == 6 ? Geo<6>::kMaxNb : Geo<9>::kMaxNb;
   int dev = 0;
   cudaError_t e;
   auto bail = [&](int rc) {
@@ -998,15 +1282,26 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
     b->max_tiles += 2 * ((in.M + 15) / 16);
     std::vector<uint16_t> sv, ss;
     std::vector<int> av, as;
-    slice_operator(d[i].Av, in.kv, in.ks, in.kvp, in.ksp, sv, av);
-    slice_operator(d[i].As, in.ks, in.kv, in.ksp, in.kvp, ss, as);
-    std::vector<float> bh((size_t)in.Mp * in.kvp, 0.f), bl((size_t)in.Mp * in.kvp, 0.f);
+    slice_operator(d[i].Av, in.kv, in.ks, in.kvp, in.ksp, slices, sv, av);
+    slice_operator(d[i].As, in.ks, in.kv, in.ksp, in.kvp, slices, ss, as);
+    std::vector<float> bh, bl;
+    std::vector<double> b64;
+    if (slices == 6) {
+      bh.assign((size_t)in.Mp * in.kvp, 0.f);
+      bl.assign((size_t)in.Mp * in.kvp, 0.f);
+    } else {
+      b64.assign((size_t)in.Mp * in.kvp, 0.0);
+    }
     for (uint32_t c = 0; c < in.M; ++c)
       for (uint32_t r = 0; r < in.kv; ++r) {
         const double v = d[i].b[(size_t)c * in.kv + r];
-        const float h = (float)v;
-        bh[(size_t)c * in.kvp + r] = h;
-        bl[(size_t)c * in.kvp + r] = (float)(v - (double)h);
+        if (slices == 6) {
+          const float h = (float)v;
+          bh[(size_t)c * in.kvp + r] = h;
+          bl[(size_t)c * in.kvp + r] = (float)(v - (double)h);
+        } else {
+          b64[(size_t)c * in.kvp + r] = v;
+        }
       }
     auto alloc = [&](void** ptr, size_t bytes) {
       const cudaError_t r = cudaMalloc(ptr, bytes);
@@ -1018,22 +1313,32 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
     OZ_TRY(alloc((void**)&in.As, ss.size() * 2));
     OZ_TRY(alloc((void**)&in.alpha_v, in.kvp * sizeof(int)));
     OZ_TRY(alloc((void**)&in.alpha_s, in.ksp * sizeof(int)));
-    OZ_TRY(alloc((void**)&in.bh, nv * sizeof(float)));
-    OZ_TRY(alloc((void**)&in.bl, nv * sizeof(float)));
-    OZ_TRY(alloc((void**)&in.xvh, nv * sizeof(float)));
-    OZ_TRY(alloc((void**)&in.xvl, nv * sizeof(float)));
-    OZ_TRY(alloc((void**)&in.xsh, ns * sizeof(float)));
-    OZ_TRY(alloc((void**)&in.xsl, ns * sizeof(float)));
+    if (slices == 6) {
+      OZ_TRY(alloc((void**)&in.bh, nv * sizeof(float)));
+      OZ_TRY(alloc((void**)&in.bl, nv * sizeof(float)));
+      OZ_TRY(alloc((void**)&in.xvh, nv * sizeof(float)));
+      OZ_TRY(alloc((void**)&in.xvl, nv * sizeof(float)));
+      OZ_TRY(alloc((void**)&in.xsh, ns * sizeof(float)));
+      OZ_TRY(alloc((void**)&in.xsl, ns * sizeof(float)));
+    } else {
+      OZ_TRY(alloc((void**)&in.b64, nv * sizeof(double)));
+      OZ_TRY(alloc((void**)&in.xv64, nv * sizeof(double)));
+      OZ_TRY(alloc((void**)&in.xs64, ns * sizeof(double)));
+    }
     OZ_TRY(alloc((void**)&in.expo, 3 * (size_t)in.Mp * sizeof(int)));
     OZ_TRY(cudaMemcpyAsync((void*)in.Av, sv.data(), sv.size() * 2, cudaMemcpyHostToDevice, s));
     OZ_TRY(cudaMemcpyAsync((void*)in.As, ss.data(), ss.size() * 2, cudaMemcpyHostToDevice, s));
     OZ_TRY(cudaMemcpyAsync((void*)in.alpha_v, av.data(), av.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     OZ_TRY(cudaMemcpyAsync((void*)in.alpha_s, as.data(), as.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    OZ_TRY(cudaMemcpyAsync((void*)in.bh, bh.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
-    OZ_TRY(cudaMemcpyAsync((void*)in.bl, bl.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
+    if (slices == 6) {
+      OZ_TRY(cudaMemcpyAsync((void*)in.bh, bh.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
+      OZ_TRY(cudaMemcpyAsync((void*)in.bl, bl.data(), nv * sizeof(float), cudaMemcpyHostToDevice, s));
+    } else {
+      OZ_TRY(cudaMemcpyAsync((void*)in.b64, b64.data(), nv * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
     OZ_TRY(cudaStreamSynchronize(s));  // the host vectors go out of scope
   }
-  b->bscratch = (size_t)(kmax_p / kKc) * bstage_bytes(kMaxNb);
+  b->bscratch = (size_t)(kmax_p / kKc) * kRowBytes * (size_t)slices * b->max_nb;  // one B operand, widest tile
   OZ_TRY(cudaMalloc(&b->d_inst, n * sizeof(OzInst)));
   OZ_TRY(cudaMalloc(&b->d_tiles, b->max_tiles * sizeof(OzTile)));
   OZ_TRY(cudaMalloc(&b->d_order, b->max_tiles * sizeof(uint32_t)));
@@ -1045,13 +1350,14 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
   OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)b->sms * sizeof(unsigned int)));
   OZ_TRY(cudaMalloc(&b->pair_colmax, (size_t)b->sms * 4 * kMaxNb * sizeof(unsigned int)));
 #undef OZ_TRY
-  b->smem = (size_t)kStages * kStageBytes + sizeof(Shared);
+  b->smem = slices == 6 ? (size_t)Geo<6>::kStages * Geo<6>::kStageBytes + sizeof(Shared)
+                         : (size_t)Geo<9>::kStages * Geo<9>::kStageBytes + sizeof(Shared);
   // default tiling: tiles split across CTA pairs where they fit (the widest tiles that
   // still occupy half the SMs, else the narrowest); otherwise 32-column tiles (64 when a
-  // single wide system fills every SM twice)
+  // single wide system fills every SM twice), at most the form's widest tile
   uint32_t pw = 0;
   for (uint32_t W : {16u, 32u, 64u}) {
-    if (!pairing_fits(b, W)) continue;
+    if (W > b->max_nb || !pairing_fits(b, W)) continue;
     uint32_t parts = 0;
     for (const OzInst& in : b->inst) parts += 2 * ((in.M + tile_width_for(in.M, W) - 1) / tile_width_for(in.M, W));
     if (pw == 0 || 2 * parts >= (uint32_t)b->sms) pw = W;
@@ -1059,7 +1365,7 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s) {
   if (pw)
     build_tiles(b, pw, true);
   else
-    build_tiles(b, (n == 1 && d[0].M >= 64u * (uint32_t)b->sms) ? 64u : 32u);
+    build_tiles(b, std::min(b->max_nb, (n == 1 && d[0].M >= 64u * (uint32_t)b->sms) ? 64u : 32u));
   p = b;
   return reset(p, s);
 }
@@ -1098,7 +1404,7 @@ int set_receivers(Batch* p, uint32_t i, const double* rows, uint32_t R, double* 
   const uint32_t Rp = round_up(R, 128);
   std::vector<uint16_t> sl;
   std::vector<int> al;
-  slice_operator(rows, R, in.kv, Rp, in.kvp, sl, al);
+  slice_operator(rows, R, in.kv, Rp, in.kvp, p->slices, sl, al);
   uint8_t* dA = nullptr;
   int* dal = nullptr;
   SHAW_CUDA(cudaMalloc(&dA, sl.size() * 2));
@@ -1119,10 +1425,15 @@ int set_receivers(Batch* p, uint32_t i, const double* rows, uint32_t R, double* 
 int reset(Batch* p, cudaStream_t s) {
   for (const OzInst& in : p->inst) {
     const size_t nv = (size_t)in.Mp * in.kvp, ns = (size_t)in.Mp * in.ksp;
-    SHAW_CUDA(cudaMemsetAsync(in.xvh, 0, nv * sizeof(float), s));
-    SHAW_CUDA(cudaMemsetAsync(in.xvl, 0, nv * sizeof(float), s));
-    SHAW_CUDA(cudaMemsetAsync(in.xsh, 0, ns * sizeof(float), s));
-    SHAW_CUDA(cudaMemsetAsync(in.xsl, 0, ns * sizeof(float), s));
+    if (p->slices == 6) {
+      SHAW_CUDA(cudaMemsetAsync(in.xvh, 0, nv * sizeof(float), s));
+      SHAW_CUDA(cudaMemsetAsync(in.xvl, 0, nv * sizeof(float), s));
+      SHAW_CUDA(cudaMemsetAsync(in.xsh, 0, ns * sizeof(float), s));
+      SHAW_CUDA(cudaMemsetAsync(in.xsl, 0, ns * sizeof(float), s));
+    } else {
+      SHAW_CUDA(cudaMemsetAsync(in.xv64, 0, nv * sizeof(double), s));
+      SHAW_CUDA(cudaMemsetAsync(in.xs64, 0, ns * sizeof(double), s));
+    }
     SHAW_CUDA(cudaMemsetAsync(in.expo, 0x80, 3 * (size_t)in.Mp * sizeof(int), s));  // kNoPrediction
   }
   SHAW_CUDA(cudaMemsetAsync(p->error, 0, sizeof(unsigned int), s));
@@ -1139,14 +1450,14 @@ int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsig
   a.bvt = p->bvt; a.bst = p->bst; a.bscratch = p->bscratch;
   a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error; a.tile_ns = p->tile_ns;
   a.pair_sync = p->pair_sync; a.pair_colmax = p->pair_colmax;
-  SHAW_CUDA(cudaFuncSetAttribute(rom_rank2_ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
+  void (*kern)(OzArgs) = p->slices == 6 ? rom_rank2_ozaki_kernel<6> : rom_rank2_ozaki_kernel<9>;
+  SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
   if (p->paired) {  // the parts of a pair wait on each other: all CTAs resident (cooperative launch)
     SHAW_CUDA(cudaMemsetAsync(p->pair_sync, 0, p->ctas / 2 * sizeof(unsigned int), s));
     void* args[] = {&a};
-    SHAW_CUDA(cudaLaunchCooperativeKernel((const void*)rom_rank2_ozaki_kernel, dim3(p->ctas), dim3(kThreads), args,
-                                          p->smem, s));
+    SHAW_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3(p->ctas), dim3(kThreads), args, p->smem, s));
   } else {
-    rom_rank2_ozaki_kernel<<<p->ctas, kThreads, p->smem, s>>>(a);
+    kern<<<p->ctas, kThreads, p->smem, s>>>(a);
   }
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
@@ -1165,14 +1476,21 @@ int check(Batch* p, cudaStream_t s) {
 int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs) {
   if (i >= p->inst.size()) return fail(SHAW_ERR_INVALID_ARG, "instance index out of range");
   const OzInst& in = p->inst[i];
-  oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xvh, in.xvl, in.kv, in.M, in.kvp, dxv);
-  oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xsh, in.xsl, in.ks, in.M, in.ksp, dxs);
+  if (p->slices == 6) {
+    oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xvh, in.xvl, in.kv, in.M, in.kvp, dxv);
+    oz_gather_state_kernel<<<256, 256, 0, s>>>(in.xsh, in.xsl, in.ks, in.M, in.ksp, dxs);
+  } else {
+    oz_gather_state64_kernel<<<256, 256, 0, s>>>(in.xv64, in.kv, in.M, in.kvp, dxv);
+    oz_gather_state64_kernel<<<256, 256, 0, s>>>(in.xs64, in.ks, in.M, in.ksp, dxs);
+  }
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
 }
 
 int set_tiling(Batch* p, uint32_t width, bool paired) {
   if (width != 16 && width != 32 && width != 64) return fail(SHAW_ERR_INVALID_ARG, "tile width must be 16, 32 or 64");
+  if (width > p->max_nb)
+    return fail(SHAW_ERR_UNSUPPORTED, "tiles of the 9-slice (FP64-grade) form are at most 16 columns wide");
   if (paired && !pairing_fits(p, width))
     return fail(SHAW_ERR_UNSUPPORTED, "paired tiles need >= 256 modes per dof and two CTAs per tile on the SMs");
   build_tiles(p, width, paired);
@@ -1211,9 +1529,10 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
   report.clear();
   do {
     float warm = 0.f;
-    build_tiles(p, 32);
+    build_tiles(p, std::min(32u, p->max_nb));
     if ((rc = timed(warm))) break;  // first launch: module load, caches
     for (uint32_t W : {16u, 32u, 64u}) {
+      if (W > p->max_nb) continue;
       build_tiles(p, W);
       float ms_model = 0.f;
       if ((rc = timed(ms_model))) break;
@@ -1239,7 +1558,7 @@ int tune(Batch* p, cudaStream_t s, double dt, unsigned long long trial_steps, st
     }
     if (rc) break;
     for (uint32_t W : {16u, 32u, 64u}) {  // tiles split over CTA pairs, where they fit
-      if (!pairing_fits(p, W)) continue;
+      if (W > p->max_nb || !pairing_fits(p, W)) continue;
       build_tiles(p, W, true);
       float ms_pair = 0.f;
       if ((rc = timed(ms_pair))) break;

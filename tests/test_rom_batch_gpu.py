@@ -215,3 +215,53 @@ def test_batch_tiling_errors(shaw):
         bt.set_tiling(32)
     assert e.value.code == shaw.ERR_UNSUPPORTED
     bt.close()
+
+
+def test_batch_ozaki_fp64_form(shaw):
+    """The FP64-grade tensor-core batch: every instance within 1e-12 of the FP64 batch,
+    bit for bit the single-system kernel (exact accumulation: independent of the tiling,
+    paired or not), seismograms within 1e-12; tiles are at most 16 columns wide."""
+    insts = _instances(14)
+    n, dt = 300, 0.5
+    rng = np.random.default_rng(15)
+    rows = [rng.standard_normal((R, d["rom_jvp"].shape[0])) for R, d in zip((3, 130, 1, 7, 20), insts)]
+    res = {}
+    for p in (shaw.FP64, shaw.OZAKI_FP64):
+        bt = shaw.RomBatch(insts, precision=p)
+        for i in range(len(insts)):
+            bt.set_snapshots(i, 25, 30, n)
+            bt.set_receivers(i, rows[i], 4, n)
+        bt.run(dt, n)
+        res[p] = [(bt.get_state(i), bt.snapshots(i), bt.seismogram(i)) for i in range(len(insts))]
+        if p == shaw.OZAKI_FP64:
+            with pytest.raises(shaw.ShawError) as e:
+                bt.set_tiling(32)
+            assert e.value.code == shaw.ERR_UNSUPPORTED
+        bt.close()
+    for i in range(len(insts)):
+        (x64, s64, g64), (xoz, soz, goz) = res[shaw.FP64][i], res[shaw.OZAKI_FP64][i]
+        errs = [relerr(xoz[0], x64[0]), relerr(xoz[1], x64[1]), relerr(soz[0], s64[0]), relerr(soz[1], s64[1]),
+                relerr(goz, g64)]
+        assert max(errs) <= 1e-12, (i, errs)
+    for i, d in enumerate(insts):
+        r = shaw.Rom(d["rom_jvp"], d["rom_jsp"], d["b"], rank=2, precision=shaw.OZAKI_FP64)
+        r.set_signals(d["kind"], d["period"], d["delay"])
+        r.run(dt, n)
+        a = r.get_state()
+        r.close()
+        assert np.array_equal(a[0], res[shaw.OZAKI_FP64][i][0][0]) and np.array_equal(a[1], res[shaw.OZAKI_FP64][i][0][1])
+
+
+def test_batch_ozaki_fp64_paired_bitwise(shaw):
+    insts = _instances(16, shapes=[(384, 256, 40), (512, 512, 20)])
+    out = {}
+    for paired in (False, True):
+        bt = shaw.RomBatch(insts, precision=shaw.OZAKI_FP64)
+        bt.set_tiling(16, paired=paired)
+        bt.advance(0.5, 17)
+        bt.advance(0.5, 43)
+        bt.synchronize()
+        out[paired] = [bt.get_state(i) for i in range(len(insts))]
+        bt.close()
+    for i in range(len(insts)):
+        assert np.array_equal(out[False][i][0], out[True][i][0]) and np.array_equal(out[False][i][1], out[True][i][1])

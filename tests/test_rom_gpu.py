@@ -296,3 +296,56 @@ def test_rank2_tf32x3_receivers_unsupported(shaw):
         r.set_receivers(np.ones((3, 128)), 1, 10)
     assert e.value.code == shaw.ERR_UNSUPPORTED
     r.close()
+
+
+# ---- SHAW_OZAKI_FP64: 9 six-bit slices, FP64 state: held to the FP64 bar -----------------
+
+@pytest.mark.parametrize("M", [1, 5, 16])
+def test_rank2_ozaki_fp64_matches_oracle(shaw, oracle, setup, M):
+    """The FP64-grade tensor-core form against the oracle at the FP64 path's bar (1e-12):
+    snapshots, final states and the in-loop seismogram."""
+    rng = np.random.default_rng(M)
+    specs = [(float(rng.uniform(200, 1500)), float(rng.uniform(0, 180))) for _ in range(M)]
+    pv, av, as_, b = _rom_inputs(shaw, setup, 48, specs)
+    periods = rng.uniform(30, 90, M)
+    n, dt = 400, 1.0
+    r = shaw.Rom(av, as_, b, rank=2, precision=shaw.OZAKI_FP64)
+    r.set_signals("gaussDer", periods, 100.0)
+    r.set_snapshots(4, 8, n)
+    rcv = [setup[0].map_receiver(a) for a in (20, 80, 160)]
+    r.set_receivers(pv[rcv, :], 2, n)
+    r.run(dt, n)
+    ref = oracle.rom_run(av, as_, b, n, dt, [2] * M, periods, [100.0] * M, 4, 8)
+    svp, ssp = r.snapshots()
+    assert relerr(svp, ref["snaps_vp"]) <= 1e-12 and relerr(ssp, ref["snaps_sp"]) <= 1e-12
+    xv, xs = r.get_state()
+    assert relerr(xv, ref["final_vp"]) <= 1e-12 and relerr(xs, ref["final_sp"]) <= 1e-12
+    seis = r.seismogram()
+    expect = np.einsum("rk,ktm->rtm", pv[rcv, :], ref["snaps_vp"])
+    assert relerr(seis[:, 1::2, :], expect) <= 1e-12
+    r.close()
+
+
+@pytest.mark.parametrize("kv,ks,M", [(100, 72, 45), (256, 256, 300), (512, 512, 64), (1024, 640, 40)])
+def test_rank2_ozaki_fp64_long_runs_within_1e12(shaw, kv, ks, M):
+    """2000 steps against the FP64 (DGEMM) path: states and snapshots within 1e-12."""
+    ((xv64, xs64), (sv64, ss64)), ((xvoz, xsoz), (svoz, ssoz)) = _fp64_vs_mixed(
+        shaw, shaw.OZAKI_FP64, kv, ks, M, 2000, 0.5, kv + M + 1, freq=50, smax=0.2)
+    errs = [relerr(a, b) for a, b in ((xvoz, xv64), (xsoz, xs64), (svoz, sv64), (ssoz, ss64))]
+    assert max(errs) <= 1e-12, errs
+
+
+def test_rank2_ozaki_fp64_advance_in_pieces(shaw):
+    av, as_, _ = stable_system(256, 19)
+    b = np.random.default_rng(19).standard_normal((256, 40)) * 1e-3
+    r = shaw.Rom(av * 0.2, as_ * 0.2, b, rank=2, precision=shaw.OZAKI_FP64)
+    r.set_signals("ricker", 40.0, 20.0)
+    r.run(0.5, 100)
+    whole = r.get_state()
+    r.reset()
+    r.advance(0.5, 31)
+    r.advance(0.5, 69)
+    r.synchronize()
+    part = r.get_state()
+    assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
+    r.close()
