@@ -79,8 +79,8 @@ constexpr uint32_t kTmemCols = 512;
 template <int S>
 struct Geo {
   static constexpr uint32_t kABytes = S * kATile;                              // 48 / 72 KB
-  static constexpr uint32_t kMaxNb = S == 6 ? 64u : 16u;
-  static constexpr uint32_t kStageBytes = kABytes + S * kMaxNb * kRowBytes;  // 72 / 81 KB
+  static constexpr uint32_t kMaxNb = S == 6 ? 64u : 32u;
+  static constexpr uint32_t kStageBytes = kABytes + S * kMaxNb * kRowBytes;  // 72 / 90 KB
   static constexpr int kStages = S == 6 ? 3 : 2;
   __host__ __device__ static constexpr uint32_t bstage_bytes(uint32_t nb) { return S * nb * kRowBytes; }
   __host__ __device__ static constexpr uint32_t acc_buffers(uint32_t nb) { return (S * nb <= 256) ? 2u : 1u; }
@@ -464,6 +464,62 @@ __device__ __forceinline__ void load_combine8_fp64(uint32_t tcols, uint32_t nb, 
   }
 }
 
+// With one accumulator set (9 nb > 256, i.e. nb = 32) the columns after it, [9 nb, 13 nb),
+// stage the combined pairs of one M-tile as raw FP64 words (yH at +2j, yL at +2nb+2j):
+// the epilogue drains the accumulator, hands it back to the MMA issuer and finishes the
+// state update while the next M-tile's MMAs run.
+__device__ __forceinline__ void words_of(const double* y, float* w) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const long long b = __double_as_longlong(y[i]);
+    w[2 * i] = __int_as_float((int)b);
+    w[2 * i + 1] = __int_as_float((int)(b >> 32));
+  }
+}
+__device__ __forceinline__ void doubles_of(const float* w, double* y) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    y[i] = __longlong_as_double(((long long)__float_as_int(w[2 * i + 1]) << 32) |
+                                (unsigned int)__float_as_int(w[2 * i]));
+}
+__device__ __forceinline__ bool stage_accumulator_fp64(uint32_t tcols, uint32_t spare, uint32_t nb, int q,
+                                                       uint32_t jbeg, uint32_t jend, uint64_t* acc_empty) {
+  for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+    double yH[8], yL[8];
+    load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+    float w[8];
+    words_of(yH, w);
+    tmem_st8(spare + 2 * j0, w);
+    words_of(yH + 4, w);
+    tmem_st8(spare + 2 * j0 + 8, w);
+    words_of(yL, w);
+    tmem_st8(spare + 2 * nb + 2 * j0, w);
+    words_of(yL + 4, w);
+    tmem_st8(spare + 2 * nb + 2 * j0 + 8, w);
+  }
+  tmem_wait_st();
+  tc_fence_before();
+  mbar_arrive(acc_empty);
+  return true;
+}
+__device__ __forceinline__ void fetch_combined8_fp64(bool staged, uint32_t tcols, uint32_t spare, uint32_t nb, int q,
+                                                     uint32_t j0, double* yH, double* yL) {
+  if (staged) {
+    float w[4][8];
+    tmem_ld8(spare + 2 * j0, w[0]);
+    tmem_ld8(spare + 2 * j0 + 8, w[1]);
+    tmem_ld8(spare + 2 * nb + 2 * j0, w[2]);
+    tmem_ld8(spare + 2 * nb + 2 * j0 + 8, w[3]);
+    tmem_wait_ld();
+    doubles_of(w[0], yH);
+    doubles_of(w[1], yH + 4);
+    doubles_of(w[2], yL);
+    doubles_of(w[3], yL + 4);
+  } else {
+    load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+  }
+}
+
 // x * 2^(54 - beta) rounded to an integer, from the bits of x (no FP64 arithmetic): the
 // 54-bit fixed-point value of x / 2^beta for |x| < 2^beta.  Values at or above 2^beta
 // give meaningless results; the caller re-slices such columns exactly.
@@ -705,9 +761,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const uint32_t part = sh->tile.pinfo & 1u, slot = sh->tile.pinfo >> 2;
     const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
     const uint32_t bbytes = G::bstage_bytes(nb);                                   // B stage bytes
-    // single accumulator set: stage it in TMEM (6-slice form, nb = 64; the 9-slice form
-    // keeps tiles of 16 columns and two sets)
-    const bool stage = S == 6 && G::acc_buffers(nb) == 1;
+    // single accumulator set (6-slice form with nb = 64, 9-slice form with nb = 32):
+    // stage its combined values in the TMEM columns after it
+    const bool stage = G::acc_buffers(nb) == 1;
     const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + S * nb;
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
     float* const xvh = S == 6 ? in.xvh + (size_t)col0 * in.kvp : nullptr;
@@ -853,7 +909,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       });
       } else {
       gemm_phase<S>(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t*) {
+                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row] - 60;
         uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
@@ -868,7 +925,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             f[jj] = b64[si];
           }
           double yH[8], yL[8];
-          load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+          fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
@@ -887,7 +944,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
           note_max8_keys(sh, j0, key);
         }
-        return false;
+        return staged;
       });
       }
       if (paired) exchange();
@@ -988,7 +1045,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       });
       } else {
       gemm_phase<S>(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t*) {
+                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row] - 60;
         uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
@@ -999,7 +1057,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) x[jj] = xs64[(size_t)(j0 + jj) * in.ksp + row];
           double yH[8], yL[8];
-          load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+          fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
@@ -1016,7 +1074,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
           note_max8_keys(sh, j0, key);
         }
-        return false;
+        return staged;
       });
       }
       if (paired) exchange();
@@ -1490,7 +1548,7 @@ int get_state(Batch* p, uint32_t i, cudaStream_t s, double* dxv, double* dxs) {
 int set_tiling(Batch* p, uint32_t width, bool paired) {
   if (width != 16 && width != 32 && width != 64) return fail(SHAW_ERR_INVALID_ARG, "tile width must be 16, 32 or 64");
   if (width > p->max_nb)
-    return fail(SHAW_ERR_UNSUPPORTED, "tiles of the 9-slice (FP64-grade) form are at most 16 columns wide");
+    return fail(SHAW_ERR_UNSUPPORTED, "tiles of the 9-slice (FP64-grade) form are at most 32 columns wide");
   if (paired && !pairing_fits(p, width))
     return fail(SHAW_ERR_UNSUPPORTED, "paired tiles need >= 256 modes per dof and two CTAs per tile on the SMs");
   build_tiles(p, width, paired);

@@ -22,7 +22,7 @@ struct Batch;
 // Slice every instance's operators into row-scaled BF16 slices, allocate the states, and
 // pick the default tiling.  slices = 6: 36-bit products, FP32 hi + lo states
 // (SHAW_MIXED_OZAKI_BF16); slices = 9: 54-bit products and FP64 states, FP64-grade
-// results (SHAW_OZAKI_FP64), tiles of 16 columns.
+// results (SHAW_OZAKI_FP64), tiles of at most 32 columns.
 int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s, int slices = 6);
 // Per-column signals of instance i (device arrays of M entries, owned by the caller).
 int set_signals(Batch* p, uint32_t i, const int* kind, const double* period, const double* delay);

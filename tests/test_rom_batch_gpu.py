@@ -220,7 +220,7 @@ def test_batch_tiling_errors(shaw):
 def test_batch_ozaki_fp64_form(shaw):
     """The FP64-grade tensor-core batch: every instance within 1e-12 of the FP64 batch,
     bit for bit the single-system kernel (exact accumulation: independent of the tiling,
-    paired or not), seismograms within 1e-12; tiles are at most 16 columns wide."""
+    paired or not), seismograms within 1e-12; tiles are at most 32 columns wide."""
     insts = _instances(14)
     n, dt = 300, 0.5
     rng = np.random.default_rng(15)
@@ -235,7 +235,7 @@ def test_batch_ozaki_fp64_form(shaw):
         res[p] = [(bt.get_state(i), bt.snapshots(i), bt.seismogram(i)) for i in range(len(insts))]
         if p == shaw.OZAKI_FP64:
             with pytest.raises(shaw.ShawError) as e:
-                bt.set_tiling(32)
+                bt.set_tiling(64)
             assert e.value.code == shaw.ERR_UNSUPPORTED
         bt.close()
     for i in range(len(insts)):
@@ -252,12 +252,15 @@ def test_batch_ozaki_fp64_form(shaw):
         assert np.array_equal(a[0], res[shaw.OZAKI_FP64][i][0][0]) and np.array_equal(a[1], res[shaw.OZAKI_FP64][i][0][1])
 
 
-def test_batch_ozaki_fp64_paired_bitwise(shaw):
+@pytest.mark.parametrize("width", [16, 32])
+def test_batch_ozaki_fp64_paired_bitwise(shaw, width):
+    """Tiles of 16 columns (two accumulator sets) and 32 columns (one set staged in TMEM),
+    whole or split across CTA pairs, advanced in pieces: the same numbers bit for bit."""
     insts = _instances(16, shapes=[(384, 256, 40), (512, 512, 20)])
     out = {}
     for paired in (False, True):
         bt = shaw.RomBatch(insts, precision=shaw.OZAKI_FP64)
-        bt.set_tiling(16, paired=paired)
+        bt.set_tiling(width, paired=paired)
         bt.advance(0.5, 17)
         bt.advance(0.5, 43)
         bt.synchronize()
