@@ -46,7 +46,8 @@ def parse():
     p.add_argument("--forcings", type=int, default=M)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extra", action="store_true", help="skip the other configurations' lines")
-    p.add_argument("--profile-rom", default=None, choices=["ozaki", "tf32x3", "fp64", "rank1-fp64", "rank1-mixed"],
+    p.add_argument("--profile-rom", default=None,
+                   choices=["ozaki", "ozaki-fp64", "tf32x3", "fp64", "rank1-fp64", "rank1-mixed"],
                    help="only run the rank-2 ROM (k=512, M=4096) or the rank-1 ROM (k=256, 181 receivers) "
                         "for --steps steps, for profiler captures")
     p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32"],
@@ -285,7 +286,7 @@ def extra_workloads(np, torch, shaw):
     b = forcing_vectors(k, [mesh.map_source(float(d), 0.0) for d in depths])
     rows = basis["phi_v"][rcv, :k]
     res = {}
-    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.MIXED_TF32X3):
+    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.OZAKI_FP64, shaw.MIXED_TF32X3):
         r = shaw.Rom(av, as_, b, rank=2, precision=prec)
         r.set_signals("gaussDer", periods, 180.0)
         r.set_snapshots(n // 4, n // 4, n)
@@ -301,11 +302,16 @@ def extra_workloads(np, torch, shaw):
     t64 = res[shaw.FP64][0]
     out["rom_rank2_k512_M4096"] = {
         "metric": "ROM forcing-steps/s", "steps": n, "fp64": M * n / t64,
-        "ozaki_bf16": M * n / res[shaw.MIXED_OZAKI_BF16][0], "tf32x3": M * n / res[shaw.MIXED_TF32X3][0],
-        "speedup_ozaki": t64 / res[shaw.MIXED_OZAKI_BF16][0], "speedup_tf32x3": t64 / res[shaw.MIXED_TF32X3][0],
+        "ozaki_bf16": M * n / res[shaw.MIXED_OZAKI_BF16][0], "ozaki_fp64": M * n / res[shaw.OZAKI_FP64][0],
+        "tf32x3": M * n / res[shaw.MIXED_TF32X3][0],
+        "speedup_ozaki": t64 / res[shaw.MIXED_OZAKI_BF16][0], "speedup_ozaki_fp64": t64 / res[shaw.OZAKI_FP64][0],
+        "speedup_tf32x3": t64 / res[shaw.MIXED_TF32X3][0],
         "seismogram_rel_err_ozaki": _relerr(np, res[shaw.MIXED_OZAKI_BF16][1], res[shaw.FP64][1]),
+        "seismogram_rel_err_ozaki_fp64": _relerr(np, res[shaw.OZAKI_FP64][1], res[shaw.FP64][1]),
+        "state_rel_err_ozaki_fp64": _relerr(np, res[shaw.OZAKI_FP64][2], res[shaw.FP64][2]),
         "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
+        "algorithmic_tflops_ozaki_fp64": 4.0 * k * k * M * n / res[shaw.OZAKI_FP64][0] / 1e12,
         "cpu_oracle": rom_cpu_oracle(np, av, as_, b[:, :64], 60, dt, periods[:64]),
         "basis": "leading 512 modes of the POD basis of config 3"}
     out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
@@ -416,7 +422,7 @@ def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_i
     dtr, n64, n_oz, n_cmp = dt, 6, 120, 6
     rows = {i: basis["phi_v"][rcv, :int(ks[i])] for i in range(n_inst)}
     res = {}
-    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16):
+    for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.OZAKI_FP64):
         bt = shaw.RomBatch(insts, precision=prec)
         report = bt.tune(dtr, 4) if prec != shaw.FP64 else ""
         bt.reset()
@@ -435,12 +441,15 @@ def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_i
         seis = [rows[i] @ bt.get_state(i)[0] for i in range(n_inst)]
         res[prec] = dict(t=t, n=n, seis=seis, describe=bt.describe(), report=report, launches=launches)
         bt.close()
-    r64, roz = res[shaw.FP64], res[shaw.MIXED_OZAKI_BF16]
+    r64, roz, rof = res[shaw.FP64], res[shaw.MIXED_OZAKI_BF16], res[shaw.OZAKI_FP64]
     err = max(_relerr(np, a, b) for a, b in zip(roz["seis"], r64["seis"]))
-    v64, voz = cols * r64["n"] / r64["t"], cols * roz["n"] / roz["t"]
+    err_f = max(_relerr(np, a, b) for a, b in zip(rof["seis"], r64["seis"]))
+    v64, voz, vof = cols * r64["n"] / r64["t"], cols * roz["n"] / roz["t"], cols * rof["n"] / rof["t"]
     return {"metric": "ROM forcing-steps/s", "instances": n_inst, "total_forcings": cols,
             "k_range": [int(ks.min()), int(ks.max())], "M_range": [int(Ms.min()), int(Ms.max())],
             "fp64": v64, "ozaki_bf16": voz, "speedup_ozaki": voz / v64,
+            "ozaki_fp64": vof, "speedup_ozaki_fp64": vof / v64, "seismogram_rel_err_ozaki_fp64": err_f,
+            "algorithmic_tflops_ozaki_fp64": flops * rof["n"] / rof["t"] / 1e12, "tiling_ozaki_fp64": rof["describe"],
             "fp64_steps": r64["n"], "ozaki_steps": roz["n"], "ozaki_launches": roz["launches"],
             "algorithmic_tflops_fp64": flops * r64["n"] / r64["t"] / 1e12,
             "algorithmic_tflops_ozaki": flops * roz["n"] / roz["t"] / 1e12,
@@ -646,7 +655,8 @@ def main():
             r.set_signals("gaussDer", 60.0, 180.0)
             r.set_receivers(rng.standard_normal((181, 256)) / 16.0, 1, args.steps)
         else:
-            prec = {"ozaki": shaw.MIXED_OZAKI_BF16, "tf32x3": shaw.MIXED_TF32X3, "fp64": shaw.FP64}[args.profile_rom]
+            prec = {"ozaki": shaw.MIXED_OZAKI_BF16, "ozaki-fp64": shaw.OZAKI_FP64, "tf32x3": shaw.MIXED_TF32X3,
+                    "fp64": shaw.FP64}[args.profile_rom]
             av, as_ = stable_rom(np, 512, 7, 0.004, 0.2)
             rng = np.random.default_rng(8)
             r = shaw.Rom(av, as_, rng.standard_normal((512, 4096)) * 1e-3, rank=2, precision=prec)
