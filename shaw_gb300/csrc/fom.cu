@@ -185,10 +185,18 @@ __device__ __forceinline__ void apply_forcing(V& v, const FomArgs& a, uint32_t c
 }
 
 // updateVelocity (fom_update_kernels.hpp:60-90 rank-1, :132-167 rank-2) for one step.
+// Programmatic dependent launch: the two half-step kernels are launched so that the next
+// one may be scheduled while this one drains.  Each waits for the complete previous
+// grid (and its memory) before touching any state, and releases its dependents once
+// its own stores are issued.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_next_grid() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename T, int VEC>
 __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint32_t k_local,
                                                                 unsigned long long host_step) {
   using V = VecT<T, VEC>;
+  wait_prior_grid();
   T* const xv = static_cast<T*>(a.xv);
   const T* const xs = static_cast<const T*>(a.xs);
   const T* const cvp = static_cast<const T*>(a.cvp);
@@ -223,6 +231,7 @@ __global__ void __launch_bounds__(kThreads) fom_velocity_kernel(FomArgs a, uint3
   // forcing: the thread owning (src[m], m) adds it, evaluating the signal at t_{n-1}
   apply_forcing<typename V::type, VEC>(v, a, c, p, k_local, host_step);
   V::st(xp, v);
+  allow_next_grid();
 }
 
 // updateStress (fom_update_kernels.hpp:93-104, :170-181) + fused receiver gather.
@@ -230,6 +239,7 @@ template <typename T, int VEC>
 __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_t k_local,
                                                               unsigned long long host_step) {
   using V = VecT<T, VEC>;
+  wait_prior_grid();
   const T* const xv = static_cast<const T*>(a.xv);
   T* const xs = static_cast<T*>(a.xs);
   const T* const csp = static_cast<const T*>(a.csp);
@@ -273,6 +283,7 @@ __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_
   fma_into(s, cA, V::ld(xv + (size_t)gA * a.M + off));
   fma_into(s, cB, V::ld(xv + (size_t)gB * a.M + off));
   V::st(sp, s);
+  allow_next_grid();
 }
 
 // y = Jvp x (Jvp: nvp x nsp) or y = Jsp x (nsp x nvp) on column-major multivectors
@@ -433,21 +444,34 @@ FomArgs make_args(const H* h, double dt) {
   return a;
 }
 
+// A half-step kernel on h's stream with programmatic stream serialization.
+template <typename K>
+int launch_half_step(H* h, K kern, uint32_t blocks, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
+  cudaLaunchConfig_t cfg;
+  std::memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a, k_local, host_step));
+  h->launches++;
+  return SHAW_OK;
+}
+
 int launch_velocity(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
   const uint32_t blocks = (a.vp_items + kThreads - 1) / kThreads;
   const uint32_t vec = h->M / a.chunks;
   if (h->esz == sizeof(float)) {
-    if (vec == 4) fom_velocity_kernel<float, 4><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-    else if (vec == 2) fom_velocity_kernel<float, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-    else fom_velocity_kernel<float, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  } else if (vec == 2) {
-    fom_velocity_kernel<double, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  } else {
-    fom_velocity_kernel<double, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    if (vec == 4) return launch_half_step(h, fom_velocity_kernel<float, 4>, blocks, a, k_local, host_step);
+    if (vec == 2) return launch_half_step(h, fom_velocity_kernel<float, 2>, blocks, a, k_local, host_step);
+    return launch_half_step(h, fom_velocity_kernel<float, 1>, blocks, a, k_local, host_step);
   }
-  h->launches++;
-  SHAW_CUDA(cudaGetLastError());
-  return SHAW_OK;
+  if (vec == 2) return launch_half_step(h, fom_velocity_kernel<double, 2>, blocks, a, k_local, host_step);
+  return launch_half_step(h, fom_velocity_kernel<double, 1>, blocks, a, k_local, host_step);
 }
 
 int launch_stress(H* h, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
@@ -455,17 +479,12 @@ int launch_stress(H* h, const FomArgs& a, uint32_t k_local, unsigned long long h
   if (a.R && a.seis_freq) blocks += (a.R * a.M + kThreads - 1) / kThreads;
   const uint32_t vec = h->M / a.chunks;
   if (h->esz == sizeof(float)) {
-    if (vec == 4) fom_stress_kernel<float, 4><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-    else if (vec == 2) fom_stress_kernel<float, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-    else fom_stress_kernel<float, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  } else if (vec == 2) {
-    fom_stress_kernel<double, 2><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
-  } else {
-    fom_stress_kernel<double, 1><<<blocks, kThreads, 0, h->stream>>>(a, k_local, host_step);
+    if (vec == 4) return launch_half_step(h, fom_stress_kernel<float, 4>, blocks, a, k_local, host_step);
+    if (vec == 2) return launch_half_step(h, fom_stress_kernel<float, 2>, blocks, a, k_local, host_step);
+    return launch_half_step(h, fom_stress_kernel<float, 1>, blocks, a, k_local, host_step);
   }
-  h->launches++;
-  SHAW_CUDA(cudaGetLastError());
-  return SHAW_OK;
+  if (vec == 2) return launch_half_step(h, fom_stress_kernel<double, 2>, blocks, a, k_local, host_step);
+  return launch_half_step(h, fom_stress_kernel<double, 1>, blocks, a, k_local, host_step);
 }
 
 int ensure_folded(H* h, double dt) {
