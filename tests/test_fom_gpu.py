@@ -119,21 +119,33 @@ def test_input_file_driver_matches_reference_golds(shaw, oracle, case, tmp_path)
     assert (tmp_path / "coords_vp.txt").exists() and (tmp_path / "coords_sp.txt").exists()
 
 
-def test_graph_replay_equals_direct_launches(shaw, oracle):
-    m, om = meshes(shaw, oracle, "fullMesh21x51")
-    n = 200  # > one 64-step graph chunk, with a ragged tail
+@pytest.mark.parametrize("grid", ["small", "large"])
+def test_graph_replay_equals_direct_launches(shaw, oracle, grid):
+    """Without snapshots a run of >= 64 steps replays CUDA-graph chunks (half-step kernels
+    chained by programmatic dependent launch); with snapshots, per-step launches.
+    Seismograms and final states agree bit for bit, on a small and a large grid."""
+    if grid == "small":
+        m, _ = meshes(shaw, oracle, "fullMesh21x51")
+        n, M, dt = 200, 4, 1.0  # > one 64-step chunk, with a ragged tail
+    else:
+        m = shaw.Mesh.generate(1000, 2000)
+        m.set_material("unilayer", CFG_MATERIAL)
+        n, M = 70, 4
+        dt = 0.25 * min(m.info[5], m.info[4] * m.info[2]) / (np.sqrt(2.0) * 7300.0)
     rcv = [m.map_receiver(a) for a in (10, 45, 90, 170)]
     out = []
     for snaps in (False, True):
-        f = shaw.Fom(m, 2, 4)
+        f = shaw.Fom(m, 2, M)
         f.set_sources([m.map_source(d, 45.0) for d in (300.0, 600.0, 900.0, 1200.0)], "ricker", 40.0, 10.0)
         f.set_receivers(rcv, 2, n)
         if snaps:
-            f.set_snapshots(50, 50, n)  # snapshots force per-step launches
-        f.run(1.0, n)
-        out.append(f.seismogram())
+            f.set_snapshots(35 if grid == "large" else 50, 35 if grid == "large" else 50, n)  # per-step launches
+        f.run(dt, n)
+        out.append((f.seismogram(), f.get_state()))
         f.close()
-    assert np.array_equal(out[0], out[1])
+    assert np.max(np.abs(out[0][1][0])) > 0  # (the large grid's surface receivers are still silent)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1][0], out[1][1][0]) and np.array_equal(out[0][1][1], out[1][1][1])
 
 
 def test_generated_large_mesh_rank2(shaw, oracle):
