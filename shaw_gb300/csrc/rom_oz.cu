@@ -201,6 +201,36 @@ __device__ __forceinline__ void acc_next(uint32_t nbuf, uint32_t (&uses)[2], uin
 // Instruction-descriptor bit: B operand MN-major ("transpose B").
 constexpr uint32_t kIdescBMnMajor = 1u << 16;
 
+// The MMAs of one 32-wide K stage for tiles of NB columns.  The B slices of a stage are
+// stacked along N (slice t = rows t*NB ..), and the diagonal accumulators along TMEM
+// columns (diagonal d = columns d*NB ..), so operator slice sa times the state slices
+// tb = 0 .. S-1-sa is ONE MMA of N = (S-sa)*NB whose output columns start at diagonal
+// sa: S MMAs per K-step instead of S(S+1)/2 pair MMAs, each A slice read from shared
+// memory once.  N is capped at 256 (split into two MMAs where needed).  The first MMA
+// of a tile (sa = 0 covers every diagonal) starts the accumulation.  Descriptors of the
+// stage's first A / B slice; the others differ only in the start-address field (16-byte
+// units, no carry: shared addresses < 256 KB).
+template <int S, uint32_t NB>
+__device__ __forceinline__ void issue_stage(uint32_t dcol, uint32_t abase, uint32_t bbase, bool first_chunk) {
+  const uint64_t adesc0 = smem_desc(abase, 128, 512);
+  const uint64_t bdesc0 = smem_desc(bbase, 16u * S * NB, 128);  // MN-major state slices
+  constexpr uint32_t kTake = 256u / NB;
+#pragma unroll
+  for (uint32_t k = 0; k < kKc / 16; ++k) {
+#pragma unroll
+    for (int sa = 0; sa < S; ++sa) {
+      const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
+      const uint32_t acc = (!first_chunk || k > 0 || sa > 0) ? 1u : 0u;
+#pragma unroll
+      for (uint32_t tb = 0; tb < (uint32_t)(S - sa); tb += kTake) {
+        const uint32_t take = ((uint32_t)(S - sa) - tb) < kTake ? ((uint32_t)(S - sa) - tb) : kTake;
+        const uint64_t bdesc = bdesc0 + ((tb * 16u * NB + k * 32u * S * NB) >> 4);
+        mma_f16(dcol + (sa + tb) * NB, adesc, bdesc, idesc_bf16(take * NB) | kIdescBMnMajor, acc);
+      }
+    }
+  }
+}
+
 // One GEMM phase: for every 128-row M-tile, D_d = sum over K of the slice pairs on
 // diagonal d into an accumulator set; the epilogue `epi(mt, tmem_cols)` runs on warps
 // 4..11 while the MMAs of the next M-tile fill the other set.
@@ -237,33 +267,15 @@ __device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const ui
         if (!mbar_wait(&sh->full[s], ph)) { raise(sh, err, 4u); break; }
         tc_fence_after();
         const uint32_t abase = smem_u32(stages + (size_t)s * kStageBytes);
-        // descriptors of the stage's first A / B slice; the others differ only in the
-        // start-address field (16-byte units, no carry: shared addresses < 256 KB)
-        const uint64_t adesc0 = smem_desc(abase, 128, 512);
-        const uint64_t bdesc0 = smem_desc(abase + kABytes, 16u * S * nb, 128);  // MN-major state slices
-        // The B slices of a stage are stacked along N (slice t = rows t*nb ..), and the
-        // diagonal accumulators along TMEM columns (diagonal d = columns d*nb ..), so
-        // operator slice sa times the state slices tb = 0 .. S-1-sa is ONE MMA of
-        // N = (S-sa)*nb whose output columns start at diagonal sa: S MMAs per K-step
-        // instead of S(S+1)/2 pair MMAs, each A slice read from shared memory once.  N
-        // is capped at 256 (split into two MMAs where needed).  The first MMA of a tile
-        // (sa = 0 covers every diagonal) starts the accumulation.
-#pragma unroll
-        for (uint32_t k = 0; k < kKc / 16; ++k) {
-#pragma unroll
-          for (int sa = 0; sa < S; ++sa) {
-            const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
-            const uint32_t acc = (c > 0 || k > 0 || sa > 0) ? 1u : 0u;
-            uint32_t tb = 0, left = (uint32_t)(S - sa);
-            while (left) {
-              const uint32_t take = min(left, 256u / nb);
-              const uint64_t bdesc = bdesc0 + ((tb * 16u * nb + k * 32u * S * nb) >> 4);
-              mma_f16(dcol + (sa + tb) * nb, adesc, bdesc, idesc_bf16(take * nb) | kIdescBMnMajor, acc);
-              tb += take;
-              left -= take;
-            }
-          }
-        }
+        // tile width as a compile-time constant: the issue sequence of a stage is then
+        // straight-line code with constant descriptor offsets (a single thread issues
+        // every MMA, and per-instruction index arithmetic would pace the tensor pipe)
+        if (nb == 16)
+          issue_stage<S, 16>(dcol, abase, abase + kABytes, c == 0);
+        else if (nb == 32)
+          issue_stage<S, 32>(dcol, abase, abase + kABytes, c == 0);
+        else if constexpr (S * 64 <= 2 * 256)
+          issue_stage<S, 64>(dcol, abase, abase + kABytes, c == 0);
         mma_commit(&sh->empty[s]);
       }
       mma_commit(&sh->acc_full[buf]);
