@@ -101,12 +101,10 @@ struct RomArgs {
   double* snap_vp;  // kv x Tvp (device)
   double* snap_sp;  // ks x Tsp
   unsigned long long Tvp, Tsp;
-  uint32_t R, fseis;
-  const double* phi_rcv;  // R x kv row-major (PhiVp[gid_r, :])
-  const void* phi_rcv_t;  // the same rows as the kernel's element type (double, or df for the mixed form)
-  double* seis;           // R x Tseis
-  unsigned long long Tseis;
-  unsigned int* error;    // set when an exchange wait runs out
+  uint32_t fseis;
+  double* hist;                 // kv x (samples of this launch): XV on the seismogram's sample steps
+  unsigned long long hist_t0;   // sample index of hist's first column
+  unsigned int* error;          // set when an exchange wait runs out
 };
 
 // Dynamic shared memory of the rank-1 kernel, in elements of T (double or df):
@@ -252,17 +250,6 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1Threads) bv[r - v0] = A::load(a.b[r]);
   cluster.sync();
 
-  // ROM seismogram S(r) = PhiVp[gid_r, :] . XV after step nn, on its sample steps
-  // (main_reconstruct_seismo.cc:157-185); receiver r on CTA r % csize, so the rows
-  // spread evenly over the cluster; receiver rows in the kernel's own arithmetic
-  auto seismogram = [&](const T* x, unsigned long long nn) {
-    if (!a.fseis || nn % a.fseis != 0) return;
-    for (uint32_t r = crank + csize * warp; r < a.R; r += csize * kR1Warps) {
-      const T* prow = static_cast<const T*>(a.phi_rcv_t) + (size_t)r * a.kv;
-      const T s = A::dot(prow, x, a.kv, lane);
-      if (lane == 0) A::store_sample(a.seis + r + (size_t)a.R * (nn / a.fseis - 1), s);
-    }
-  };
   const T dtT = A::load(a.dt);
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
     const unsigned long long n = a.step0 + it + 1;
@@ -271,6 +258,10 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
     const T fdt = static_cast<const T*>(a.fdt_t)[it];
     // sample steps of the observers, decided once per step
     const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
+    // the ROM seismogram S = PhiVp[gid_r, :] XV (main_reconstruct_seismo.cc:157-185) is one
+    // GEMM kernel after the launch over the XV of the sample steps, kept here in hist
+    double* const hcol = a.hist && a.fseis && n % a.fseis == 0
+                             ? a.hist + (size_t)a.kv * (n / a.fseis - 1 - a.hist_t0) : nullptr;
     const uint32_t cur = (uint32_t)(it & 1), nxt = cur ^ 1u, par = (uint32_t)((it >> 1) & 1);
     const T* const xvc = xvb + (size_t)cur * a.kv;
     const T* const xsc = xsb + (size_t)cur * a.ks;
@@ -286,6 +277,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
         st_async8(peer_addr(smem_addr(xv + r), lane), bits8(x), peer_addr(smem_addr(&xbar[nxt]), lane));
         if (lane == 0 && snap_v)
           a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
+        if (lane == 0 && hcol) A::store_sample(hcol + r, x);
       }
     }
     bool ok = xbar_wait(&xbar[nxt], par);
@@ -304,8 +296,6 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
           a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
       }
     }
-    // the seismogram while the stress rows travel: it reads only this step's XV copy
-    seismogram(xv, n);
     ok = xbar_wait(&xbar[2 + nxt], par);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicOr(a.error, 2u);
@@ -327,6 +317,28 @@ __global__ void rom_split_df_kernel(const double* in, df* out, size_t n) {
     const double v = in[e];
     out[e] = df_split(v);
   }
+}
+
+// out (R x T, leading dimension R) = phi (R x k row-major) * hist (k x T): one 16 x 16
+// output tile per block, the k sum in ascending order with FMAs, so every element's
+// arithmetic is independent of how the columns are split across launches.
+__global__ void rom_seis_gemm_kernel(const double* __restrict__ phi, const double* __restrict__ hist, uint32_t R,
+                                     uint32_t k, uint32_t T, double* __restrict__ out) {
+  __shared__ double ps[16][17], hs[16][17];
+  const uint32_t tx = threadIdx.x, ty = threadIdx.y;
+  const uint32_t r = blockIdx.x * 16 + ty, t = blockIdx.y * 16 + tx;
+  double acc = 0.0;
+  for (uint32_t k0 = 0; k0 < k; k0 += 16) {
+    const uint32_t rr = blockIdx.x * 16 + ty, kk = k0 + tx;
+    ps[ty][tx] = (rr < R && kk < k) ? phi[(size_t)rr * k + kk] : 0.0;
+    const uint32_t kh = k0 + ty, th = blockIdx.y * 16 + tx;
+    hs[ty][tx] = (kh < k && th < T) ? hist[(size_t)th * k + kh] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc = fma(ps[ty][j], hs[j][tx], acc);
+    __syncthreads();
+  }
+  if (r < R && t < T) out[(size_t)t * R + r] = acc;
 }
 
 // Samples stored as FP32 hi + lo pairs in place of doubles -> FP64, in place.
@@ -400,9 +412,10 @@ struct shaw_rom_s {
   uint32_t R = 0;
   uint64_t fseis = 0, seis_T = 0, seis_nsteps = 0;
   double *phi_rcv = nullptr, *seis = nullptr;
-  void* phi_rcv_df = nullptr;  // receiver rows split into FP32 hi + lo (rank-1 mixed form)
   double* fdt = nullptr;  // rank-1 forcing table of the current launch
   uint64_t fdt_cap = 0;
+  double* hist = nullptr;  // rank-1: XV on the sample steps of a launch (seismogram GEMM input)
+  size_t hist_cap = 0;
   unsigned int* r1_err = nullptr;  // rank-1 kernel: an exchange wait ran out
   // rank-1 cluster launch shape
   uint32_t cluster = 1, rows_v = 0, rows_s = 0;
@@ -468,8 +481,21 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   a.kv = (uint32_t)h->kv; a.ks = (uint32_t)h->ks; a.rows_v = h->rows_v; a.rows_s = h->rows_s;
   a.step0 = h->step; a.nsteps = nsteps;
   a.fvp = (uint32_t)h->fvp; a.fsp = (uint32_t)h->fsp; a.snap_vp = h->snap_vp; a.snap_sp = h->snap_sp;
-  a.R = h->R; a.fseis = (uint32_t)h->fseis; a.phi_rcv = h->phi_rcv; a.seis = h->seis; a.Tseis = h->seis_T;
-  a.phi_rcv_t = MIXED ? static_cast<const void*>(h->phi_rcv_df) : static_cast<const void*>(h->phi_rcv);
+  // seismogram samples of this launch: XV history in the kernel, one GEMM kernel afterwards
+  const uint64_t t0 = h->fseis ? h->step / h->fseis : 0, t1 = h->fseis ? (h->step + nsteps) / h->fseis : 0;
+  if (h->seis && t1 > t0) {
+    const size_t need = (size_t)h->kv * (t1 - t0);
+    if (h->hist_cap < need) {
+      if (h->hist) cudaFree(h->hist);
+      h->hist = nullptr;
+      h->hist_cap = 0;
+      SHAW_CUDA(cudaMalloc(&h->hist, need * sizeof(double)));
+      h->hist_cap = need;
+    }
+    a.hist = h->hist;
+    a.hist_t0 = t0;
+    a.fseis = (uint32_t)h->fseis;
+  }
   auto kern = rom_rank1_cluster_kernel<MIXED>;
   SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
   if (h->cluster > 8) SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -488,15 +514,20 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   cfg.numAttrs = 1;
   SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
   h->launches++;
-  if (MIXED && h->seis && h->fseis) {  // this launch's seismogram samples -> FP64
-    const uint64_t t0 = h->step / h->fseis, t1 = (h->step + nsteps) / h->fseis;
-    if (t1 > t0) {
-      const size_t cnt = (size_t)h->R * (t1 - t0);
-      rom_samples_to_fp64_kernel<<<(unsigned)std::min<size_t>((cnt + 255) / 256, 1024), 256, 0, h->stream>>>(
-          h->seis + (size_t)h->R * t0, cnt);
+  if (a.hist) {
+    const size_t cnt = (size_t)h->kv * (t1 - t0);
+    if (MIXED) {  // the history as FP32 pairs -> FP64
+      rom_samples_to_fp64_kernel<<<(unsigned)std::min<size_t>((cnt + 255) / 256, 1024), 256, 0, h->stream>>>(h->hist,
+                                                                                                             cnt);
       h->launches++;
       SHAW_CUDA(cudaGetLastError());
     }
+    // S(:, t0:t1) = PhiRcv (R x kv, row-major) * hist (kv x (t1 - t0))
+    const dim3 grid((unsigned)((h->R + 15) / 16), (unsigned)((t1 - t0 + 15) / 16));
+    rom_seis_gemm_kernel<<<grid, dim3(16, 16), 0, h->stream>>>(h->phi_rcv, h->hist, (uint32_t)h->R, (uint32_t)h->kv,
+                                                              (uint32_t)(t1 - t0), h->seis + (size_t)h->R * t0);
+    h->launches++;
+    SHAW_CUDA(cudaGetLastError());
   }
   return SHAW_OK;
 }
@@ -615,7 +646,7 @@ void shaw_rom_destroy(shaw_rom_t h) {
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
   void* bufs[] = {h->Av, h->As, h->b, h->xv, h->xs, h->kind, h->period, h->delay,
-                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->phi_rcv_df, h->r1_err};
+                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->hist, h->r1_err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -681,7 +712,6 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   if (h->phi_rcv) { cudaFree(h->phi_rcv); h->phi_rcv = nullptr; }
-  if (h->phi_rcv_df) { cudaFree(h->phi_rcv_df); h->phi_rcv_df = nullptr; }
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->fseis = 0; h->seis_T = 0; h->seis_nsteps = 0;
   if (h->oz)
@@ -709,13 +739,6 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t R, uin
   SHAW_CUDA(cudaMemcpyAsync(h->phi_rcv, phi_rows, (size_t)R * h->kv * sizeof(double), cudaMemcpyHostToDevice,
                             h->stream));
   SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
-  if (h->rank == 1 && h->precision == SHAW_MIXED_FP32) {
-    SHAW_CUDA(cudaMalloc(&h->phi_rcv_df, (size_t)R * h->kv * sizeof(df)));
-    rom_split_df_kernel<<<256, 256, 0, h->stream>>>(h->phi_rcv, static_cast<df*>(h->phi_rcv_df),
-                                                    (size_t)R * h->kv);
-    h->launches++;
-    SHAW_CUDA(cudaGetLastError());
-  }
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   h->R = R; h->fseis = freq; h->seis_T = T; h->seis_nsteps = nsteps;
   return SHAW_OK;
