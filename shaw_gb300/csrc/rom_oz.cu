@@ -702,18 +702,19 @@ __device__ __forceinline__ void pair_sync(Shared* sh, unsigned int* ctr, uint32_
   __syncthreads();
   ++nsync;
   if (threadIdx.x == 0 && !sh->abort) {
-    __threadfence();
-    atomicAdd(ctr, 1u);
+    // release this CTA's writes (ordered before by the block barrier) with the arrival,
+    // acquire the peer's with the observing load; polled without sleeping (two CTAs)
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
     bool ok = false;
     for (unsigned long long i = 0; i < kWaitLimit; ++i) {
-      if (*reinterpret_cast<volatile unsigned int*>(ctr) >= 2u * nsync) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+      if (v >= 2u * nsync) {
         ok = true;
         break;
       }
-      __nanosleep(64);
     }
     if (!ok) raise(sh, err, 32u);
-    __threadfence();
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
   __syncthreads();
