@@ -206,26 +206,30 @@ constexpr uint32_t kIdescBMnMajor = 1u << 16;
 // columns (diagonal d = columns d*NB ..), so operator slice sa times the state slices
 // tb = 0 .. S-1-sa is ONE MMA of N = (S-sa)*NB whose output columns start at diagonal
 // sa: S MMAs per K-step instead of S(S+1)/2 pair MMAs, each A slice read from shared
-// memory once.  N is capped at 256 (split into two MMAs where needed).  The first MMA
-// of a tile (sa = 0 covers every diagonal) starts the accumulation.  Descriptors of the
-// stage's first A / B slice; the others differ only in the start-address field (16-byte
-// units, no carry: shared addresses < 256 KB).
+// memory once.  N is capped at 256: a longer stack is split into the fewest MMAs, with
+// the slices spread evenly over them (an MMA costs ~N/2 cycles above N = 128, so 192 +
+// 192 issues faster than 256 + 128).  The first MMA of a tile (sa = 0 covers every
+// diagonal) starts the accumulation.  Descriptors of the stage's first A / B slice; the
+// others differ only in the start-address field (16-byte units, no carry: shared
+// addresses < 256 KB).
 template <int S, uint32_t NB>
 __device__ __forceinline__ void issue_stage(uint32_t dcol, uint32_t abase, uint32_t bbase, bool first_chunk) {
   const uint64_t adesc0 = smem_desc(abase, 128, 512);
   const uint64_t bdesc0 = smem_desc(bbase, 16u * S * NB, 128);  // MN-major state slices
-  constexpr uint32_t kTake = 256u / NB;
+  constexpr uint32_t kCap = 256u / NB;
 #pragma unroll
   for (uint32_t k = 0; k < kKc / 16; ++k) {
 #pragma unroll
     for (int sa = 0; sa < S; ++sa) {
       const uint64_t adesc = adesc0 + ((sa * kATile + k * 256) >> 4);
       const uint32_t acc = (!first_chunk || k > 0 || sa > 0) ? 1u : 0u;
+      const uint32_t total = (uint32_t)(S - sa), parts = (total + kCap - 1) / kCap;
 #pragma unroll
-      for (uint32_t tb = 0; tb < (uint32_t)(S - sa); tb += kTake) {
-        const uint32_t take = ((uint32_t)(S - sa) - tb) < kTake ? ((uint32_t)(S - sa) - tb) : kTake;
+      for (uint32_t p = 0, tb = 0; p < parts; ++p) {
+        const uint32_t take = (total - tb + (parts - p) - 1) / (parts - p);
         const uint64_t bdesc = bdesc0 + ((tb * 16u * NB + k * 32u * S * NB) >> 4);
         mma_f16(dcol + (sa + tb) * NB, adesc, bdesc, idesc_bf16(take * NB) | kIdescBMnMajor, acc);
+        tb += take;
       }
     }
   }
