@@ -169,12 +169,16 @@ struct Shared {
   uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], drain;
   uint32_t tmem;
   int abort;
-  int beta_v[kMaxNb], beta_s[kMaxNb];   // exponents the current B tiles were sliced with
-  int pred_v[kMaxNb], pred_s[kMaxNb];   // predicted exponents for slicing the next new state
+  // per-column arrays 16-byte aligned: the epilogue reads them 8 columns at a time
+  __align__(16) int beta_v[kMaxNb];
+  __align__(16) int beta_s[kMaxNb];   // exponents the current B tiles were sliced with
+  __align__(16) int pred_v[kMaxNb];
+  __align__(16) int pred_s[kMaxNb];   // predicted exponents for slicing the next new state
   unsigned int colmax[kMaxNb];
   unsigned long long reslice_v, reslice_s;  // columns to re-slice exactly after a phase
-  float fdt_h[kMaxNb], fdt_l[kMaxNb];  // f_j(t_{n-1}) * dt of the current step, as FP32 hi + lo
-  double fdt64[kMaxNb];                 // the same in FP64 (9-slice form)
+  __align__(16) float fdt_h[kMaxNb];   // f_j(t_{n-1}) * dt of the current step, as FP32 hi + lo
+  __align__(16) float fdt_l[kMaxNb];
+  __align__(16) double fdt64[kMaxNb];  // the same in FP64 (9-slice form)
   OzInst in;
   OzTile tile;
 };
@@ -696,6 +700,25 @@ __device__ __forceinline__ void note_max8(Shared* sh, uint32_t j0, const float* 
   note_max8_keys(sh, j0, key);
 }
 
+// 8 consecutive per-column values (j0 a multiple of 8) from shared memory as vector loads.
+template <typename T>
+__device__ __forceinline__ void ld8(const T* p, T* v) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  if constexpr (sizeof(T) == 4) {
+    const int4 a = reinterpret_cast<const int4*>(p)[0], b = reinterpret_cast<const int4*>(p)[1];
+    const int w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) memcpy(v + i, w + i, 4);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const double2 d = reinterpret_cast<const double2*>(p)[i];
+      memcpy(v + 2 * i, &d.x, 8);
+      memcpy(v + 2 * i + 1, &d.y, 8);
+    }
+  }
+}
+
 __device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
 // Step barrier of the two CTAs of a paired tile (block-wide call).  Thread 0 publishes this
@@ -898,23 +921,29 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           }
           float yh[8], yl[8];
           fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
+          int b8[8], p8[8];
+          float fh8[8], fl8[8];
+          ld8(sh->beta_s + j0, b8);
+          ld8(sh->pred_v + j0, p8);
+          ld8(sh->fdt_h + j0, fh8);
+          ld8(sh->fdt_l + j0, fl8);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + sh->beta_s[j];
+            const int e = alpha + b8[jj];
             const size_t si = (size_t)j * in.kvp + row;
             float xh = ph[jj], xl = pl[jj];
             float s1, s2;
             pow2_pair(e, s1, s2);
             df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-            df_fma(xh, xl, sh->fdt_h[j], sh->fdt_l[j], qh[jj], ql[jj]);
+            df_fma(xh, xl, fh8[jj], fl8[jj], qh[jj], ql[jj]);
             st_f32(xvh + si, xh);
             st_f32(xvl + si, xl);
             ph[jj] = xh;
             pl[jj] = xl;
             // a column without a prediction is sliced with any exponent: it is re-sliced
             // exactly after the phase
-            const int pv = sh->pred_v[j];
+            const int pv = p8[jj];
             pe[jj] = pv != kNoPrediction ? pv : 0;
             if (snap_v && row < in.kv && col < in.M)
               st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), (double)xh + (double)xl);
@@ -943,18 +972,23 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           }
           double yH[8], yL[8];
           fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
+          int b8[8], p8[8];
+          double f8[8];
+          ld8(sh->beta_s + j0, b8);
+          ld8(sh->pred_v + j0, p8);
+          ld8(sh->fdt64 + j0, f8);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + sh->beta_s[j];
+            const int e = alpha + b8[jj];
             // x += dt * y with y = (yH 2^36 + yL) 2^e, then x += fdt * b
             double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
             xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
-            xn = fma(sh->fdt64[j], f[jj], xn);
+            xn = fma(f8[jj], f[jj], xn);
             st_f64(xv64 + (size_t)j * in.kvp + row, xn);
             x[jj] = xn;
             key[jj] = max_key64(xn);
-            const int pv = sh->pred_v[j];
+            const int pv = p8[jj];
             pe[jj] = pv != kNoPrediction ? pv : 0;
             if (snap_v && row < in.kv && col < in.M) st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), xn);
           }
@@ -1037,10 +1071,13 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           }
           float yh[8], yl[8];
           fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
+          int b8[8], p8[8];
+          ld8(sh->beta_v + j0, b8);
+          ld8(sh->pred_s + j0, p8);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + sh->beta_v[j];
+            const int e = alpha + b8[jj];
             const size_t si = (size_t)j * in.ksp + row;
             float xh = ph[jj], xl = pl[jj];
             float s1, s2;
@@ -1050,7 +1087,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
             st_f32(xsl + si, xl);
             ph[jj] = xh;
             pl[jj] = xl;
-            const int ps = sh->pred_s[j];
+            const int ps = p8[jj];
             pe[jj] = ps != kNoPrediction ? ps : 0;
             if (snap_s && row < in.ks && col < in.M)
               st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), (double)xh + (double)xl);
@@ -1075,16 +1112,19 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           for (int jj = 0; jj < 8; ++jj) x[jj] = xs64[(size_t)(j0 + jj) * in.ksp + row];
           double yH[8], yL[8];
           fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
+          int b8[8], p8[8];
+          ld8(sh->beta_v + j0, b8);
+          ld8(sh->pred_s + j0, p8);
 #pragma unroll
           for (int jj = 0; jj < 8; ++jj) {
             const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + sh->beta_v[j];
+            const int e = alpha + b8[jj];
             double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
             xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
             st_f64(xs64 + (size_t)j * in.ksp + row, xn);
             x[jj] = xn;
             key[jj] = max_key64(xn);
-            const int ps = sh->pred_s[j];
+            const int ps = p8[jj];
             pe[jj] = ps != kNoPrediction ? ps : 0;
             if (snap_s && row < in.ks && col < in.M) st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), xn);
           }
