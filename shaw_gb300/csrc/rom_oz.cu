@@ -376,6 +376,26 @@ __device__ __forceinline__ void fetch_combined8(bool staged, uint32_t tcols, uin
   }
 }
 
+// x * 2^-e: one exact (or once-rounded) product when 2^-e is a normal FP32, else ldexpf.
+__device__ __forceinline__ float scale_exp2f(float x, int e) {
+  return (e >= -126 && e <= 126) ? x * __int_as_float((127 - e) << 23) : ldexpf(x, -e);
+}
+
+// The 6 balanced base-64 digits of v = h + l (|v| < 1, double-float): digits 0-2 from h
+// alone (each step exact: th = 64 h, a = rint(th), h = th - a), then l is folded in at
+// its weight (2^18 after three steps) with one rounded add (error below 2^-42 of the
+// unit), digits 3-5 from that sum.  Digit 0 is in [-64, 64], the others in [-32, 32]:
+// integers, exact in BF16; the expansion matches v to within 2^-37.
+__device__ __forceinline__ void six_digits(float h, float l, float (&a)[6]) {
+#pragma unroll
+  for (int s = 0; s < 6; ++s) {
+    if (s == 3) h += l * 0x1p18f;
+    const float th = h * 64.f;
+    a[s] = rintf(th);
+    h = th - a[s];
+  }
+}
+
 // Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
 // into the BF16 B tiles with per-column exponents beta[j] (|x| < 2^beta).
 __device__ __forceinline__ void slice_state(const float* xh, const float* xl, uint32_t kp, uint32_t nb,
@@ -401,16 +421,12 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
     for (int u = 0; u < 4; ++u) {
       if (e0 + u * kEpiThreads >= n) break;
       if (!((mask >> jj[u]) & 1ull)) continue;
-      float h = ldexpf(vh[u], -beta[jj[u]]), l = ldexpf(vl[u], -beta[jj[u]]);
+      float a[6];
+      six_digits(scale_exp2f(vh[u], beta[jj[u]]), scale_exp2f(vl[u], beta[jj[u]]), a);
       uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + bslice_off<6>(nb, 0, jj[u], rr[u] % kKc);
 #pragma unroll
-      for (int s = 0; s < 6; ++s) {
-        const float th = h * 64.f, tl = l * 64.f;
-        float a = rintf(th);
-        a = fminf(64.f, fmaxf(-64.f, a));
-        two_sum(th - a, tl, h, l);
-        *reinterpret_cast<__nv_bfloat16*>(base + s * 16u * nb) = __float2bfloat16_rn(a);
-      }
+      for (int s = 0; s < 6; ++s)
+        *reinterpret_cast<__nv_bfloat16*>(base + s * 16u * nb) = __float2bfloat16_rn(a[s]);
     }
   }
 }
@@ -422,27 +438,15 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
 // exactly.  Below 2^e the first slice is in [-64, 64] and every slice is exact in BF16.
 __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, const int* e, uint8_t* dst,
                                              uint32_t nb) {
-  float h[8], l[8];
+  float a[8][6];
 #pragma unroll
-  for (int jj = 0; jj < 8; ++jj) {
-    if (e[jj] >= -126 && e[jj] <= 126) {  // 2^-e is a normal FP32: one exact (or once-rounded) product
-      const float f = __int_as_float((127 - e[jj]) << 23);
-      h[jj] = xh[jj] * f;
-      l[jj] = xl[jj] * f;
-    } else {
-      h[jj] = ldexpf(xh[jj], -e[jj]);
-      l[jj] = ldexpf(xl[jj], -e[jj]);
-    }
-  }
+  for (int jj = 0; jj < 8; ++jj) six_digits(scale_exp2f(xh[jj], e[jj]), scale_exp2f(xl[jj], e[jj]), a[jj]);
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
     uint32_t w[4];
 #pragma unroll
     for (int jj = 0; jj < 8; ++jj) {
-      const float th = h[jj] * 64.f, tl = l[jj] * 64.f;
-      const float a = rintf(th);
-      two_sum(th - a, tl, h[jj], l[jj]);
-      const uint32_t bits = __bfloat16_as_ushort(__float2bfloat16_rn(a));
+      const uint32_t bits = __float_as_uint(a[jj][s]) >> 16;  // small integers: the BF16 bits exactly
       w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
     }
     st_v4(dst + s * 16u * nb, w);
