@@ -162,11 +162,15 @@ struct OzArgs {
   unsigned int* error;
   unsigned long long* tile_ns;  // per tile: device time of its last run
   unsigned int* pair_sync;      // per pair slot: arrival counter (zeroed before each launch)
+  unsigned int* pair_early;     // per pair slot: early-gate openings of both parts (zeroed likewise)
   unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima (zeroed before each launch)
 };
 
 struct Shared {
   uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], drain;
+  uint64_t gate_early, gate_full;  // opened by the epilogue once per new state (see the producer)
+  uint32_t meta[kMaxStages];       // per pipeline stage: kMeta* flags
+  int redo[2];                     // per new state (alternating): its early slices were re-sliced
   uint32_t tmem;
   int abort;
   // per-column arrays 16-byte aligned: the epilogue reads them 8 columns at a time
@@ -239,76 +243,60 @@ __device__ __forceinline__ void issue_stage(uint32_t dcol, uint32_t abase, uint3
   }
 }
 
-// One GEMM phase: for every 128-row M-tile, D_d = sum over K of the slice pairs on
-// diagonal d into an accumulator set; the epilogue `epi(mt, tmem_cols)` runs on warps
-// 4..11 while the MMAs of the next M-tile fill the other set.
-template <int S, typename Epi>
-__device__ __forceinline__ void gemm_phase(uint8_t* stages, Shared* sh, const uint8_t* Aop, const uint8_t* Bop,
-                                           uint32_t mt0, uint32_t n_mt, uint32_t n_kc, uint32_t nb, uint32_t& it,
-                                           uint32_t (&uses)[2], unsigned int* err, Epi epi) {
+// Stage metadata, written by the producer before it hands a stage over: the stage opens an
+// M-tile (the issuer takes the next accumulator set), starts its accumulation, closes it
+// (commit to acc_full), or ends the tile (no copies, no MMAs).
+constexpr uint32_t kMetaBegin = 1u, kMetaFirst = 2u, kMetaLast = 4u, kMetaEnd = 8u;
+
+// Producer: hand the next pipeline stage over (bounded wait for it to be free), with its
+// metadata and, unless it ends the tile, the bulk copies of one operator and one B stage.
+template <int S>
+__device__ __forceinline__ bool push_stage(uint8_t* stages, Shared* sh, uint32_t& it, uint32_t meta,
+                                           const uint8_t* asrc, const uint8_t* bsrc, uint32_t bbytes,
+                                           unsigned int* err) {
   using G = Geo<S>;
-  constexpr int kStages = G::kStages;
-  constexpr uint32_t kStageBytes = G::kStageBytes, kABytes = G::kABytes;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t bbytes = G::bstage_bytes(nb), nbuf = G::acc_buffers(nb);
-  if (warp == 0 && lane == 0) {
-    for (uint32_t q = 0; q < n_mt * n_kc && !sh->abort; ++q) {
-      const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
-      if (!mbar_wait(&sh->empty[s], ph ^ 1u)) { raise(sh, err, 1u); break; }
-      const uint32_t mt = q / n_kc, c = q - mt * n_kc;
-      uint8_t* st = stages + (size_t)s * kStageBytes;
-      mbar_expect_tx(&sh->full[s], kABytes + bbytes);
-      bulk_g2s(st, Aop + ((size_t)(mt0 + mt) * n_kc + c) * kABytes, kABytes, &sh->full[s]);
-      bulk_g2s(st + kABytes, Bop + (size_t)c * bbytes, bbytes, &sh->full[s]);
-    }
-  } else if (warp == 1 && lane == 0) {
-    uint32_t lu[2] = {uses[0], uses[1]};
-    for (uint32_t mt = 0; mt < n_mt && !sh->abort; ++mt) {
-      uint32_t buf, par;
-      acc_next(nbuf, lu, buf, par);
-      if (!mbar_wait(&sh->acc_empty[buf], par ^ 1u)) { raise(sh, err, 2u); break; }
-      tc_fence_after();
-      const uint32_t dcol = sh->tmem + buf * 256u;
-      for (uint32_t c = 0; c < n_kc && !sh->abort; ++c) {
-        const uint32_t q = mt * n_kc + c;
-        const uint32_t s = (it + q) % kStages, ph = ((it + q) / kStages) & 1u;
-        if (!mbar_wait(&sh->full[s], ph)) { raise(sh, err, 4u); break; }
-        tc_fence_after();
-        const uint32_t abase = smem_u32(stages + (size_t)s * kStageBytes);
-        // tile width as a compile-time constant: the issue sequence of a stage is then
-        // straight-line code with constant descriptor offsets (a single thread issues
-        // every MMA, and per-instruction index arithmetic would pace the tensor pipe)
-        if (nb == 16)
-          issue_stage<S, 16>(dcol, abase, abase + kABytes, c == 0);
-        else if (nb == 32)
-          issue_stage<S, 32>(dcol, abase, abase + kABytes, c == 0);
-        else if constexpr (S * 64 <= 2 * 256)
-          issue_stage<S, 64>(dcol, abase, abase + kABytes, c == 0);
-        mma_commit(&sh->empty[s]);
-      }
-      mma_commit(&sh->acc_full[buf]);
-    }
-  } else if (warp >= 4) {
-    uint32_t lu[2] = {uses[0], uses[1]};
-    for (uint32_t mt = 0; mt < n_mt; ++mt) {
-      uint32_t buf, par;
-      acc_next(nbuf, lu, buf, par);
-      if (!mbar_wait(&sh->acc_full[buf], par)) { raise(sh, err, 8u); break; }
-      tc_fence_after();
-      // the epilogue may hand the accumulator back early (returns true once it has)
-      const bool released = !sh->abort && epi(mt0 + mt, sh->tmem + buf * 256u, &sh->acc_empty[buf]);
-      if (!released) {
-        tc_fence_before();
-        mbar_arrive(&sh->acc_empty[buf]);
-      }
+  const uint32_t s = it % G::kStages, ph = (it / G::kStages) & 1u;
+  if (!mbar_wait(&sh->empty[s], ph ^ 1u)) {
+    raise(sh, err, 1u);
+    return false;
+  }
+  ++it;
+  sh->meta[s] = meta;  // released to the issuer by the arrival below
+  if (meta & kMetaEnd) {
+    mbar_arrive(&sh->full[s]);
+  } else {
+    uint8_t* st = stages + (size_t)s * G::kStageBytes;
+    mbar_expect_tx(&sh->full[s], G::kABytes + bbytes);
+    bulk_g2s(st, asrc, G::kABytes, &sh->full[s]);
+    bulk_g2s(st + G::kABytes, bsrc, bbytes, &sh->full[s]);
+  }
+  return true;
+}
+
+// Producer: wait (bounded) until `gate` has opened for the gi-th new state of the launch,
+// then order its bulk copies after the generic-proxy writes the gate covers.
+__device__ __forceinline__ bool wait_gate(Shared* sh, uint64_t* gate, uint32_t gi, unsigned int* err) {
+  if (!mbar_wait(gate, gi & 1u)) {
+    raise(sh, err, 64u);
+    return false;
+  }
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  return true;
+}
+
+// Producer of a paired tile: wait (bounded) until both parts have opened the early gate of
+// new state g of the tile (a counter both parts add to once per state).
+__device__ __forceinline__ bool wait_peer_early(Shared* sh, const unsigned int* ctr, uint32_t g, unsigned int* err) {
+  for (unsigned long long i = 0; i < kWaitLimit; ++i) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+    if (v >= 2u * (g + 1u)) {
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      return true;
     }
   }
-  // every thread advances the counters the same way
-  it += n_mt * n_kc;
-  for (uint32_t mt = 0; mt < n_mt; ++mt) {
-    uint32_t buf, par;
-    acc_next(nbuf, uses, buf, par);
-  }
+  raise(sh, err, 128u);
+  return false;
 }
 
 // 2^e as an FP32 factor pair (e may leave the normal range of one factor).
@@ -724,15 +712,25 @@ __device__ __forceinline__ void ld8(const T* p, T* v) {
 }
 
 __device__ __forceinline__ void epi_barrier() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+// OR of a predicate over the 256 epilogue threads (named barrier 1).
+__device__ __forceinline__ bool epi_any(bool p) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred a, b;\n setp.ne.u32 a, %1, 0;\n bar.red.or.pred b, 1, 256, a;\n selp.u32 %0, 1, 0, b;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)p)
+      : "memory");
+  return r != 0u;
+}
 
-// Step barrier of the two CTAs of a paired tile (block-wide call).  Thread 0 publishes this
-// CTA's global writes (release), counts its arrival and waits, bounded, until the peer has
-// arrived as often; then it acquires the peer's writes for the generic and the bulk-copy
-// (async) proxies.  A wait that runs out raises the error flag.
+// Step barrier of the two CTAs of a paired tile (called by all epilogue threads).  Thread
+// 128 publishes the epilogue's global writes (release), counts its arrival and waits,
+// bounded, until the peer has arrived as often; then it acquires the peer's writes for the
+// generic and the bulk-copy (async) proxies.  A wait that runs out raises the error flag.
 __device__ __forceinline__ void pair_sync(Shared* sh, unsigned int* ctr, uint32_t& nsync, unsigned int* err) {
-  __syncthreads();
+  epi_barrier();
   ++nsync;
-  if (threadIdx.x == 0 && !sh->abort) {
+  if (threadIdx.x == 128 && !sh->abort) {
     // release this CTA's writes (ordered before by the block barrier) with the arrival,
     // acquire the peer's with the observing load; polled without sleeping (two CTAs)
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ctr) : "memory");
@@ -748,17 +746,24 @@ __device__ __forceinline__ void pair_sync(Shared* sh, unsigned int* ctr, uint32_
     if (!ok) raise(sh, err, 32u);
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
-  __syncthreads();
+  epi_barrier();
 }
 
 // S = 6: FP32 hi + lo state (SHAW_MIXED_OZAKI_BF16); S = 9: FP64 state (SHAW_OZAKI_FP64).
+//
+// Roles run decoupled within a tile: the producer (warp 0) walks the tile's phases and
+// pushes pipeline stages, the MMA issuer (warp 1) consumes them in order, the epilogue
+// warps (4..11) drain the accumulators, update and re-slice the state and open the gates
+// through which the producer may read the new slices.  Block-wide barriers are taken only
+// at tile boundaries; the epilogue warps synchronise among themselves on named barrier 1.
 template <int S>
 __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) {
   using G = Geo<S>;
   constexpr int kStages = G::kStages;
+  constexpr uint32_t kABytes = G::kABytes, kStageBytes = G::kStageBytes;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* stages = smem;
-  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * G::kStageBytes);
+  Shared* sh = reinterpret_cast<Shared*>(smem + kStages * kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ew = warp - 4;  // >= 0 on the epilogue warps
   const int q = warp & 3;   // TMEM lane quarter of this warp
@@ -773,6 +778,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       mbar_init(&sh->acc_empty[b], kEpiThreads);
     }
     mbar_init(&sh->drain, 1);
+    mbar_init(&sh->gate_early, 1);
+    mbar_init(&sh->gate_full, 1);
     sh->abort = 0;
     mbar_init_fence();
   }
@@ -782,7 +789,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
   tc_fence_after();
 
   const float dth = (float)a.dt, dtl = (float)(a.dt - (double)dth);
-  uint32_t it = 0, uses[2] = {0u, 0u};
+  // it: pipeline stages pushed (producer) / consumed (issuer); uses: accumulator sets taken
+  // (issuer, epilogue); gbase: states produced before this tile (initial slicing + two per step)
+  uint32_t it = 0, uses[2] = {0u, 0u}, gbase = 0;
   unsigned long long t_start = 0;
   for (uint32_t ti = a.cta_begin[blockIdx.x]; ti < a.cta_begin[blockIdx.x + 1]; ++ti) {
     if (threadIdx.x == 0) {
@@ -803,22 +812,9 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const uint32_t nb = sh->tile.nb, col0 = sh->tile.col0;
     const bool paired = (sh->tile.pinfo & 2u) != 0u;
     const uint32_t part = sh->tile.pinfo & 1u, slot = sh->tile.pinfo >> 2;
-    const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
-    const uint32_t bbytes = G::bstage_bytes(nb);                                   // B stage bytes
-    // single accumulator set (6-slice form with nb = 64, 9-slice form with nb = 32):
-    // stage its combined values in the TMEM columns after it
-    const bool stage = G::acc_buffers(nb) == 1;
-    const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + S * nb;
+    const uint32_t bbytes = G::bstage_bytes(nb);  // B stage bytes
+    const uint32_t nbuf = G::acc_buffers(nb);
     const uint32_t n_mt_v = in.kvp / 128, n_mt_s = in.ksp / 128, n_kc_v = in.ksp / kKc, n_kc_s = in.kvp / kKc;
-    float* const xvh = S == 6 ? in.xvh + (size_t)col0 * in.kvp : nullptr;
-    float* const xvl = S == 6 ? in.xvl + (size_t)col0 * in.kvp : nullptr;
-    float* const xsh = S == 6 ? in.xsh + (size_t)col0 * in.ksp : nullptr;
-    float* const xsl = S == 6 ? in.xsl + (size_t)col0 * in.ksp : nullptr;
-    const float* const bh = S == 6 ? in.bh + (size_t)col0 * in.kvp : nullptr;
-    const float* const bl = S == 6 ? in.bl + (size_t)col0 * in.kvp : nullptr;
-    double* const xv64 = S == 9 ? in.xv64 + (size_t)col0 * in.kvp : nullptr;
-    double* const xs64 = S == 9 ? in.xs64 + (size_t)col0 * in.ksp : nullptr;
-    const double* const b64 = S == 9 ? in.b64 + (size_t)col0 * in.kvp : nullptr;
     // M-tiles of this CTA: all of them, or its half of a paired tile (part 0 the first
     // ceil(n/2), part 1 the rest); the B slices are then one buffer per pair
     auto half = [&](uint32_t n, uint32_t& m0, uint32_t& m1) {
@@ -832,63 +828,253 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     uint8_t* const bvt = a.bvt + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     uint8_t* const bst = a.bst + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     unsigned int* const pctr = paired ? a.pair_sync + slot : nullptr;
+    unsigned int* const ectr = paired ? a.pair_early + slot : nullptr;
     unsigned int* const pcol = paired ? a.pair_colmax + (size_t)slot * 4 * kMaxNb : nullptr;  // [parity][part][nb]
-    uint32_t nsync = 0, nx = 0;
-    // Paired: combine the column maxima of both parts (block-wide call).  Each part
-    // stores its own maxima, both pass the step barrier, each folds in the peer's; the
-    // buffers alternate between exchanges, so a part never overwrites maxima the peer
-    // has yet to read (it would first have to pass the next barrier).
-    auto exchange = [&]() {
-      const uint32_t t = threadIdx.x - 128;
-      unsigned int* const xb = pcol + (size_t)(nx & 1u) * 2 * kMaxNb;
-      ++nx;
-      if (ew >= 0) {
-        asm volatile("fence.proxy.async.global;" ::: "memory");  // slices written in the phase, for the peer's TMA
-        epi_barrier();
-        if (t < nb) __stcg(xb + part * kMaxNb + t, sh->colmax[t]);
-      }
-      pair_sync(sh, pctr, nsync, a.error);
-      if (ew >= 0 && t < nb) sh->colmax[t] = max(sh->colmax[t], __ldcg(xb + (part ^ 1u) * kMaxNb + t));
-    };
 
-    // B tiles of the current XS (the state may be non-zero when advancing in pieces):
-    // with the exponents the previous launch left (so a run in pieces slices exactly
-    // as an uninterrupted run), or exact exponents for a fresh state
-    if (ew >= 0) {
-      const uint32_t nr = (ms1 - ms0) * 128;
-      for (uint32_t e = threadIdx.x - 128; e < nr * nb; e += kEpiThreads) {
-        const uint32_t j = e / nr, row = ms0 * 128 + (e - j * nr);
-        const size_t si = (size_t)j * in.ksp + row;
-        atomicMax(&sh->colmax[j], S == 6 ? __float_as_uint(fabsf(xsh[si])) : max_key64(xs64[si]));
+    if (warp == 0) {
+      // ---------------- producer ----------------
+      // Phase by phase, the stages of its M-tiles.  The B operand of a phase is the state
+      // produced before it (index g within the tile: 0 = the initial slicing, 2n + 1 = XV
+      // of step n, 2n + 2 = XS of step n).  The first M-tile starts with the K-chunks that
+      // are ready first -- the rows of the first M-tile of each part of the producing phase
+      // (early gate) -- and takes the rest once that phase has settled its exponents (full
+      // gate); if it re-sliced columns, the early chunks are dropped and the M-tile is
+      // issued again from chunk 0.  Every partial sum is exact, so the K order does not
+      // change the result.
+      if (lane == 0) {
+        uint32_t passed = ~0u;  // the last full gate passed (index over the whole launch)
+        auto phase = [&](const uint8_t* Aop, const uint8_t* Bop, uint32_t m0, uint32_t m1, uint32_t n_kc,
+                         uint32_t n_src, uint32_t g) -> bool {
+          const uint32_t gi = gbase + g;
+          constexpr uint32_t kCpm = 128 / kKc;  // K-chunks per M-tile of the producing phase
+          uint32_t e0 = ~0u, e1 = ~0u;          // its early M-tiles
+          if (g > 0 && passed != gi) {
+            if (paired) {
+              const uint32_t h = (n_src + 1) / 2;
+              if (h >= 2 && n_src - h >= 2) {
+                e0 = 0;
+                e1 = h;
+              }
+            } else if (n_src >= 2) {
+              e0 = 0;
+            }
+          }
+          auto early = [&](uint32_t c) { return c / kCpm == e0 || c / kCpm == e1; };
+          for (uint32_t mt = m0; mt < m1; ++mt) {
+            const uint8_t* const arow = Aop + (size_t)mt * n_kc * kABytes;
+            auto put = [&](uint32_t c, uint32_t meta) {
+              return push_stage<S>(stages, sh, it, meta, arow + (size_t)c * kABytes, Bop + (size_t)c * bbytes,
+                                   bbytes, a.error);
+            };
+            if (mt == m0 && e0 != ~0u) {
+              if (!wait_gate(sh, &sh->gate_early, gi, a.error)) return false;
+              if (paired && !wait_peer_early(sh, ectr, g, a.error)) return false;
+              uint32_t meta = kMetaBegin | kMetaFirst;
+              for (uint32_t c = 0; c < n_kc; ++c) {
+                if (!early(c)) continue;
+                if (!put(c, meta)) return false;
+                meta = 0u;
+              }
+              if (!wait_gate(sh, &sh->gate_full, gi, a.error)) return false;
+              passed = gi;
+              const bool redo = sh->redo[gi & 1u] != 0;
+              uint32_t last = n_kc - 1;
+              while (!redo && early(last)) --last;  // the last late chunk (the early set is a strict subset)
+              for (uint32_t c = 0; c < n_kc; ++c) {
+                if (!redo && early(c)) continue;
+                if (!put(c, (redo && c == 0 ? kMetaFirst : 0u) | (c == last ? kMetaLast : 0u))) return false;
+              }
+            } else {
+              if (passed != gi) {
+                if (!wait_gate(sh, &sh->gate_full, gi, a.error)) return false;
+                passed = gi;
+              }
+              for (uint32_t c = 0; c < n_kc; ++c)
+                if (!put(c, (c == 0 ? kMetaBegin | kMetaFirst : 0u) | (c == n_kc - 1 ? kMetaLast : 0u)))
+                  return false;
+            }
+            if (sh->abort) return false;
+          }
+          return true;
+        };
+        bool ok = true;
+        for (unsigned long long st = 0; st < a.nsteps && ok; ++st) {
+          const unsigned long long n = a.step0 + st + 1;
+          const uint32_t g = 2u * (uint32_t)st;
+          ok = phase(in.Av, bst, mv0, mv1, n_kc_v, n_mt_s, g);
+          if (ok && in.seis && in.fseis && n % in.fseis == 0) ok = phase(in.Ar, bvt, mr0, mr1, n_kc_s, n_mt_v, g + 1);
+          if (ok) ok = phase(in.As, bvt, ms0, ms1, n_kc_s, n_mt_v, g + 1);
+        }
+        push_stage<S>(stages, sh, it, kMetaEnd, nullptr, nullptr, 0u, a.error);  // the issuer leaves the tile
       }
-    }
-    if (paired) exchange();
-    if (ew >= 0) {
-      epi_barrier();
-      column_exponents<S>(sh, nb, sh->beta_s, sh->pred_s);
-      const uint32_t t = threadIdx.x - 128;
-      if (t < nb) {
-        const int bs = in.expo[col0 + t];
-        if (bs != kNoPrediction) {
-          sh->beta_s[t] = bs;
-          sh->pred_v[t] = in.expo[in.Mp + col0 + t];
-          sh->pred_s[t] = in.expo[2 * in.Mp + col0 + t];
+    } else if (warp == 1) {
+      // ---------------- MMA issuer ----------------
+      if (lane == 0) {
+        uint32_t buf = 0u, dcol = sh->tmem;
+        for (;;) {
+          const uint32_t s = it % kStages, ph = (it / kStages) & 1u;
+          if (!mbar_wait(&sh->full[s], ph)) {
+            raise(sh, a.error, 4u);
+            break;
+          }
+          ++it;
+          tc_fence_after();
+          const uint32_t meta = sh->meta[s];
+          if (meta & kMetaEnd) {
+            mbar_arrive(&sh->empty[s]);
+            break;
+          }
+          if (meta & kMetaBegin) {
+            uint32_t par;
+            acc_next(nbuf, uses, buf, par);
+            if (!mbar_wait(&sh->acc_empty[buf], par ^ 1u)) {
+              raise(sh, a.error, 2u);
+              break;
+            }
+            tc_fence_after();
+            dcol = sh->tmem + buf * 256u;
+          }
+          const uint32_t abase = smem_u32(stages + (size_t)s * kStageBytes);
+          const bool first = (meta & kMetaFirst) != 0u;
+          // tile width as a compile-time constant: the issue sequence of a stage is then
+          // straight-line code with constant descriptor offsets (a single thread issues
+          // every MMA, and per-instruction index arithmetic would pace the tensor pipe)
+          if (nb == 16)
+            issue_stage<S, 16>(dcol, abase, abase + kABytes, first);
+          else if (nb == 32)
+            issue_stage<S, 32>(dcol, abase, abase + kABytes, first);
+          else if constexpr (S * 64 <= 2 * 256)
+            issue_stage<S, 64>(dcol, abase, abase + kABytes, first);
+          mma_commit(&sh->empty[s]);
+          if (meta & kMetaLast) mma_commit(&sh->acc_full[buf]);
         }
       }
-      epi_barrier();
-      if constexpr (S == 6)
-        slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
-      else
-        slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-    }
-    if (paired) pair_sync(sh, pctr, nsync, a.error);  // both halves of the XS slices written
-    if (__syncthreads_or(sh->abort != 0)) break;
+    } else if (ew >= 0) {
+      // ---------------- epilogue ----------------
+      const uint32_t t = threadIdx.x - 128;
+      const uint32_t jbeg = (uint32_t)((ew >> 2) * (nb / 2)), jend = jbeg + nb / 2;  // this group's columns
+      // single accumulator set (6-slice form with nb = 64, 9-slice form with nb = 32):
+      // stage its combined values in the TMEM columns after it
+      const bool stage = nbuf == 1;
+      const uint32_t spare = sh->tmem + ((uint32_t)(q * 32) << 16) + S * nb;
+      float* const xvh = S == 6 ? in.xvh + (size_t)col0 * in.kvp : nullptr;
+      float* const xvl = S == 6 ? in.xvl + (size_t)col0 * in.kvp : nullptr;
+      float* const xsh = S == 6 ? in.xsh + (size_t)col0 * in.ksp : nullptr;
+      float* const xsl = S == 6 ? in.xsl + (size_t)col0 * in.ksp : nullptr;
+      const float* const bh = S == 6 ? in.bh + (size_t)col0 * in.kvp : nullptr;
+      const float* const bl = S == 6 ? in.bl + (size_t)col0 * in.kvp : nullptr;
+      double* const xv64 = S == 9 ? in.xv64 + (size_t)col0 * in.kvp : nullptr;
+      double* const xs64 = S == 9 ? in.xs64 + (size_t)col0 * in.ksp : nullptr;
+      const double* const b64 = S == 9 ? in.b64 + (size_t)col0 * in.kvp : nullptr;
+      uint32_t nsync = 0, nx = 0, gp = gbase;
+      // Paired: combine the column maxima of both parts.  Each part stores its own maxima,
+      // both pass the step barrier, each folds in the peer's; the buffers alternate between
+      // exchanges, so a part never overwrites maxima the peer has yet to read (it would
+      // first have to pass the next barrier).
+      auto exchange = [&]() {
+        unsigned int* const xb = pcol + (size_t)(nx & 1u) * 2 * kMaxNb;
+        ++nx;
+        epi_barrier();
+        if (t < nb) __stcg(xb + part * kMaxNb + t, sh->colmax[t]);
+        pair_sync(sh, pctr, nsync, a.error);
+        if (t < nb) sh->colmax[t] = max(sh->colmax[t], __ldcg(xb + (part ^ 1u) * kMaxNb + t));
+      };
+      // The early gate of the state being produced: the slices of this part's first M-tile
+      // are written (and, paired, the peer is told).
+      auto open_early = [&]() {
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        epi_barrier();
+        if (t == 0) {
+          mbar_arrive(&sh->gate_early);
+          if (paired) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ectr) : "memory");
+        }
+      };
+      // The full gate: every slice of the new state is final (both parts), with the re-slice
+      // decision for the producer.
+      auto open_full = [&](bool redo) {
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        epi_barrier();
+        if (t == 0) {
+          sh->redo[gp & 1u] = redo ? 1 : 0;
+          mbar_arrive(&sh->gate_full);
+        }
+        ++gp;
+      };
+      // One phase: its M-tiles in order; a phase that produces a state opens its early gate
+      // after the first.
+      auto epi_phase = [&](uint32_t m0, uint32_t m1, bool producing, auto&& epi) {
+        for (uint32_t mt = m0; mt < m1; ++mt) {
+          uint32_t buf, par;
+          acc_next(nbuf, uses, buf, par);
+          bool ok = !sh->abort;
+          if (ok && !mbar_wait(&sh->acc_full[buf], par)) {
+            raise(sh, a.error, 8u);
+            ok = false;
+          }
+          if (ok) {
+            tc_fence_after();
+            // the epilogue may hand the accumulator back early (returns true once it has)
+            const bool released = epi(mt, sh->tmem + buf * 256u, &sh->acc_empty[buf]);
+            if (!released) {
+              tc_fence_before();
+              mbar_arrive(&sh->acc_empty[buf]);
+            }
+          }
+          if (producing && mt == m0) open_early();
+        }
+      };
+      // After a producing phase: settle its exponents (both parts), re-slice the columns that
+      // left their predicted range, open the full gate.
+      auto settle = [&](int* beta, int* pred, unsigned long long* mask, unsigned long long* other, auto&& reslice) {
+        asm volatile("fence.proxy.async.global;" ::: "memory");  // slices written in the phase, for the peer's copies
+        if (paired) exchange();
+        epi_barrier();
+        settle_exponents<S>(sh, nb, beta, pred, mask, other);
+        epi_barrier();
+        const unsigned long long redo = *mask;
+        if (redo && !sh->abort) reslice(redo);
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        // paired: the re-sliced rows of both parts must land before either reads them (the
+        // mask is the same in both parts, so both take this barrier or neither)
+        if (paired && redo) pair_sync(sh, pctr, nsync, a.error);
+        open_full(redo != 0ull);
+      };
 
-    for (unsigned long long st = 0; st < a.nsteps; ++st) {
-      const unsigned long long n = a.step0 + st + 1;
-      if (ew >= 0) {
-        const uint32_t t = threadIdx.x - 128;
+      // B tiles of the current XS (the state may be non-zero when advancing in pieces):
+      // with the exponents the previous launch left (so a run in pieces slices exactly
+      // as an uninterrupted run), or exact exponents for a fresh state
+      {
+        const uint32_t nr = (ms1 - ms0) * 128;
+        for (uint32_t e = t; e < nr * nb; e += kEpiThreads) {
+          const uint32_t j = e / nr, row = ms0 * 128 + (e - j * nr);
+          const size_t si = (size_t)j * in.ksp + row;
+          atomicMax(&sh->colmax[j], S == 6 ? __float_as_uint(fabsf(xsh[si])) : max_key64(xs64[si]));
+        }
+        if (paired) exchange();
+        epi_barrier();
+        column_exponents<S>(sh, nb, sh->beta_s, sh->pred_s);
+        if (t < nb) {
+          const int bs = in.expo[col0 + t];
+          if (bs != kNoPrediction) {
+            sh->beta_s[t] = bs;
+            sh->pred_v[t] = in.expo[in.Mp + col0 + t];
+            sh->pred_s[t] = in.expo[2 * in.Mp + col0 + t];
+          }
+        }
+        epi_barrier();
+        if constexpr (S == 6)
+          slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
+        else
+          slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        if (paired) pair_sync(sh, pctr, nsync, a.error);  // both halves of the XS slices written
+        open_early();
+        open_full(false);
+      }
+
+      for (unsigned long long st = 0; st < a.nsteps; ++st) {
+        if (epi_any(sh->abort != 0)) break;
+        const unsigned long long n = a.step0 + st + 1;
         if (t < nb) {
           const uint32_t col = col0 + t;
           const double f =
@@ -899,15 +1085,13 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           sh->fdt64[t] = f;
         }
         epi_barrier();
-      }
-      // snapshot steps (StateObserver), decided once per step
-      const bool snap_v = in.snap_vp && in.fvp && n % in.fvp == 0;
-      const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
-      const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
-      // ---------------- velocity: XV += dt Av XS + fdt b ----------------
-      if constexpr (S == 6) {
-      gemm_phase<S>(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        // snapshot steps (StateObserver), decided once per step
+        const bool snap_v = in.snap_vp && in.fvp && n % in.fvp == 0;
+        const bool snap_s = in.snap_sp && in.fsp && n % in.fsp == 0;
+        const unsigned long long tv = snap_v ? n / in.fvp - 1 : 0, ts = snap_s ? n / in.fsp - 1 : 0;
+        // ---------------- velocity: XV += dt Av XS + fdt b ----------------
+        if constexpr (S == 6)
+          epi_phase(mv0, mv1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row];
@@ -957,9 +1141,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
-      } else {
-      gemm_phase<S>(stages, sh, in.Av, bst, mv0, mv1 - mv0, n_kc_v, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        else
+          epi_phase(mv0, mv1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_v[row] - 60;
@@ -1001,32 +1184,19 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
-      }
-      if (paired) exchange();
-      if (ew >= 0) {
-        epi_barrier();
-        settle_exponents<S>(sh, nb, sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s);
-        epi_barrier();
-        const unsigned long long redo = sh->reslice_v;
-        if (redo && !sh->abort) {
+        settle(sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s, [&](unsigned long long redo) {
           if constexpr (S == 6)
             slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
           else
             slice_state_fp64(xv64, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
-        }
-        asm volatile("fence.proxy.async.global;" ::: "memory");
-      }
-      // paired: the re-sliced rows of both parts must land before either reads them (the
-      // mask is the same in both parts, so both take this barrier or neither)
-      if (paired && __syncthreads_or(ew >= 0 && sh->reslice_v != 0ull)) pair_sync(sh, pctr, nsync, a.error);
-      if (__syncthreads_or(sh->abort != 0)) break;
-      // ---------------- seismogram on sample steps: S(:, t, cols) = PhiRcv XV ----------------
-      // (main_reconstruct_seismo.cc:157-185 in the loop; the XV slices of the stress GEMM
-      // are its B operand, so the product is exact like the leapfrog's)
-      if (in.seis && in.fseis && n % in.fseis == 0) {
-        const unsigned long long tcnt = n / in.fseis - 1;
-        gemm_phase<S>(stages, sh, in.Ar, bvt, mr0, mr1 - mr0, n_kc_s, nb, it, uses, a.error,
-                   [&](uint32_t mt, uint32_t tcols, uint64_t*) {
+        });
+        if (epi_any(sh->abort != 0)) break;
+        // ---------------- seismogram on sample steps: S(:, t, cols) = PhiRcv XV ----------------
+        // (main_reconstruct_seismo.cc:157-185 in the loop; the XV slices of the stress GEMM
+        // are its B operand, so the product is exact like the leapfrog's)
+        if (in.seis && in.fseis && n % in.fseis == 0) {
+          const unsigned long long tcnt = n / in.fseis - 1;
+          epi_phase(mr0, mr1, false, [&](uint32_t mt, uint32_t tcols, uint64_t*) {
                      const uint32_t r = mt * 128 + q * 32 + lane;
                      const int alpha = in.alpha_r[r];
                      for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
@@ -1054,12 +1224,11 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
                      }
                      return false;
                    });
-        if (__syncthreads_or(sh->abort != 0)) break;
-      }
-      // ---------------- stress: XS += dt As XV ----------------
-      if constexpr (S == 6) {
-      gemm_phase<S>(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+          if (epi_any(sh->abort != 0)) break;
+        }
+        // ---------------- stress: XS += dt As XV ----------------
+        if constexpr (S == 6)
+          epi_phase(ms0, ms1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row];
@@ -1101,9 +1270,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
-      } else {
-      gemm_phase<S>(stages, sh, in.As, bvt, ms0, ms1 - ms0, n_kc_s, nb, it, uses, a.error,
-                 [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
+        else
+          epi_phase(ms0, ms1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
         const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
         const uint32_t row = mt * 128 + q * 32 + lane;
         const int alpha = in.alpha_s[row] - 60;
@@ -1137,32 +1305,23 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         return staged;
       });
-      }
-      if (paired) exchange();
-      if (ew >= 0) {
-        epi_barrier();
-        settle_exponents<S>(sh, nb, sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v);
-        epi_barrier();
-        const unsigned long long redo = sh->reslice_s;
-        if (redo && !sh->abort) {
+        settle(sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v, [&](unsigned long long redo) {
           if constexpr (S == 6)
             slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
           else
             slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
-        }
-        asm volatile("fence.proxy.async.global;" ::: "memory");
+        });
       }
-      if (paired && __syncthreads_or(ew >= 0 && sh->reslice_s != 0ull)) pair_sync(sh, pctr, nsync, a.error);
-      if (__syncthreads_or(sh->abort != 0)) break;
+      if (t < nb && part == 0u) {  // exponents for the next launch
+        in.expo[col0 + t] = sh->beta_s[t];
+        in.expo[in.Mp + col0 + t] = sh->pred_v[t];
+        in.expo[2 * in.Mp + col0 + t] = sh->pred_s[t];
+      }
     }
-    if (ew >= 0 && threadIdx.x - 128 < nb && part == 0u) {  // exponents for the next launch
-      const uint32_t t = threadIdx.x - 128;
-      in.expo[col0 + t] = sh->beta_s[t];
-      in.expo[in.Mp + col0 + t] = sh->pred_v[t];
-      in.expo[2 * in.Mp + col0 + t] = sh->pred_s[t];
-    }
+    gbase += 2u * (uint32_t)a.nsteps + 1u;
+    const bool stop = __syncthreads_or(sh->abort != 0);
     if (threadIdx.x == 0 && a.tile_ns) a.tile_ns[a.order[ti]] = global_ns() - t_start;
-    if (__syncthreads_or(sh->abort != 0)) break;
+    if (stop) break;
   }
   // drain: no MMA may still be in flight when TMEM is released
   if (warp == 1 && lane == 0) {
@@ -1466,7 +1625,7 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s, int sli
   OZ_TRY(cudaMalloc(&b->bst, (size_t)b->sms * b->bscratch));
   OZ_TRY(cudaMalloc(&b->error, sizeof(unsigned int)));
   OZ_TRY(cudaMalloc(&b->tile_ns, b->max_tiles * sizeof(unsigned long long)));
-  OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)b->sms * sizeof(unsigned int)));
+  OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)2 * b->sms * sizeof(unsigned int)));  // step barrier, early gates
   OZ_TRY(cudaMalloc(&b->pair_colmax, (size_t)b->sms * 4 * kMaxNb * sizeof(unsigned int)));
 #undef OZ_TRY
   b->smem = slices == 6 ? (size_t)Geo<6>::kStages * Geo<6>::kStageBytes + sizeof(Shared)
@@ -1568,11 +1727,11 @@ int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsig
   a.inst = p->d_inst; a.tiles = p->d_tiles; a.order = p->d_order; a.cta_begin = p->d_begin;
   a.bvt = p->bvt; a.bst = p->bst; a.bscratch = p->bscratch;
   a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error; a.tile_ns = p->tile_ns;
-  a.pair_sync = p->pair_sync; a.pair_colmax = p->pair_colmax;
+  a.pair_sync = p->pair_sync; a.pair_early = p->pair_sync + p->sms; a.pair_colmax = p->pair_colmax;
   void (*kern)(OzArgs) = p->slices == 6 ? rom_rank2_ozaki_kernel<6> : rom_rank2_ozaki_kernel<9>;
   SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
   if (p->paired) {  // the parts of a pair wait on each other: all CTAs resident (cooperative launch)
-    SHAW_CUDA(cudaMemsetAsync(p->pair_sync, 0, p->ctas / 2 * sizeof(unsigned int), s));
+    SHAW_CUDA(cudaMemsetAsync(p->pair_sync, 0, (size_t)2 * p->sms * sizeof(unsigned int), s));
     void* args[] = {&a};
     SHAW_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3(p->ctas), dim3(kThreads), args, p->smem, s));
   } else {
