@@ -66,6 +66,7 @@ constexpr uint32_t kRowBytes = kKc * 2;
 constexpr uint32_t kATile = 128 * kRowBytes;  // one slice of a 128 x 32 operator tile: 8 KB
 constexpr uint32_t kMaxNb = 64;               // widest tile of either form
 constexpr int kMaxStages = 3;
+constexpr uint32_t kLevels = 8;  // M-tiles per phase and CTA: at most 1024 / 128
 // TMEM: two accumulator sets at columns 0 and 256 when S nb <= 256; otherwise one set at
 // column 0 and the staging of its combined values at column S nb
 constexpr uint32_t kTmemCols = 512;
@@ -162,13 +163,13 @@ struct OzArgs {
   unsigned int* error;
   unsigned long long* tile_ns;  // per tile: device time of its last run
   unsigned int* pair_sync;      // per pair slot: arrival counter (zeroed before each launch)
-  unsigned int* pair_early;     // per pair slot: early-gate openings of both parts (zeroed likewise)
+  unsigned int* pair_early;     // per pair slot and part: level gates opened (zeroed likewise)
   unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima (zeroed before each launch)
 };
 
 struct Shared {
   uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], drain;
-  uint64_t gate_early, gate_full;  // opened by the epilogue once per new state (see the producer)
+  uint64_t gate_lvl[kLevels], gate_full;  // opened by the epilogue once per new state (see the producer)
   uint32_t meta[kMaxStages];       // per pipeline stage: kMeta* flags
   int redo[2];                     // per new state (alternating): its early slices were re-sliced
   uint32_t tmem;
@@ -245,8 +246,9 @@ __device__ __forceinline__ void issue_stage(uint32_t dcol, uint32_t abase, uint3
 
 // Stage metadata, written by the producer before it hands a stage over: the stage opens an
 // M-tile (the issuer takes the next accumulator set), starts its accumulation, closes it
-// (commit to acc_full), or ends the tile (no copies, no MMAs).
-constexpr uint32_t kMetaBegin = 1u, kMetaFirst = 2u, kMetaLast = 4u, kMetaEnd = 8u;
+// (commit to acc_full after its MMAs), only closes it (no copies, no MMAs), or ends the
+// tile (no copies, no MMAs).
+constexpr uint32_t kMetaBegin = 1u, kMetaFirst = 2u, kMetaLast = 4u, kMetaEnd = 8u, kMetaCommit = 16u;
 
 // Producer: hand the next pipeline stage over (bounded wait for it to be free), with its
 // metadata and, unless it ends the tile, the bulk copies of one operator and one B stage.
@@ -262,7 +264,7 @@ __device__ __forceinline__ bool push_stage(uint8_t* stages, Shared* sh, uint32_t
   }
   ++it;
   sh->meta[s] = meta;  // released to the issuer by the arrival below
-  if (meta & kMetaEnd) {
+  if (meta & (kMetaEnd | kMetaCommit)) {
     mbar_arrive(&sh->full[s]);
   } else {
     uint8_t* st = stages + (size_t)s * G::kStageBytes;
@@ -284,13 +286,13 @@ __device__ __forceinline__ bool wait_gate(Shared* sh, uint64_t* gate, uint32_t g
   return true;
 }
 
-// Producer of a paired tile: wait (bounded) until both parts have opened the early gate of
-// new state g of the tile (a counter both parts add to once per state).
-__device__ __forceinline__ bool wait_peer_early(Shared* sh, const unsigned int* ctr, uint32_t g, unsigned int* err) {
+// Producer of a paired tile: wait (bounded) until the peer part's counter of opened level
+// gates (kLevels per new state) has reached `target`.
+__device__ __forceinline__ bool wait_peer(Shared* sh, const unsigned int* ctr, uint32_t target, unsigned int* err) {
   for (unsigned long long i = 0; i < kWaitLimit; ++i) {
     unsigned int v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
-    if (v >= 2u * (g + 1u)) {
+    if (v >= target) {
       asm volatile("fence.proxy.async.global;" ::: "memory");
       return true;
     }
@@ -778,7 +780,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
       mbar_init(&sh->acc_empty[b], kEpiThreads);
     }
     mbar_init(&sh->drain, 1);
-    mbar_init(&sh->gate_early, 1);
+    for (uint32_t l = 0; l < kLevels; ++l) mbar_init(&sh->gate_lvl[l], 1);
     mbar_init(&sh->gate_full, 1);
     sh->abort = 0;
     mbar_init_fence();
@@ -828,67 +830,61 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     uint8_t* const bvt = a.bvt + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     uint8_t* const bst = a.bst + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     unsigned int* const pctr = paired ? a.pair_sync + slot : nullptr;
-    unsigned int* const ectr = paired ? a.pair_early + slot : nullptr;
+    unsigned int* const ectr = paired ? a.pair_early + 2 * slot + part : nullptr;  // this part's level count
     unsigned int* const pcol = paired ? a.pair_colmax + (size_t)slot * 4 * kMaxNb : nullptr;  // [parity][part][nb]
 
     if (warp == 0) {
       // ---------------- producer ----------------
       // Phase by phase, the stages of its M-tiles.  The B operand of a phase is the state
       // produced before it (index g within the tile: 0 = the initial slicing, 2n + 1 = XV
-      // of step n, 2n + 2 = XS of step n).  The first M-tile starts with the K-chunks that
-      // are ready first -- the rows of the first M-tile of each part of the producing phase
-      // (early gate) -- and takes the rest once that phase has settled its exponents (full
-      // gate); if it re-sliced columns, the early chunks are dropped and the M-tile is
-      // issued again from chunk 0.  Every partial sum is exact, so the K order does not
-      // change the result.
+      // of step n, 2n + 2 = XS of step n).  The first M-tile against a new state takes its
+      // K-chunks level by level as the producing phase finishes its M-tiles -- level l =
+      // the rows of the l-th M-tile of each part (level gates) -- and is closed once that
+      // phase has settled its exponents (full gate): by a commit-only stage, or, if columns
+      // were re-sliced, by issuing the M-tile again from chunk 0.  Every partial sum is
+      // exact, so the K order does not change the result.
       if (lane == 0) {
         uint32_t passed = ~0u;  // the last full gate passed (index over the whole launch)
+        const unsigned int* const peer_ctr = paired ? ectr - part + (part ^ 1u) : nullptr;
         auto phase = [&](const uint8_t* Aop, const uint8_t* Bop, uint32_t m0, uint32_t m1, uint32_t n_kc,
                          uint32_t n_src, uint32_t g) -> bool {
           const uint32_t gi = gbase + g;
           constexpr uint32_t kCpm = 128 / kKc;  // K-chunks per M-tile of the producing phase
-          uint32_t e0 = ~0u, e1 = ~0u;          // its early M-tiles
-          if (g > 0 && passed != gi) {
-            if (paired) {
-              const uint32_t h = (n_src + 1) / 2;
-              if (h >= 2 && n_src - h >= 2) {
-                e0 = 0;
-                e1 = h;
-              }
-            } else if (n_src >= 2) {
-              e0 = 0;
-            }
-          }
-          auto early = [&](uint32_t c) { return c / kCpm == e0 || c / kCpm == e1; };
+          // M-tiles of the producing phase: this part's from own0, the peer's from peer0
+          const uint32_t h = paired ? (n_src + 1) / 2 : n_src;
+          const uint32_t own0 = part ? h : 0u, own_n = part ? n_src - h : h;
+          const uint32_t peer0 = part ? 0u : h, peer_n = paired ? n_src - own_n : 0u;
+          const uint32_t levels = max(own_n, peer_n);
           for (uint32_t mt = m0; mt < m1; ++mt) {
             const uint8_t* const arow = Aop + (size_t)mt * n_kc * kABytes;
             auto put = [&](uint32_t c, uint32_t meta) {
               return push_stage<S>(stages, sh, it, meta, arow + (size_t)c * kABytes, Bop + (size_t)c * bbytes,
                                    bbytes, a.error);
             };
-            if (mt == m0 && e0 != ~0u) {
-              if (!wait_gate(sh, &sh->gate_early, gi, a.error)) return false;
-              if (paired && !wait_peer_early(sh, ectr, g, a.error)) return false;
+            if (passed != gi) {
               uint32_t meta = kMetaBegin | kMetaFirst;
-              for (uint32_t c = 0; c < n_kc; ++c) {
-                if (!early(c)) continue;
-                if (!put(c, meta)) return false;
-                meta = 0u;
+              for (uint32_t l = 0; l < levels; ++l) {
+                if (!wait_gate(sh, &sh->gate_lvl[l], gi, a.error)) return false;
+                if (paired && !wait_peer(sh, peer_ctr, kLevels * g + l + 1u, a.error)) return false;
+                const uint32_t m_a = l < own_n ? own0 + l : ~0u, m_b = l < peer_n ? peer0 + l : ~0u;
+                const uint32_t lo = min(m_a, m_b), hi = max(m_a, m_b);  // ascending K order
+                for (uint32_t src : {lo, hi}) {
+                  if (src == ~0u) continue;
+                  for (uint32_t c = src * kCpm; c < (src + 1) * kCpm; ++c) {
+                    if (!put(c, meta)) return false;
+                    meta = 0u;
+                  }
+                }
               }
               if (!wait_gate(sh, &sh->gate_full, gi, a.error)) return false;
               passed = gi;
-              const bool redo = sh->redo[gi & 1u] != 0;
-              uint32_t last = n_kc - 1;
-              while (!redo && early(last)) --last;  // the last late chunk (the early set is a strict subset)
-              for (uint32_t c = 0; c < n_kc; ++c) {
-                if (!redo && early(c)) continue;
-                if (!put(c, (redo && c == 0 ? kMetaFirst : 0u) | (c == last ? kMetaLast : 0u))) return false;
+              if (sh->redo[gi & 1u] == 0) {
+                if (!put(0u, kMetaCommit)) return false;
+              } else {
+                for (uint32_t c = 0; c < n_kc; ++c)
+                  if (!put(c, (c == 0 ? kMetaFirst : 0u) | (c == n_kc - 1 ? kMetaLast : 0u))) return false;
               }
             } else {
-              if (passed != gi) {
-                if (!wait_gate(sh, &sh->gate_full, gi, a.error)) return false;
-                passed = gi;
-              }
               for (uint32_t c = 0; c < n_kc; ++c)
                 if (!put(c, (c == 0 ? kMetaBegin | kMetaFirst : 0u) | (c == n_kc - 1 ? kMetaLast : 0u)))
                   return false;
@@ -923,6 +919,11 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           if (meta & kMetaEnd) {
             mbar_arrive(&sh->empty[s]);
             break;
+          }
+          if (meta & kMetaCommit) {  // the M-tile's MMAs are all issued: close it
+            mma_commit(&sh->acc_full[buf]);
+            mbar_arrive(&sh->empty[s]);
+            continue;
           }
           if (meta & kMetaBegin) {
             uint32_t par;
@@ -979,14 +980,16 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         pair_sync(sh, pctr, nsync, a.error);
         if (t < nb) sh->colmax[t] = max(sh->colmax[t], __ldcg(xb + (part ^ 1u) * kMaxNb + t));
       };
-      // The early gate of the state being produced: the slices of this part's first M-tile
-      // are written (and, paired, the peer is told).
-      auto open_early = [&]() {
+      // Level gate l of the state being produced: the slices of this part's l-th M-tile are
+      // written (and, paired, the peer is told); after the last M-tile every remaining level
+      // opens, so each level gate opens once per state.
+      auto open_level = [&](uint32_t l, bool last) {
         asm volatile("fence.proxy.async.global;" ::: "memory");
         epi_barrier();
         if (t == 0) {
-          mbar_arrive(&sh->gate_early);
-          if (paired) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(ectr) : "memory");
+          const uint32_t top = last ? kLevels : l + 1u;
+          for (uint32_t u = l; u < top; ++u) mbar_arrive(&sh->gate_lvl[u]);
+          if (paired) asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(ectr), "r"(top - l) : "memory");
         }
       };
       // The full gate: every slice of the new state is final (both parts), with the re-slice
@@ -1000,8 +1003,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         }
         ++gp;
       };
-      // One phase: its M-tiles in order; a phase that produces a state opens its early gate
-      // after the first.
+      // One phase: its M-tiles in order; a phase that produces a state opens a level gate
+      // after each.
       auto epi_phase = [&](uint32_t m0, uint32_t m1, bool producing, auto&& epi) {
         for (uint32_t mt = m0; mt < m1; ++mt) {
           uint32_t buf, par;
@@ -1020,7 +1023,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
               mbar_arrive(&sh->acc_empty[buf]);
             }
           }
-          if (producing && mt == m0) open_early();
+          if (producing) open_level(mt - m0, mt + 1 == m1);
         }
       };
       // After a producing phase: settle its exponents (both parts), re-slice the columns that
@@ -1068,7 +1071,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
           slice_state_fp64(xs64, in.ksp, nb, sh->beta_s, bst, ~0ull, ms0 * 128, ms1 * 128);
         asm volatile("fence.proxy.async.global;" ::: "memory");
         if (paired) pair_sync(sh, pctr, nsync, a.error);  // both halves of the XS slices written
-        open_early();
+        open_level(0u, true);
         open_full(false);
       }
 
