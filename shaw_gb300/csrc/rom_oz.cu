@@ -371,19 +371,28 @@ __device__ __forceinline__ float scale_exp2f(float x, int e) {
   return (e >= -126 && e <= 126) ? x * __int_as_float((127 - e) << 23) : ldexpf(x, -e);
 }
 
+// Nearest integer of |x| < 2^22 (ties to even): adding 1.5 * 2^23 rounds x to the integer
+// grid of that binade; two full-rate adds instead of a conversion-pipe rint.
+__device__ __forceinline__ float round_int(float x) { return (x + 0x1.8p23f) - 0x1.8p23f; }
+
 // The 6 balanced base-64 digits of v = h + l (|v| < 1, double-float): digits 0-2 from h
-// alone (each step exact: th = 64 h, a = rint(th), h = th - a), then l is folded in at
-// its weight (2^18 after three steps) with one rounded add (error below 2^-42 of the
-// unit), digits 3-5 from that sum.  Digit 0 is in [-64, 64], the others in [-32, 32]:
-// integers, exact in BF16; the expansion matches v to within 2^-37.
+// alone (each step exact: th = 64 h, a = nearest integer of th, h = th - a), then l is
+// folded in at its weight (2^18 after three steps) with one rounded add (error below
+// 2^-42 of the unit), digits 3-5 from that sum.  Digit 0 is in [-64, 64], the others in
+// [-32, 32]: integers, exact in BF16; the expansion matches v to within 2^-37.
 __device__ __forceinline__ void six_digits(float h, float l, float (&a)[6]) {
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
     if (s == 3) h += l * 0x1p18f;
     const float th = h * 64.f;
-    a[s] = rintf(th);
+    a[s] = round_int(th);
     h = th - a[s];
   }
+}
+
+// Two FP32 values whose low 16 bits are zero (small integers) as one word of two BF16s.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
 // Slice a state block (rows x nb, column-major with leading dimension kp, double-float)
@@ -415,8 +424,8 @@ __device__ __forceinline__ void slice_state(const float* xh, const float* xl, ui
       six_digits(scale_exp2f(vh[u], beta[jj[u]]), scale_exp2f(vl[u], beta[jj[u]]), a);
       uint8_t* base = tiles + (size_t)(rr[u] / kKc) * bbytes + bslice_off<6>(nb, 0, jj[u], rr[u] % kKc);
 #pragma unroll
-      for (int s = 0; s < 6; ++s)
-        *reinterpret_cast<__nv_bfloat16*>(base + s * 16u * nb) = __float2bfloat16_rn(a[s]);
+      for (int s = 0; s < 6; ++s)  // small integers: the upper half of the FP32 bits is the BF16
+        *reinterpret_cast<uint16_t*>(base + s * 16u * nb) = (uint16_t)(__float_as_uint(a[s]) >> 16);
     }
   }
 }
@@ -435,10 +444,7 @@ __device__ __forceinline__ void slice_value8(const float* xh, const float* xl, c
   for (int s = 0; s < 6; ++s) {
     uint32_t w[4];
 #pragma unroll
-    for (int jj = 0; jj < 8; ++jj) {
-      const uint32_t bits = __float_as_uint(a[jj][s]) >> 16;  // small integers: the BF16 bits exactly
-      w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
-    }
+    for (int i = 0; i < 4; ++i) w[i] = pack_bf16x2(a[2 * i][s], a[2 * i + 1][s]);
     st_v4(dst + s * 16u * nb, w);
   }
 }
@@ -556,11 +562,10 @@ __device__ __forceinline__ long long fixed54(double x, int beta) {
   return bits < 0 ? -v : v;
 }
 
-// BF16 bits of a small integer (|a| <= 256 exactly): a + 1.5 * 2^23 as FP32 bits, back to
-// the float a, whose low 16 bits are zero.
-__device__ __forceinline__ uint32_t bf16_of_int(int a) {
-  return __float_as_uint(__int_as_float(0x4B400000 + a) - 12582912.0f) >> 16;
-}
+// A small integer (|a| <= 256) as FP32 without a conversion: a + 1.5 * 2^23 as FP32 bits,
+// back to the float a (whose low 16 bits are zero: its upper half is the BF16 of a).
+__device__ __forceinline__ float float_of_int(int a) { return __int_as_float(0x4B400000 + a) - 12582912.0f; }
+__device__ __forceinline__ uint32_t bf16_of_int(int a) { return __float_as_uint(float_of_int(a)) >> 16; }
 
 // Balanced base-64 digit s (most significant first) of a 54-bit fixed-point value v;
 // v keeps the remainder.  Digit 0 is in [-64, 64], the others in [-32, 32).
@@ -580,9 +585,9 @@ template <int s>
 __device__ __forceinline__ void slice9_step(long long (&v)[8], uint8_t* dst, uint32_t nb) {
   uint32_t w[4];
 #pragma unroll
-  for (int jj = 0; jj < 8; ++jj) {
-    const uint32_t bits = bf16_of_int(take_digit<s>(v[jj]));
-    w[jj >> 1] = (jj & 1) ? (w[jj >> 1] | (bits << 16)) : bits;
+  for (int i = 0; i < 4; ++i) {
+    const float lo = float_of_int(take_digit<s>(v[2 * i]));
+    w[i] = pack_bf16x2(lo, float_of_int(take_digit<s>(v[2 * i + 1])));
   }
   st_v4(dst + s * 16u * nb, w);
   if constexpr (s < 8) slice9_step<s + 1>(v, dst, nb);
