@@ -31,8 +31,11 @@
 // CTA c advances the tiles order[cta_begin[c] .. cta_begin[c+1]) one after another.
 // Tile widths nb in {16, 32, 64} and the schedule (longest-processing-time-first over
 // modelled or measured tile costs) are picked by the autotuner `tune`.
-// All waits are bounded: a wait that runs out sets an error flag, the kernel leaves its
-// loops at the next block-wide vote, releases TMEM and returns.
+// Within a tile the producer, the MMA issuer and the epilogue warps run decoupled (stage
+// metadata, accumulator barriers, and gates through which the epilogue releases each new
+// state to the producer); block-wide barriers are taken only between tiles.
+// All waits are bounded: a wait that runs out sets an error flag, every role leaves its
+// loop (the epilogue at its next vote), the kernel releases TMEM and returns.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -1330,6 +1333,13 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     const bool stop = __syncthreads_or(sh->abort != 0);
     if (threadIdx.x == 0 && a.tile_ns) a.tile_ns[a.order[ti]] = global_ns() - t_start;
     if (stop) break;
+  }
+  // no bulk copy may still be landing in shared memory when the CTA leaves (after an
+  // aborted run the issuer may not have consumed the last stages): wait, bounded, for the
+  // full barriers of the producer's last pushes
+  if (warp == 0 && lane == 0) {
+    for (uint32_t i = it > (uint32_t)kStages ? it - kStages : 0u; i < it; ++i)
+      if (!mbar_wait(&sh->full[i % kStages], (i / kStages) & 1u)) atomicOr(a.error, 16u);
   }
   // drain: no MMA may still be in flight when TMEM is released
   if (warp == 1 && lane == 0) {
