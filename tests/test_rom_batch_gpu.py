@@ -171,11 +171,13 @@ def test_batch_seismograms(shaw):
         assert relerr(seis[shaw.MIXED_OZAKI_BF16][i], single) <= 1e-8
 
 
-def test_batch_ozaki_paired_tiles_bitwise(shaw):
+@pytest.mark.parametrize("width", [16, 64])
+def test_batch_ozaki_paired_tiles_bitwise(shaw, width):
     """Tiles split across CTA pairs (each CTA half of the 128-row blocks, shared slices,
-    a step barrier) give the same numbers as whole tiles: states, snapshots and
-    seismograms bit for bit, also when advanced in pieces and with an odd number of
-    row blocks (384 modes) or a part without receiver rows (3 receivers)."""
+    a step barrier, level gates on the peer's row blocks) give the same numbers as whole
+    tiles: states, snapshots and seismograms bit for bit, also when advanced in pieces
+    and with an odd number of row blocks (384 modes) or a part without receiver rows (3
+    receivers).  Width 16: two accumulator sets; width 64: one set staged in TMEM."""
     insts = _instances(9, shapes=[(384, 256, 100), (512, 512, 33), (256, 384, 20)])
     n, dt = 60, 0.5
     rng = np.random.default_rng(10)
@@ -183,7 +185,7 @@ def test_batch_ozaki_paired_tiles_bitwise(shaw):
     out = {}
     for paired in (False, True):
         bt = shaw.RomBatch(insts, precision=shaw.MIXED_OZAKI_BF16)
-        bt.set_tiling(16, paired=paired)
+        bt.set_tiling(width, paired=paired)
         assert ("pair" in bt.describe()) == paired
         for i in range(len(insts)):
             bt.set_snapshots(i, 7, 5, n)
