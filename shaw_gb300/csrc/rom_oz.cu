@@ -1103,98 +1103,99 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         // ---------------- velocity: XV += dt Av XS + fdt b ----------------
         if constexpr (S == 6)
           epi_phase(mv0, mv1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
-        const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
-        const uint32_t row = mt * 128 + q * 32 + lane;
-        const int alpha = in.alpha_v[row];
-        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
-        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-          float ph[8], pl[8], qh[8], ql[8];
-          int pe[8];
+            const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
+            const uint32_t row = mt * 128 + q * 32 + lane;
+            const int alpha = in.alpha_v[row];
+            uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+            for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+              float ph[8], pl[8], qh[8], ql[8];
+              int pe[8];
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
-            const size_t si = (size_t)(j0 + jj) * in.kvp + row;
-            ph[jj] = xvh[si];
-            pl[jj] = xvl[si];
-            qh[jj] = bh[si];
-            ql[jj] = bl[si];
-          }
-          float yh[8], yl[8];
-          fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
-          int b8[8], p8[8];
-          float fh8[8], fl8[8];
-          ld8(sh->beta_s + j0, b8);
-          ld8(sh->pred_v + j0, p8);
-          ld8(sh->fdt_h + j0, fh8);
-          ld8(sh->fdt_l + j0, fl8);
+              for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
+                const size_t si = (size_t)(j0 + jj) * in.kvp + row;
+                ph[jj] = xvh[si];
+                pl[jj] = xvl[si];
+                qh[jj] = bh[si];
+                ql[jj] = bl[si];
+              }
+              float yh[8], yl[8];
+              fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
+              int b8[8], p8[8];
+              float fh8[8], fl8[8];
+              ld8(sh->beta_s + j0, b8);
+              ld8(sh->pred_v + j0, p8);
+              ld8(sh->fdt_h + j0, fh8);
+              ld8(sh->fdt_l + j0, fl8);
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + b8[jj];
-            const size_t si = (size_t)j * in.kvp + row;
-            float xh = ph[jj], xl = pl[jj];
-            float s1, s2;
-            pow2_pair(e, s1, s2);
-            df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-            df_fma(xh, xl, fh8[jj], fl8[jj], qh[jj], ql[jj]);
-            st_f32(xvh + si, xh);
-            st_f32(xvl + si, xl);
-            ph[jj] = xh;
-            pl[jj] = xl;
-            // a column without a prediction is sliced with any exponent: it is re-sliced
-            // exactly after the phase
-            const int pv = p8[jj];
-            pe[jj] = pv != kNoPrediction ? pv : 0;
-            if (snap_v && row < in.kv && col < in.M)
-              st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), (double)xh + (double)xl);
-          }
-          slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
-          note_max8(sh, j0, ph);
-        }
-        return staged;
-      });
+              for (int jj = 0; jj < 8; ++jj) {
+                const uint32_t j = j0 + jj, col = col0 + j;
+                const int e = alpha + b8[jj];
+                const size_t si = (size_t)j * in.kvp + row;
+                float xh = ph[jj], xl = pl[jj];
+                float s1, s2;
+                pow2_pair(e, s1, s2);
+                df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
+                df_fma(xh, xl, fh8[jj], fl8[jj], qh[jj], ql[jj]);
+                st_f32(xvh + si, xh);
+                st_f32(xvl + si, xl);
+                ph[jj] = xh;
+                pl[jj] = xl;
+                // a column without a prediction is sliced with any exponent: it is re-sliced
+                // exactly after the phase
+                const int pv = p8[jj];
+                pe[jj] = pv != kNoPrediction ? pv : 0;
+                if (snap_v && row < in.kv && col < in.M)
+                  st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), (double)xh + (double)xl);
+              }
+              slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
+              note_max8(sh, j0, ph);
+            }
+            return staged;
+          });
         else
           epi_phase(mv0, mv1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
-        const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
-        const uint32_t row = mt * 128 + q * 32 + lane;
-        const int alpha = in.alpha_v[row] - 60;
-        uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
-        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-          double x[8], f[8];
-          int pe[8];
-          unsigned int key[8];
+            const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
+            const uint32_t row = mt * 128 + q * 32 + lane;
+            const int alpha = in.alpha_v[row] - 60;
+            uint8_t* const brow = bvt + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+            for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+              double x[8], f[8];
+              int pe[8];
+              unsigned int key[8];
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
-            const size_t si = (size_t)(j0 + jj) * in.kvp + row;
-            x[jj] = xv64[si];
-            f[jj] = b64[si];
-          }
-          double yH[8], yL[8];
-          fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
-          int b8[8], p8[8];
-          double f8[8];
-          ld8(sh->beta_s + j0, b8);
-          ld8(sh->pred_v + j0, p8);
-          ld8(sh->fdt64 + j0, f8);
+              for (int jj = 0; jj < 8; ++jj) {  // state and forcing loads ahead of the TMEM reads
+                const size_t si = (size_t)(j0 + jj) * in.kvp + row;
+                x[jj] = xv64[si];
+                f[jj] = b64[si];
+              }
+              double yH[8], yL[8];
+              fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
+              int b8[8], p8[8];
+              double f8[8];
+              ld8(sh->beta_s + j0, b8);
+              ld8(sh->pred_v + j0, p8);
+              ld8(sh->fdt64 + j0, f8);
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + b8[jj];
-            // x += dt * y with y = (yH 2^36 + yL) 2^e, then x += fdt * b
-            double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
-            xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
-            xn = fma(f8[jj], f[jj], xn);
-            st_f64(xv64 + (size_t)j * in.kvp + row, xn);
-            x[jj] = xn;
-            key[jj] = max_key64(xn);
-            const int pv = p8[jj];
-            pe[jj] = pv != kNoPrediction ? pv : 0;
-            if (snap_v && row < in.kv && col < in.M) st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), xn);
-          }
-          slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
-          note_max8_keys(sh, j0, key);
-        }
-        return staged;
-      });
+              for (int jj = 0; jj < 8; ++jj) {
+                const uint32_t j = j0 + jj, col = col0 + j;
+                const int e = alpha + b8[jj];
+                // x += dt * y with y = (yH 2^36 + yL) 2^e, then x += fdt * b
+                double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
+                xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
+                xn = fma(f8[jj], f[jj], xn);
+                st_f64(xv64 + (size_t)j * in.kvp + row, xn);
+                x[jj] = xn;
+                key[jj] = max_key64(xn);
+                const int pv = p8[jj];
+                pe[jj] = pv != kNoPrediction ? pv : 0;
+                if (snap_v && row < in.kv && col < in.M)
+                  st_f64(in.snap_vp + row + (size_t)in.kv * (tv + in.Tvp * col), xn);
+              }
+              slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
+              note_max8_keys(sh, j0, key);
+            }
+            return staged;
+          });
         settle(sh->beta_v, sh->pred_v, &sh->reslice_v, &sh->reslice_s, [&](unsigned long long redo) {
           if constexpr (S == 6)
             slice_state(xvh, xvl, in.kvp, nb, sh->beta_v, bvt, redo, mv0 * 128, mv1 * 128);
@@ -1208,114 +1209,115 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
         if (in.seis && in.fseis && n % in.fseis == 0) {
           const unsigned long long tcnt = n / in.fseis - 1;
           epi_phase(mr0, mr1, false, [&](uint32_t mt, uint32_t tcols, uint64_t*) {
-                     const uint32_t r = mt * 128 + q * 32 + lane;
-                     const int alpha = in.alpha_r[r];
-                     for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-                       double v[8];
-                       if constexpr (S == 6) {
-                         float yh[8], yl[8];
-                         load_combine8(tcols, nb, q, j0, yh, yl);
+            const uint32_t r = mt * 128 + q * 32 + lane;
+            const int alpha = in.alpha_r[r];
+            for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+              double v[8];
+              if constexpr (S == 6) {
+                float yh[8], yl[8];
+                load_combine8(tcols, nb, q, j0, yh, yl);
 #pragma unroll
-                         for (int jj = 0; jj < 8; ++jj)
-                           v[jj] = ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]);
-                       } else {
-                         double yH[8], yL[8];
-                         load_combine8_fp64(tcols, nb, q, j0, yH, yL);
+                for (int jj = 0; jj < 8; ++jj)
+                  v[jj] = ldexp((double)yh[jj] + (double)yl[jj], alpha + sh->beta_v[j0 + jj]);
+              } else {
+                double yH[8], yL[8];
+                load_combine8_fp64(tcols, nb, q, j0, yH, yL);
 #pragma unroll
-                         for (int jj = 0; jj < 8; ++jj) {
-                           const int e = alpha + sh->beta_v[j0 + jj] - 60;
-                           v[jj] = fma(scale_pow2(1.0, e + 36), yH[jj], scale_pow2(yL[jj], e));
-                         }
-                       }
+                for (int jj = 0; jj < 8; ++jj) {
+                  const int e = alpha + sh->beta_v[j0 + jj] - 60;
+                  v[jj] = fma(scale_pow2(1.0, e + 36), yH[jj], scale_pow2(yL[jj], e));
+                }
+              }
 #pragma unroll
-                       for (int jj = 0; jj < 8; ++jj) {
-                         const uint32_t col = col0 + j0 + jj;
-                         if (r < in.R && col < in.M) st_f64(in.seis + r + (size_t)in.R * (tcnt + in.Tseis * col), v[jj]);
-                       }
-                     }
-                     return false;
-                   });
+              for (int jj = 0; jj < 8; ++jj) {
+                const uint32_t col = col0 + j0 + jj;
+                if (r < in.R && col < in.M) st_f64(in.seis + r + (size_t)in.R * (tcnt + in.Tseis * col), v[jj]);
+              }
+            }
+            return false;
+          });
           if (epi_any(sh->abort != 0)) break;
         }
         // ---------------- stress: XS += dt As XV ----------------
         if constexpr (S == 6)
           epi_phase(ms0, ms1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
-        const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
-        const uint32_t row = mt * 128 + q * 32 + lane;
-        const int alpha = in.alpha_s[row];
-        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
-        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-          float ph[8], pl[8];
-          int pe[8];
+            const bool staged = stage && stage_accumulator(tcols, spare, nb, q, jbeg, jend, acc_empty);
+            const uint32_t row = mt * 128 + q * 32 + lane;
+            const int alpha = in.alpha_s[row];
+            uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+            for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+              float ph[8], pl[8];
+              int pe[8];
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const size_t si = (size_t)(j0 + jj) * in.ksp + row;
-            ph[jj] = xsh[si];
-            pl[jj] = xsl[si];
-          }
-          float yh[8], yl[8];
-          fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
-          int b8[8], p8[8];
-          ld8(sh->beta_v + j0, b8);
-          ld8(sh->pred_s + j0, p8);
+              for (int jj = 0; jj < 8; ++jj) {
+                const size_t si = (size_t)(j0 + jj) * in.ksp + row;
+                ph[jj] = xsh[si];
+                pl[jj] = xsl[si];
+              }
+              float yh[8], yl[8];
+              fetch_combined8(staged, tcols, spare, nb, q, j0, yh, yl);
+              int b8[8], p8[8];
+              ld8(sh->beta_v + j0, b8);
+              ld8(sh->pred_s + j0, p8);
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + b8[jj];
-            const size_t si = (size_t)j * in.ksp + row;
-            float xh = ph[jj], xl = pl[jj];
-            float s1, s2;
-            pow2_pair(e, s1, s2);
-            df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
-            st_f32(xsh + si, xh);
-            st_f32(xsl + si, xl);
-            ph[jj] = xh;
-            pl[jj] = xl;
-            const int ps = p8[jj];
-            pe[jj] = ps != kNoPrediction ? ps : 0;
-            if (snap_s && row < in.ks && col < in.M)
-              st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), (double)xh + (double)xl);
-          }
-          slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
-          note_max8(sh, j0, ph);
-        }
-        return staged;
-      });
+              for (int jj = 0; jj < 8; ++jj) {
+                const uint32_t j = j0 + jj, col = col0 + j;
+                const int e = alpha + b8[jj];
+                const size_t si = (size_t)j * in.ksp + row;
+                float xh = ph[jj], xl = pl[jj];
+                float s1, s2;
+                pow2_pair(e, s1, s2);
+                df_fma(xh, xl, dth, dtl, yh[jj] * s1 * s2, yl[jj] * s1 * s2);
+                st_f32(xsh + si, xh);
+                st_f32(xsl + si, xl);
+                ph[jj] = xh;
+                pl[jj] = xl;
+                const int ps = p8[jj];
+                pe[jj] = ps != kNoPrediction ? ps : 0;
+                if (snap_s && row < in.ks && col < in.M)
+                  st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), (double)xh + (double)xl);
+              }
+              slice_value8(ph, pl, pe, brow + ((j0 >> 3) << 7), nb);
+              note_max8(sh, j0, ph);
+            }
+            return staged;
+          });
         else
           epi_phase(ms0, ms1, true, [&](uint32_t mt, uint32_t tcols, uint64_t* acc_empty) {
-        const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
-        const uint32_t row = mt * 128 + q * 32 + lane;
-        const int alpha = in.alpha_s[row] - 60;
-        uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
-        for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
-          double x[8];
-          int pe[8];
-          unsigned int key[8];
+            const bool staged = stage && stage_accumulator_fp64(tcols, spare, nb, q, jbeg, jend, acc_empty);
+            const uint32_t row = mt * 128 + q * 32 + lane;
+            const int alpha = in.alpha_s[row] - 60;
+            uint8_t* const brow = bst + (size_t)(row / kKc) * bbytes + bslice_off<S>(nb, 0, 0, row % kKc);
+            for (uint32_t j0 = jbeg; j0 < jend; j0 += 8) {
+              double x[8];
+              int pe[8];
+              unsigned int key[8];
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) x[jj] = xs64[(size_t)(j0 + jj) * in.ksp + row];
-          double yH[8], yL[8];
-          fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
-          int b8[8], p8[8];
-          ld8(sh->beta_v + j0, b8);
-          ld8(sh->pred_s + j0, p8);
+              for (int jj = 0; jj < 8; ++jj) x[jj] = xs64[(size_t)(j0 + jj) * in.ksp + row];
+              double yH[8], yL[8];
+              fetch_combined8_fp64(staged, tcols, spare, nb, q, j0, yH, yL);
+              int b8[8], p8[8];
+              ld8(sh->beta_v + j0, b8);
+              ld8(sh->pred_s + j0, p8);
 #pragma unroll
-          for (int jj = 0; jj < 8; ++jj) {
-            const uint32_t j = j0 + jj, col = col0 + j;
-            const int e = alpha + b8[jj];
-            double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
-            xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
-            st_f64(xs64 + (size_t)j * in.ksp + row, xn);
-            x[jj] = xn;
-            key[jj] = max_key64(xn);
-            const int ps = p8[jj];
-            pe[jj] = ps != kNoPrediction ? ps : 0;
-            if (snap_s && row < in.ks && col < in.M) st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), xn);
-          }
-          slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
-          note_max8_keys(sh, j0, key);
-        }
-        return staged;
-      });
+              for (int jj = 0; jj < 8; ++jj) {
+                const uint32_t j = j0 + jj, col = col0 + j;
+                const int e = alpha + b8[jj];
+                double xn = fma(scale_pow2(a.dt, e), yL[jj], x[jj]);
+                xn = fma(scale_pow2(a.dt, e + 36), yH[jj], xn);
+                st_f64(xs64 + (size_t)j * in.ksp + row, xn);
+                x[jj] = xn;
+                key[jj] = max_key64(xn);
+                const int ps = p8[jj];
+                pe[jj] = ps != kNoPrediction ? ps : 0;
+                if (snap_s && row < in.ks && col < in.M)
+                  st_f64(in.snap_sp + row + (size_t)in.ks * (ts + in.Tsp * col), xn);
+              }
+              slice_value8_fp64(x, pe, brow + ((j0 >> 3) << 7), nb);
+              note_max8_keys(sh, j0, key);
+            }
+            return staged;
+          });
         settle(sh->beta_s, sh->pred_s, &sh->reslice_s, &sh->reslice_v, [&](unsigned long long redo) {
           if constexpr (S == 6)
             slice_state(xsh, xsl, in.ksp, nb, sh->beta_s, bst, redo, ms0 * 128, ms1 * 128);
