@@ -382,7 +382,8 @@ __device__ __forceinline__ float round_int(float x) { return (x + 0x1.8p23f) - 0
 // alone (each step exact: th = 64 h, a = nearest integer of th, h = th - a), then l is
 // folded in at its weight (2^18 after three steps) with one rounded add (error below
 // 2^-42 of the unit), digits 3-5 from that sum.  Digit 0 is in [-64, 64], the others in
-// [-32, 32]: integers, exact in BF16; the expansion matches v to within 2^-37.
+// [-32, 32]: integers, exact in BF16; the expansion matches v to within 2^-37 (the
+// remainder after six digits) + 2^-43 (the rounding of the fold).
 __device__ __forceinline__ void six_digits(float h, float l, float (&a)[6]) {
 #pragma unroll
   for (int s = 0; s < 6; ++s) {
@@ -571,7 +572,8 @@ __device__ __forceinline__ float float_of_int(int a) { return __int_as_float(0x4
 __device__ __forceinline__ uint32_t bf16_of_int(int a) { return __float_as_uint(float_of_int(a)) >> 16; }
 
 // Balanced base-64 digit s (most significant first) of a 54-bit fixed-point value v;
-// v keeps the remainder.  Digit 0 is in [-64, 64], the others in [-32, 32).
+// v keeps the remainder.  Digit 0 is in [-64, 64], digits 1-7 in [-32, 32], the last
+// (the remainder itself) in [-32, 32).
 template <int s>
 __device__ __forceinline__ int take_digit(long long& v) {
   if constexpr (s == 8) {
