@@ -119,3 +119,42 @@ def test_diagonal_sums_exact_in_fp32():
             bound = sum((64 if s == 0 else 32) * (64 if t == 0 else 32) for s, t in pairs) * K
             assert bound < 2 ** 24, (S, d, bound)
     assert 2 * 64 * 32 * K + 7 * 32 * 32 * K == 11 * 2 ** 20
+
+
+def two_sum(a, b):
+    s = F32(a + b)
+    z = F32(s - a)
+    return s, F32(F32(a - F32(s - z)) + F32(b - z))
+
+
+def test_six_diagonal_combine_accuracy():
+    """The 6-slice epilogue's combination of the diagonal sums D_d (integers below 2^24 held
+    in FP32): the terms D_d 2^(6(5-d)) are exact in FP32 and are added smallest first with
+    TwoSum, the errors collected in one FP32 word; hi + lo matches the exact integer sum
+    to 2^-47 of the sum of the terms' magnitudes (2^-48 relative when nothing cancels)."""
+    rng = np.random.default_rng(5)
+    worst = Fraction(0)
+    for trial in range(20000):
+        mag = 2 ** int(rng.integers(0, 24))
+        D = [int(x) for x in rng.integers(-mag, mag, 6)]
+        if trial % 7 == 0:
+            D[0] = 0
+        if trial % 11 == 0:
+            D[:3] = [0, 0, 0]
+        if trial % 13 == 0:  # cancellation between the leading terms
+            D[1] = -64 * D[0] + int(rng.integers(-3, 4))
+            if abs(D[1]) >= 2 ** 24:
+                D[1] = 0
+        s, e = F32(D[5]), F32(0)
+        for d in range(4, -1, -1):
+            s, err = two_sum(s, F32(F32(D[d]) * F32(2.0 ** (6 * (5 - d)))))
+            e = F32(e + err)
+        h = F32(s + e)
+        l = F32(e - F32(h - s))
+        terms = [D[d] * 2 ** (6 * (5 - d)) for d in range(6)]
+        err = abs(Fraction(float(h)) + Fraction(float(l)) - sum(terms))
+        scale = sum(abs(t) for t in terms)
+        assert err <= Fraction(scale, 2 ** 47), (D, float(h), float(l))
+        if scale and abs(sum(terms)) * 2 >= scale:
+            worst = max(worst, err / abs(sum(terms)))
+    assert worst <= Fraction(1, 2 ** 48) * Fraction(11, 10)
