@@ -119,6 +119,12 @@ def test_diagonal_sums_exact_in_fp32():
             bound = sum((64 if s == 0 else 32) * (64 if t == 0 else 32) for s, t in pairs) * K
             assert bound < 2 ** 24, (S, d, bound)
     assert 2 * 64 * 32 * K + 7 * 32 * 32 * K == 11 * 2 ** 20
+    # 9-slice combination in 64-bit integers: H = D0 2^12 + D1 2^6 + D2 (exact as an FP64),
+    # L = sum_{d>=3} D_d 2^(6(8-d)) (one rounding to FP64), Y = H 2^36 + L
+    bound = [sum((64 if s == 0 else 32) * (64 if d - s == 0 else 32) for s in range(d + 1)) * K for d in range(9)]
+    H = bound[0] * 2 ** 12 + bound[1] * 2 ** 6 + bound[2]
+    L = sum(bound[d] * 2 ** (6 * (8 - d)) for d in range(3, 9))
+    assert H < 2 ** 36 and L < 2 ** 54  # each fits an int64; H is exact in FP64
 
 
 def two_sum(a, b):
