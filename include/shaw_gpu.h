@@ -259,6 +259,12 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
  * co-resident CTAs (needs >= 256 modes per dof and 2 x tiles <= SMs, else
  * SHAW_ERR_UNSUPPORTED).  SHAW_ERR_UNSUPPORTED on FP64 batches. */
 int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired);
+/* Diagnostic of failure detection: every wait of the persistent kernels is bounded and
+ * reports a timeout instead of hanging.  One small launch waits, with the same helpers,
+ * on an mbarrier phase that nothing completes and on a global counter that nothing
+ * increments, each for `polls` polls; *status receives the error bits they set (64 and
+ * 128, the codes the ROM kernels report).  The device stays usable afterwards. */
+int shaw_selftest_bounded_waits(uint64_t polls, uint32_t* status);
 /* Reduced-state snapshots of instance i: kv x (nsteps/freq_vp) x M and
  * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */
 int shaw_rom_batch_set_snapshots(shaw_rom_batch_t h, uint32_t i, uint64_t freq_vp, uint64_t freq_sp,

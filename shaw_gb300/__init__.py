@@ -95,6 +95,7 @@ SIGNATURES = [
     ("shaw_rom_batch_destroy", None, [_vp]),
     ("shaw_rom_batch_tune", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64, ctypes.c_char_p, ctypes.c_size_t]),
     ("shaw_rom_batch_set_tiling", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_int]),
+    ("shaw_selftest_bounded_waits", ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32)]),
     ("shaw_rom_batch_set_snapshots", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                                     ctypes.c_uint64, _dp, _dp]),
     ("shaw_rom_batch_set_receivers", ctypes.c_int, [_vp, ctypes.c_uint32, _dp, ctypes.c_uint32, ctypes.c_uint64,

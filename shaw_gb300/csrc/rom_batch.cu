@@ -327,6 +327,14 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
   return SHAW_OK;
 }
 
+int shaw_selftest_bounded_waits(uint64_t polls, uint32_t* status) {
+  if (!status || polls == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "status must be non-null and polls > 0");
+  unsigned int s = 0;
+  if (int rc = shaw::oz::wait_selftest(polls, &s)) return rc;
+  *status = s;
+  return SHAW_OK;
+}
+
 int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (!h->oz) return shaw::fail(SHAW_ERR_UNSUPPORTED, "FP64 batches have no tiling");

@@ -289,19 +289,25 @@ __device__ __forceinline__ bool wait_gate(Shared* sh, uint64_t* gate, uint32_t g
   return true;
 }
 
+// Acquire-poll of a global counter until it reaches target; false when `limit` polls ran out.
+__device__ __forceinline__ bool poll_counter(const unsigned int* ctr, unsigned int target, unsigned long long limit) {
+  for (unsigned long long i = 0; i < limit; ++i) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+    if (v >= target) return true;
+  }
+  return false;
+}
+
 // Producer of a paired tile: wait (bounded) until the peer part's counter of opened level
 // gates (kLevels per new state) has reached `target`.
 __device__ __forceinline__ bool wait_peer(Shared* sh, const unsigned int* ctr, uint32_t target, unsigned int* err) {
-  for (unsigned long long i = 0; i < kWaitLimit; ++i) {
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
-    if (v >= target) {
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-      return true;
-    }
+  if (!poll_counter(ctr, target, kWaitLimit)) {
+    raise(sh, err, 128u);
+    return false;
   }
-  raise(sh, err, 128u);
-  return false;
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  return true;
 }
 
 // 2^e as an FP32 factor pair (e may leave the normal range of one factor).
@@ -1356,6 +1362,25 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
   if (warp == 2) tmem_dealloc(sh->tmem, kTmemCols);
 }
 
+// Diagnostic of the bounded waits, each on an event that never happens: an mbarrier phase
+// that nothing completes (the wait of gates, stages and accumulators) and a global counter
+// that nothing increments (the wait on the peer of a paired tile).  Each must give up after
+// `polls` polls; status gets the error bits the kernel uses for them (64, 128).
+__global__ void oz_wait_selftest_kernel(unsigned long long polls, const unsigned int* ctr, unsigned int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int s = 0u;
+    if (!mbar_wait_n(&bar, 0u, polls)) s |= 64u;      // phase 0: nobody arrives
+    if (!poll_counter(ctr, 1u, polls)) s |= 128u;     // the counter stays 0
+    *status = s;
+  }
+}
+
 // state (hi + lo, [Mp][kp]) -> FP64 LayoutLeft k x M
 __global__ void oz_gather_state_kernel(const float* h, const float* l, uint32_t k, uint32_t M, uint32_t kp,
                                        double* out) {
@@ -1893,6 +1918,21 @@ std::string describe(const Batch* p) {
 }
 
 uint32_t num_ctas(const Batch* p) { return p->ctas; }
+
+int wait_selftest(unsigned long long polls, unsigned int* status) {
+  unsigned int* d = nullptr;
+  SHAW_CUDA(cudaMalloc(&d, 2 * sizeof(unsigned int)));
+  cudaError_t rc = cudaMemset(d, 0, 2 * sizeof(unsigned int));
+  if (rc == cudaSuccess) {
+    oz_wait_selftest_kernel<<<1, 32>>>(polls, d, d + 1);
+    rc = cudaGetLastError();
+  }
+  if (rc == cudaSuccess) rc = cudaDeviceSynchronize();
+  if (rc == cudaSuccess) rc = cudaMemcpy(status, d + 1, sizeof(unsigned int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (rc != cudaSuccess) return fail(SHAW_ERR_CUDA, std::string("bounded-wait self-test: ") + cudaGetErrorString(rc));
+  return SHAW_OK;
+}
 
 void destroy(Batch* p) {
   if (!p) return;

@@ -55,6 +55,9 @@ int set_tiling(Batch* p, uint32_t width, bool paired);
 std::string describe(const Batch* p);
 uint32_t num_ctas(const Batch* p);
 void destroy(Batch* p);
+// One small launch whose bounded waits (an mbarrier phase and a global counter that nothing
+// completes) run out after `polls` polls; *status gets their error bits (64, 128).
+int wait_selftest(unsigned long long polls, unsigned int* status);
 
 }  // namespace oz
 }  // namespace shaw

@@ -202,6 +202,27 @@ def test_batch_ozaki_paired_tiles_bitwise(shaw, width):
         assert np.max(np.abs(ga)) > 0
 
 
+def test_bounded_waits_report_timeouts(shaw):
+    """Failure detection without a fault: the persistent ROM kernels' waits are bounded.
+    A wait on an mbarrier phase that nothing completes and one on a counter that nothing
+    increments each give up after the poll limit and report it (error bits 64 and 128,
+    as the kernels do), and the device stays usable: a tensor-core batch runs right after
+    and matches the FP64 batch."""
+    st = ctypes.c_uint32(0)
+    assert shaw.lib().shaw_selftest_bounded_waits(1 << 14, ctypes.byref(st)) == 0
+    assert st.value == 64 | 128
+    assert shaw.lib().shaw_selftest_bounded_waits(0, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
+    insts = _instances(21, shapes=[(256, 256, 16)])
+    res = {}
+    for p in (shaw.FP64, shaw.OZAKI_FP64):
+        bt = shaw.RomBatch(insts, precision=p)
+        bt.run(0.5, 40)
+        res[p] = bt.get_state(0)
+        bt.close()
+    assert relerr(res[shaw.OZAKI_FP64][0], res[shaw.FP64][0]) <= 1e-12
+    assert relerr(res[shaw.OZAKI_FP64][1], res[shaw.FP64][1]) <= 1e-12
+
+
 def test_batch_tiling_errors(shaw):
     small = _instances(11, shapes=[(128, 256, 40)])
     bt = shaw.RomBatch(small, precision=shaw.MIXED_OZAKI_BF16)
