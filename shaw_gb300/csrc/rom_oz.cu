@@ -166,7 +166,7 @@ struct OzArgs {
   unsigned int* error;
   unsigned long long* tile_ns;  // per tile: device time of its last run
   unsigned int* pair_sync;      // per pair slot: arrival counter (zeroed before each launch)
-  unsigned int* pair_early;     // per pair slot and part: level gates opened (zeroed likewise)
+  unsigned int* pair_levels;    // per pair slot and part: level gates opened (zeroed likewise)
   unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima (zeroed before each launch)
 };
 
@@ -174,7 +174,7 @@ struct Shared {
   uint64_t full[kMaxStages], empty[kMaxStages], acc_full[2], acc_empty[2], drain;
   uint64_t gate_lvl[kLevels], gate_full;  // opened by the epilogue once per new state (see the producer)
   uint32_t meta[kMaxStages];       // per pipeline stage: kMeta* flags
-  int redo[2];                     // per new state (alternating): its early slices were re-sliced
+  int redo[2];                     // per new state (alternating): the settle re-sliced columns
   uint32_t tmem;
   int abort;
   // per-column arrays 16-byte aligned: the epilogue reads them 8 columns at a time
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
     uint8_t* const bvt = a.bvt + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     uint8_t* const bst = a.bst + (size_t)(paired ? slot : blockIdx.x) * a.bscratch;
     unsigned int* const pctr = paired ? a.pair_sync + slot : nullptr;
-    unsigned int* const ectr = paired ? a.pair_early + 2 * slot + part : nullptr;  // this part's level count
+    unsigned int* const ectr = paired ? a.pair_levels + 2 * slot + part : nullptr;  // this part's level count
     unsigned int* const pcol = paired ? a.pair_colmax + (size_t)slot * 4 * kMaxNb : nullptr;  // [parity][part][nb]
 
     if (warp == 0) {
@@ -1672,7 +1672,7 @@ int create(Batch*& p, uint32_t n, const InstanceDesc* d, cudaStream_t s, int sli
   OZ_TRY(cudaMalloc(&b->bst, (size_t)b->sms * b->bscratch));
   OZ_TRY(cudaMalloc(&b->error, sizeof(unsigned int)));
   OZ_TRY(cudaMalloc(&b->tile_ns, b->max_tiles * sizeof(unsigned long long)));
-  OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)2 * b->sms * sizeof(unsigned int)));  // step barrier, early gates
+  OZ_TRY(cudaMalloc(&b->pair_sync, (size_t)2 * b->sms * sizeof(unsigned int)));  // step barrier, level gates
   OZ_TRY(cudaMalloc(&b->pair_colmax, (size_t)b->sms * 4 * kMaxNb * sizeof(unsigned int)));
 #undef OZ_TRY
   b->smem = slices == 6 ? (size_t)Geo<6>::kStages * Geo<6>::kStageBytes + sizeof(Shared)
@@ -1774,7 +1774,7 @@ int advance(Batch* p, cudaStream_t s, double dt, unsigned long long step0, unsig
   a.inst = p->d_inst; a.tiles = p->d_tiles; a.order = p->d_order; a.cta_begin = p->d_begin;
   a.bvt = p->bvt; a.bst = p->bst; a.bscratch = p->bscratch;
   a.dt = dt; a.step0 = step0; a.nsteps = nsteps; a.error = p->error; a.tile_ns = p->tile_ns;
-  a.pair_sync = p->pair_sync; a.pair_early = p->pair_sync + p->sms; a.pair_colmax = p->pair_colmax;
+  a.pair_sync = p->pair_sync; a.pair_levels = p->pair_sync + p->sms; a.pair_colmax = p->pair_colmax;
   void (*kern)(OzArgs) = p->slices == 6 ? rom_rank2_ozaki_kernel<6> : rom_rank2_ozaki_kernel<9>;
   SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->smem));
   if (p->paired) {  // the parts of a pair wait on each other: all CTAs resident (cooperative launch)
