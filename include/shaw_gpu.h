@@ -65,8 +65,13 @@ extern "C" {
 
 /* ---- arithmetic of a run ------------------------------------------------ */
 #define SHAW_FP64             0  /* plain FP64 (the oracle-parity path)                     */
-#define SHAW_MIXED_TF32X3     1  /* ROM: split TF32x3 products, FP32 accumulate, Kahan state */
-#define SHAW_MIXED_BF16X3     2  /* ROM: split BF16x3 products, FP32 accumulate, Kahan state */
+#define SHAW_MIXED_TF32X3     1  /* EXPERIMENTAL, ROM rank 2 only: split TF32x3 products with
+                                    FP32 accumulation.  Kept as a measured negative result:
+                                    the tensor pipe's truncating FP32 accumulation drifts
+                                    (7.5e-6 relative seismogram error after 100 steps at
+                                    k = 512), so it does NOT meet the 1e-6 mixed-precision
+                                    bar; use SHAW_MIXED_OZAKI_BF16.  (Value 2 is unused:
+                                    no BF16x3 form is built, for the same reason.)        */
 #define SHAW_MIXED_FP32       3  /* ROM rank 1: FP32 hi+lo arithmetic; FOM: FP32 state     */
 #define SHAW_MIXED_OZAKI_BF16 4  /* ROM rank 2: BF16 tensor cores, 6 six-bit slices per
                                     operand (Ozaki scheme), exact FP32 accumulation,
@@ -178,13 +183,19 @@ int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const do
  *     d_phi_sp nsp x ks (LayoutLeft), d_rom_jvp kv x ks and d_rom_jsp ks x kv
  *     (row-major).  The work is enqueued on `stream` (a cudaStream_t; 0 is the
  *     default stream) and the call returns without waiting for it.
- *   - The intermediate J*Phi columns pass through one fixed 16 MiB FP64 device
- *     array inside the library; every GPU that loads the library holds it until
- *     the process exits.  One column must fit: nvp and nsp must each be at most
- *     2097152, otherwise the call returns SHAW_ERR_INVALID_ARG.
+ *   - The intermediate J*Phi passes, one block of mesh rows at a time with every
+ *     mode column, through one fixed 16 MiB FP64 device array inside the library;
+ *     every GPU that loads the library holds it until the process exits.  A block
+ *     holds 2097152 / k values per column (k = ks for romJvp, kv for romJsp), so
+ *     any mesh size works; kv and ks must be at most 65535, otherwise the call
+ *     returns SHAW_ERR_INVALID_ARG.  Cost: about 2 (nvp + nsp) kv ks FP64 flops,
+ *     like the allocating path, each basis value read about once.
  *   - It calls no cudaMalloc or cudaFree and no library routine that allocates.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Each call looks up the array's device address on the current device
+ *     (cudaGetSymbolAddress, which does not allocate); the first lookup on a
+ *     device may load the module, so make the first call before any stream
+ *     capture.  The FOM handle is only read: its stencil values do not change
+ *     after shaw_fom_create.
  *   - All calls share the one array: calls whose work overlaps on the GPU (other
  *     streams, or unordered threads) race on it. */
 int shaw_rom_project_noalloc(shaw_fom_t fom, const double* d_phi_vp, uint64_t kv, const double* d_phi_sp,
@@ -263,7 +274,9 @@ int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired);
  * reports a timeout instead of hanging.  One small launch waits, with the same helpers,
  * on an mbarrier phase that nothing completes and on a global counter that nothing
  * increments, each for `polls` polls; *status receives the error bits they set (64 and
- * 128, the codes the ROM kernels report).  The device stays usable afterwards. */
+ * 128, the codes the ROM kernels report).  The device stays usable afterwards.
+ * polls must be in 1 .. 16777216 (2^24, the kernels' own wait limit), else
+ * SHAW_ERR_INVALID_ARG. */
 int shaw_selftest_bounded_waits(uint64_t polls, uint32_t* status);
 /* Reduced-state snapshots of instance i: kv x (nsteps/freq_vp) x M and
  * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */

@@ -39,7 +39,8 @@ ERR_STATE = 13
 
 SIGNAL = {"ricker": 0, "sinusoid": 1, "gaussDer": 2}
 MATERIAL = {"unilayer": 0, "bilayer": 1, "prem": 2}
-FP64, MIXED_TF32X3, MIXED_BF16X3, MIXED_FP32, MIXED_OZAKI_BF16, OZAKI_FP64 = 0, 1, 2, 3, 4, 5
+# MIXED_TF32X3 is experimental: it does not meet the 1e-6 mixed-precision bar (see the C header).
+FP64, MIXED_TF32X3, MIXED_FP32, MIXED_OZAKI_BF16, OZAKI_FP64 = 0, 1, 3, 4, 5
 
 
 class ShawError(RuntimeError):

@@ -289,12 +289,16 @@ __global__ void __launch_bounds__(kThreads) fom_stress_kernel(FomArgs a, uint32_
 // y = Jvp x (Jvp: nvp x nsp) or y = Jsp x (nsp x nvp) on column-major multivectors
 // (one column per blockIdx.y), with the unfolded stencil values: the multivector
 // SpMV of computeRomOperatorsUsingFomJacsWithMatProp (rom_compute_jacobians.hpp:88-101).
-// Per row the products are summed in the CRS entry order (N, S, W, E / A, B).
+// Rows row0 .. row0+nrows-1 of the product are computed (x holds full columns, y
+// holds nrows rows per column).  Per row the products are summed in the CRS entry
+// order (N, S, W, E / A, B).
 __global__ void fom_apply_vp_kernel(const double* __restrict__ craw, const double* __restrict__ x,
-                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp, uint32_t row0,
+                                    uint32_t nrows) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const uint32_t p = row0 + r;
   const size_t nvp = (size_t)nth * nr;
-  if (p >= nvp) return;
   const double* xc = x + (size_t)blockIdx.y * nsp;
   const uint32_t j = p / nth, i = p - j * nth;
   double sum = 0.0;
@@ -309,13 +313,15 @@ __global__ void fom_apply_vp_kernel(const double* __restrict__ craw, const doubl
     sum = __dadd_rn(sum, __dmul_rn(craw[2 * nvp + p], xc[gW]));
     sum = __dadd_rn(sum, __dmul_rn(craw[3 * nvp + p], xc[gE]));
   }
-  y[(size_t)blockIdx.y * nvp + p] = sum;
+  y[(size_t)blockIdx.y * nrows + r] = sum;
 }
 
 __global__ void fom_apply_sp_kernel(const double* __restrict__ craw, const double* __restrict__ x,
-                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nsp) return;
+                                    double* __restrict__ y, uint32_t nth, uint32_t nr, size_t nsp, uint32_t row0,
+                                    uint32_t nrows) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const uint32_t q = row0 + r;
   const size_t nvp = (size_t)nth * nr;
   const double* xc = x + (size_t)blockIdx.y * nvp;
   const uint32_t row = 2 * nth - 1;
@@ -330,7 +336,7 @@ __global__ void fom_apply_sp_kernel(const double* __restrict__ craw, const doubl
   }
   double sum = __dmul_rn(craw[q], xc[gA]);
   sum = __dadd_rn(sum, __dmul_rn(craw[nsp + q], xc[gB]));
-  y[(size_t)blockIdx.y * nsp + q] = sum;
+  y[(size_t)blockIdx.y * nrows + r] = sum;
 }
 
 // dt folded into the stencil values in FP64, then stored in the state's precision.
@@ -979,18 +985,24 @@ uint64_t shaw_fom_kernel_launches(shaw_fom_t h) { return h ? h->launches : 0; }
 namespace shaw {
 
 // Column-major multivector products with the FOM operators (no dt, no forcing):
-// dof 0: y (nvp x ncols) = Jvp x (nsp x ncols); dof 1: y (nsp x ncols) = Jsp x (nvp x ncols).
-int fom_apply(shaw_fom_t h, int dof, const double* x, double* y, uint32_t ncols, cudaStream_t s) {
+// dof 0: y = (Jvp x)[row0 : row0+nrows, :] with x nsp x ncols;
+// dof 1: y = (Jsp x)[row0 : row0+nrows, :] with x nvp x ncols; y is nrows x ncols.
+// The handle is only read (its stencil values are immutable after shaw_fom_create),
+// so a caller may run this on its own stream while another thread steps the FOM.
+int fom_apply(shaw_fom_t h, int dof, const double* x, double* y, uint64_t row0, uint64_t nrows, uint32_t ncols,
+              cudaStream_t s) {
   if (!h || !x || !y) return fail(SHAW_ERR_INVALID_ARG, "null argument");
-  if (ncols == 0) return SHAW_OK;
+  if (ncols == 0 || nrows == 0) return SHAW_OK;
   if (ncols > 65535) return fail(SHAW_ERR_UNSUPPORTED, "at most 65535 columns per operator product");
-  const uint32_t rows = (uint32_t)(dof == 0 ? h->nvp : h->nsp);
-  dim3 grid((rows + 255) / 256, ncols);
+  const uint64_t rows = dof == 0 ? h->nvp : h->nsp;
+  if (row0 > rows || nrows > rows - row0) return fail(SHAW_ERR_INVALID_ARG, "row range outside the operator");
+  dim3 grid((unsigned)((nrows + 255) / 256), ncols);
   if (dof == 0)
-    fom_apply_vp_kernel<<<grid, 256, 0, s>>>(h->cvp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp);
+    fom_apply_vp_kernel<<<grid, 256, 0, s>>>(h->cvp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp,
+                                             (uint32_t)row0, (uint32_t)nrows);
   else
-    fom_apply_sp_kernel<<<grid, 256, 0, s>>>(h->csp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp);
-  h->launches++;
+    fom_apply_sp_kernel<<<grid, 256, 0, s>>>(h->csp_raw, x, y, (uint32_t)h->nth, (uint32_t)h->nr, h->nsp,
+                                             (uint32_t)row0, (uint32_t)nrows);
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;
 }

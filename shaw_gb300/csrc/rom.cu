@@ -25,7 +25,6 @@
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -354,26 +353,6 @@ __global__ void rom_signal_table_kernel(int kind, double delay, double period, d
                                         unsigned long long n, double* table) {
   const unsigned long long s = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
   if (s < n) table[s] = shaw::signal_value(kind, delay, period, (double)(step0 + s) * dt) * dt;
-}
-
-// Reduced-operator block out[i * ldo + j0 + c] = sum_p phi[p + n*i] * tmp[p + n*c] for
-// i < k and c < ncols: one block per output, FP64 tree reduction (no library GEMM).
-__global__ void rom_project_dot_kernel(const double* __restrict__ phi, const double* __restrict__ tmp, uint64_t n,
-                                       double* __restrict__ out, uint64_t ldo, uint64_t j0) {
-  __shared__ double part[kRomWarps];
-  const uint32_t i = blockIdx.x, c = blockIdx.y;
-  const double* a = phi + (size_t)n * i;
-  const double* b = tmp + (size_t)n * c;
-  double acc = 0.0;
-  for (uint64_t p = threadIdx.x; p < n; p += kRomThreads) acc = fma(a[p], b[p], acc);
-  acc = warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double v = threadIdx.x < kRomWarps ? part[threadIdx.x] : 0.0;
-    v = warp_sum(v);
-    if (threadIdx.x == 0) out[(size_t)i * ldo + j0 + c] = v;
-  }
 }
 
 // Rank-2 forcing: XV[:, j] += (f_j(t_{n-1}) * dt) * b[:, j]   (one block per column)
@@ -896,7 +875,7 @@ int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const do
       break;
     }
     // tmp (nvp x ks) = Jvp PhiSp ; romJvp row-major kv x ks == column-major ks x kv = tmp^T PhiVp
-    if ((rc = shaw::fom_apply(fom, 0, ps, tmp, (uint32_t)ks, s))) break;
+    if ((rc = shaw::fom_apply(fom, 0, ps, tmp, 0, nvp, (uint32_t)ks, s))) break;
     if (cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)ks, (int)kv, (int)nvp, &one, tmp, (int)nvp, pv, (int)nvp,
                     &zero, out, (int)ks) != CUBLAS_STATUS_SUCCESS) {
       rc = shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (projection vp)");
@@ -908,7 +887,7 @@ int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const do
     }
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) { rc = shaw::cuda_fail(e, "sync"); break; }
     // tmp (nsp x kv) = Jsp PhiVp ; romJsp row-major ks x kv == column-major kv x ks = tmp^T PhiSp
-    if ((rc = shaw::fom_apply(fom, 1, pv, tmp, (uint32_t)kv, s))) break;
+    if ((rc = shaw::fom_apply(fom, 1, pv, tmp, 0, nsp, (uint32_t)kv, s))) break;
     if (cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)kv, (int)ks, (int)nsp, &one, tmp, (int)nsp, ps, (int)nsp,
                     &zero, out, (int)kv) != CUBLAS_STATUS_SUCCESS) {
       rc = shaw::fail(SHAW_ERR_CUDA, "cublasDgemm (projection sp)");
@@ -934,50 +913,95 @@ int shaw_rom_project(shaw_fom_t fom, const double* phi_vp, uint64_t kv, const do
 // manages every device allocation itself.  For them the projection below keeps
 // its intermediate J * Phi block in one fixed, statically sized device array.
 //
+// The projection runs over blocks of mesh rows: for rows n0 .. n1 of the output
+// dof, T = (J PhiIn)[n0:n1, :] (all k_in columns) goes to the array, and
+// out += PhiOut[n0:n1, :]^T T accumulates in a tiled FP64 kernel, blocks in a fixed
+// order.  Every basis value is read about once, so the cost grows with
+// n * k_in * k_out flops, like the allocating path's DGEMM, for any mesh size.
+//
 // The array lives for as long as the library is loaded, on every GPU that loads
 // it.  Host code must not pass the array's name to a kernel (in host code that
 // name is a host-side stand-in, not a device address): its device address is
-// looked up once per device with cudaGetSymbolAddress.  All calls share the array,
-// so calls whose work overlaps on the GPU (different streams, or threads without
-// ordering) race on it; the array keeps whatever the last call left in it, and
-// every element this code reads is written first within the same call.
+// looked up with cudaGetSymbolAddress on each call, for the current device.  All
+// calls share the array, so calls whose work overlaps on the GPU (different
+// streams, or threads without ordering) race on it; the array keeps whatever the
+// last call left in it, and every element this code reads is written first within
+// the same call.
 namespace {
 
 constexpr uint64_t kProjectScratchDoubles = 1ull << 21;  // 16 MiB of FP64
 static __device__ __align__(256) double g_project_scratch[kProjectScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-double* g_scratch_addr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (set up on first use).
+// Device address of the scratch array on the current device.  The lookup does not
+// allocate; the first one on a device may load the module, so a caller makes its
+// first call before any stream capture.
 int project_scratch(double** out) {
-  int dev = 0;
-  SHAW_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return shaw::fail(SHAW_ERR_UNSUPPORTED, "device index out of range");
-  std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_project_scratch);
-    if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGetSymbolAddress(project scratch)");
-    g_scratch_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_project_scratch);
+  if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGetSymbolAddress(project scratch)");
+  *out = static_cast<double*>(p);
   return SHAW_OK;
 }
 
-// out (k_out x k_in, row-major) = PhiOut^T (J PhiIn), chunked through the scratch array.
-int project_block(shaw_fom_t fom, int dof, const double* phi_in, uint64_t n_in, uint64_t k_in,
-                  const double* phi_out, uint64_t n_out, uint64_t k_out, double* out, double* scratch,
-                  cudaStream_t s) {
-  uint64_t chunk = kProjectScratchDoubles / n_out;
-  if (chunk > 65535) chunk = 65535;
-  for (uint64_t j0 = 0; j0 < k_in; j0 += chunk) {
-    const uint64_t c = (k_in - j0 < chunk) ? k_in - j0 : chunk;
-    int rc = shaw::fom_apply(fom, dof, phi_in + n_in * j0, scratch, (uint32_t)c, s);
+constexpr int kProjTile = 32;  // output tile (k_out x k_in) of one CTA, and rows per K step
+
+// out[i * k_in + j] (=, or += when accumulate) sum_{r < nrows} phi_out[(row0 + r) + n_out * i] * t[r + nrows * j]
+// for i < k_out, j < k_in: a 32 x 32 output tile per CTA, 256 threads with 2 x 2 outputs
+// each, both operands staged through shared memory 32 rows at a time (FP64 FMAs).
+__global__ void __launch_bounds__(256) rom_project_accum_kernel(const double* __restrict__ phi_out, uint64_t n_out,
+                                                                uint64_t row0, uint32_t nrows,
+                                                                const double* __restrict__ t, uint32_t k_out,
+                                                                uint32_t k_in, double* __restrict__ out,
+                                                                int accumulate) {
+  __shared__ double sa[kProjTile][kProjTile + 1];
+  __shared__ double sb[kProjTile][kProjTile + 1];
+  const uint32_t i0 = blockIdx.y * kProjTile, j0 = blockIdx.x * kProjTile;
+  const uint32_t tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+  for (uint32_t r0 = 0; r0 < nrows; r0 += kProjTile) {
+    // 32 rows x 32 columns of each operand: thread (tid & 31) walks the rows (coalesced)
+    for (uint32_t e = tid; e < kProjTile * kProjTile; e += 256) {
+      const uint32_t rr = e & 31, cc = e >> 5;
+      const bool in_r = r0 + rr < nrows;
+      sa[rr][cc] = (in_r && i0 + cc < k_out) ? phi_out[(row0 + r0 + rr) + n_out * (i0 + cc)] : 0.0;
+      sb[rr][cc] = (in_r && j0 + cc < k_in) ? t[(r0 + rr) + (size_t)nrows * (j0 + cc)] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (uint32_t rr = 0; rr < kProjTile; ++rr) {
+      const double a0 = sa[rr][2 * ty], a1 = sa[rr][2 * ty + 1];
+      const double b0 = sb[rr][2 * tx], b1 = sb[rr][2 * tx + 1];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const uint32_t i = i0 + 2 * ty + a, j = j0 + 2 * tx + b;
+      if (i < k_out && j < k_in) {
+        double* o = out + (size_t)i * k_in + j;
+        *o = accumulate ? *o + acc[a][b] : acc[a][b];
+      }
+    }
+}
+
+// out (k_out x k_in, row-major) = PhiOut^T (J PhiIn), over row blocks of the scratch array.
+int project_block(shaw_fom_t fom, int dof, const double* phi_in, uint64_t k_in, const double* phi_out,
+                  uint64_t n_out, uint64_t k_out, double* out, double* scratch, cudaStream_t s) {
+  uint64_t rows = kProjectScratchDoubles / k_in;  // >= 32 for k_in <= 65535
+  rows -= rows % kProjTile;
+  const dim3 grid((unsigned)((k_in + kProjTile - 1) / kProjTile), (unsigned)((k_out + kProjTile - 1) / kProjTile));
+  for (uint64_t n0 = 0; n0 < n_out; n0 += rows) {
+    const uint64_t nb = (n_out - n0 < rows) ? n_out - n0 : rows;
+    int rc = shaw::fom_apply(fom, dof, phi_in, scratch, n0, nb, (uint32_t)k_in, s);
     if (rc) return rc;
-    rom_project_dot_kernel<<<dim3((unsigned)k_out, (unsigned)c), kRomThreads, 0, s>>>(phi_out, scratch, n_out, out,
-                                                                                  k_in, j0);
+    rom_project_accum_kernel<<<grid, 256, 0, s>>>(phi_out, n_out, n0, (uint32_t)nb, scratch, (uint32_t)k_out,
+                                                  (uint32_t)k_in, out, n0 == 0 ? 0 : 1);
     SHAW_CUDA(cudaGetLastError());
   }
   return SHAW_OK;
@@ -989,18 +1013,17 @@ extern "C" int shaw_rom_project_noalloc(shaw_fom_t fom, const double* d_phi_vp, 
                                         uint64_t ks, double* d_rom_jvp, double* d_rom_jsp, void* stream) {
   if (!fom || !d_phi_vp || !d_phi_sp || !d_rom_jvp || !d_rom_jsp)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "null argument");
-  if (kv == 0 || ks == 0 || kv > 65535 || ks > 65535) return shaw::fail(SHAW_ERR_INVALID_ARG, "bad mode counts");
+  if (kv == 0 || ks == 0 || kv > 65535 || ks > 65535)
+    return shaw::fail(SHAW_ERR_INVALID_ARG,
+                      "bad mode counts for the allocation-free projection: kv and ks must be in 1..65535 "
+                      "(a row block of J*Phi with every mode column must fit the 16 MiB scratch array)");
   uint64_t nvp = 0, nsp = 0;
   shaw::fom_sizes(fom, &nvp, &nsp);
-  if (nvp > kProjectScratchDoubles || nsp > kProjectScratchDoubles)
-    return shaw::fail(SHAW_ERR_INVALID_ARG,
-                      "mesh too large for the allocation-free projection: nvp and nsp must be <= 2097152 "
-                      "(one column of J*Phi must fit the 16 MiB scratch array); use shaw_rom_project");
   double* scratch = nullptr;
   int rc = project_scratch(&scratch);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // romJvp (kv x ks) = PhiVp^T (Jvp PhiSp);  romJsp (ks x kv) = PhiSp^T (Jsp PhiVp)
-  if ((rc = project_block(fom, 0, d_phi_sp, nsp, ks, d_phi_vp, nvp, kv, d_rom_jvp, scratch, s))) return rc;
-  return project_block(fom, 1, d_phi_vp, nvp, kv, d_phi_sp, nsp, ks, d_rom_jsp, scratch, s);
+  if ((rc = project_block(fom, 0, d_phi_sp, ks, d_phi_vp, nvp, kv, d_rom_jvp, scratch, s))) return rc;
+  return project_block(fom, 1, d_phi_vp, kv, d_phi_sp, nsp, ks, d_rom_jsp, scratch, s);
 }

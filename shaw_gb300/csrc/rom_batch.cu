@@ -329,6 +329,10 @@ int shaw_rom_batch_tune(shaw_rom_batch_t h, double dt, uint64_t trial_steps, cha
 
 int shaw_selftest_bounded_waits(uint64_t polls, uint32_t* status) {
   if (!status || polls == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "status must be non-null and polls > 0");
+  // the kernels' own limit: a larger count would let the self-test spin far longer
+  // than any wait of the ROM kernels can
+  if (polls > (1ull << 24))
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "polls must be at most 16777216 (the kernels' wait limit)");
   unsigned int s = 0;
   if (int rc = shaw::oz::wait_selftest(polls, &s)) return rc;
   *status = s;

@@ -167,7 +167,8 @@ struct OzArgs {
   unsigned long long* tile_ns;  // per tile: device time of its last run
   unsigned int* pair_sync;      // per pair slot: arrival counter (zeroed before each launch)
   unsigned int* pair_levels;    // per pair slot and part: level gates opened (zeroed likewise)
-  unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima (zeroed before each launch)
+  unsigned int* pair_colmax;    // per pair slot: [5][kMaxNb] column maxima; not zeroed: each part writes
+                                // its maxima before the step barrier that its peer waits on before reading
 };
 
 struct Shared {

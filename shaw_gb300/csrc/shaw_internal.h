@@ -16,7 +16,8 @@ int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 
 // Column-major multivector products with a FOM handle's operators (fom.cu).
-int fom_apply(shaw_fom_t h, int dof, const double* x, double* y, uint32_t ncols, cudaStream_t s);
+int fom_apply(shaw_fom_t h, int dof, const double* x, double* y, uint64_t row0, uint64_t nrows, uint32_t ncols,
+              cudaStream_t s);
 void fom_sizes(shaw_fom_t h, uint64_t* nvp, uint64_t* nsp);
 
 #define SHAW_CUDA(call)                                   \

@@ -7,7 +7,7 @@ tree is absent.  Usage:
 
     python tests/golden/make_fixtures.py [REFERENCE_ROOT]
 
-REFERENCE_ROOT defaults to /root/reference.
+REFERENCE_ROOT defaults to $SHAW_REFERENCE_ROOT (tests/oracle_lib.py:reference_root).
 """
 import hashlib
 import json
@@ -174,4 +174,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.dirname(HERE))
+    from oracle_lib import reference_root
+    main(sys.argv[1] if len(sys.argv) > 1 else reference_root())

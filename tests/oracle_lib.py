@@ -24,6 +24,13 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _lib = None
 
 
+def reference_root():
+    """Root of the reference source tree: $SHAW_REFERENCE_ROOT, else the recipes' default
+    location.  Only fixture scripts, the pinning tests and the oracle recipe read it; the
+    GPU tests, smoke() and the benchmark never do."""
+    return os.environ.get("SHAW_REFERENCE_ROOT", "/root/reference")
+
+
 def _ptr(a, t):
     if a is None:
         return ctypes.cast(None, t)

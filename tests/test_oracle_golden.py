@@ -13,9 +13,10 @@ import pytest
 
 from cases import CASES, as_text_layout, parse_case, run_case
 from conftest import GOLDEN, mesh_dir
+from oracle_lib import reference_root
 
 UNIT = json.load(open(os.path.join(GOLDEN, "unit_golds.json")))
-REF_TESTS = "/root/reference/tests"
+REF_TESTS = os.path.join(reference_root(), "tests")
 
 
 def _mesh(oracle, name, rho=1.0, vs=1.0):

@@ -212,6 +212,9 @@ def test_bounded_waits_report_timeouts(shaw):
     assert shaw.lib().shaw_selftest_bounded_waits(1 << 14, ctypes.byref(st)) == 0
     assert st.value == 64 | 128
     assert shaw.lib().shaw_selftest_bounded_waits(0, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
+    # beyond the kernels' own wait limit (2^24 polls): refused before any launch
+    assert shaw.lib().shaw_selftest_bounded_waits((1 << 24) + 1, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
+    assert shaw.lib().shaw_selftest_bounded_waits(2 ** 64 - 1, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
     insts = _instances(21, shapes=[(256, 256, 16)])
     res = {}
     for p in (shaw.FP64, shaw.OZAKI_FP64):
