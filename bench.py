@@ -160,32 +160,89 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(np, budget_s=20.0):
-    """The oracle's CRS leapfrog on a bounded sample of the same workload, all host threads."""
+def host_cpu():
+    """CPU model and core counts of this host, recorded beside every CPU timing."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=20).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for ln in fh:
+                    if ln.lower().startswith(("model name", "cpu part")):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return {"model": model or platform.processor() or platform.machine(), "nproc": os.cpu_count(),
+            "machine": platform.machine()}
+
+
+def omp_binding():
+    """Thread placement of the reference's scaling runs (python_scripts_revise/utils.py:72-74);
+    set before any OpenMP runtime starts in this process."""
+    os.environ.setdefault("OMP_PROC_BIND", "spread")
+    os.environ.setdefault("OMP_PLACES", "threads")
+    return {k: os.environ[k] for k in ("OMP_PROC_BIND", "OMP_PLACES")}
+
+
+def oracle_workload(np, world=1):
+    """The benchmark workload built with the oracle alone (its own mesher, material,
+    mappers): rank 0's M forcing columns of the job's world * M seeded draws."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
-    import shaw_gb300 as shaw
     oracle_lib.build()
-    mesh = shaw.Mesh.generate(NTH, NR)
     with tempfile.TemporaryDirectory() as d:
-        mesh.write(d)
+        oracle_lib.write_full_mesh(NTH, NR, d)
         om = oracle_lib.OracleMesh(d)
     om.set_material("unilayer", [(MATERIAL[0:3], MATERIAL[3:6])])
-    threads = oracle_lib.lib().orc_num_threads(0)
-    ms = 16  # forcing columns in the sample
-    xv = np.zeros((om.nvp, ms))
-    xs = np.random.default_rng(1).standard_normal((om.nsp, ms))
-    dt = 0.01
-    om.fom_advance(xv, xs, 1, dt)  # first touch
-    steps, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < budget_s and steps < 200:
-        om.fom_advance(xv, xs, 1, dt)
-        steps += 1
+    rng = np.random.default_rng(SEED)
+    depths = rng.uniform(200.0, 700.0, M * world)[:M]
+    periods = rng.uniform(30.0, 90.0, M * world)[:M]
+    gids = [om.map_source(float(x), 0.0) for x in depths]
+    rcv = [om.map_receiver(float(a)) for a in range(0, 181)]
+    dt = 0.25 * min(om.info[5], om.info[4] * om.info[2]) / (2.0 ** 0.5 * 7300.0)
+    return oracle_lib, om, gids, periods, rcv, dt
+
+
+def oracle_steps(np, om, gids, periods, rcv, dt, warmup, steps=None, budget_s=None):
+    """Time full leapfrog steps of all M columns on the host cores (the oracle's CRS
+    SpMM leapfrog with the forcing and the 181-receiver gather of every step): `warmup`
+    untimed steps, then `steps` timed ones (or as many as fit in budget_s)."""
+    xv = np.zeros((om.nvp, M))
+    xs = np.zeros((om.nsp, M))
+    kinds = [2] * M
+    om.fom_advance_forced(xv, xs, 0, warmup, dt, gids, kinds, periods, 180.0, rcv)
+    done = warmup
+    if steps is None:  # size the sample from one timed step
+        t0 = time.perf_counter()
+        om.fom_advance_forced(xv, xs, done, 1, dt, gids, kinds, periods, 180.0, rcv)
+        done += 1
+        steps = int(max(2, min(200, budget_s / max(time.perf_counter() - t0, 1e-3))))
+    t0 = time.perf_counter()
+    om.fom_advance_forced(xv, xs, done, steps, dt, gids, kinds, periods, 180.0, rcv)
     el = time.perf_counter() - t0
-    units = (om.nvp + om.nsp) * ms * steps
+    return steps, el
+
+
+def cpu_baseline(np, budget_s=12.0):
+    """The oracle's leapfrog on the same workload (all 256 columns), all host threads, a
+    bounded number of steps."""
+    orc, om, gids, periods, rcv, dt = oracle_workload(np)
+    threads = orc.lib().orc_num_threads(0)
+    steps, el = oracle_steps(np, om, gids, periods, rcv, dt, 2, budget_s=budget_s)
+    units = (om.nvp + om.nsp) * M * steps
     return dict(value=units / el, unit="DOF-updates/s", cores=threads, kind="port",
-                sample="%d leapfrog steps of %d of the 256 forcing columns on the 1000x2000 grid (%.1f s)"
-                       % (steps, ms, el), seconds=el, steps=steps)
+                sample="%d leapfrog steps of all %d forcing columns on the 1000x2000 grid, forcing and "
+                       "181-receiver gather every step (%.1f s)" % (steps, M, el),
+                cpu=host_cpu(), omp=omp_binding())
 
 
 def _timed(torch, stream_ptr, fn):
@@ -212,38 +269,63 @@ def stable_rom(np, k, seed, smin, smax):
     return av, -av.T.copy()
 
 
+def oracle_mesh(nth, nr):
+    """The oracle's own copy of a generated grid (mesher, material and operators of the
+    oracle), for the error legs."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    oracle_lib.build()
+    with tempfile.TemporaryDirectory() as d:
+        oracle_lib.write_full_mesh(nth, nr, d)
+        om = oracle_lib.OracleMesh(d)
+    om.set_material("unilayer", [(MATERIAL[0:3], MATERIAL[3:6])])
+    return oracle_lib, om
+
+
+def fom_rank1_config1(np, torch, shaw, nth, nr, n=2000):
+    """Config 1: FOM rank 1, one gaussDer source at 640 km on the axis (period 60 s, delay
+    180 s), 181 surface receivers, 2000 steps; then the same run against the oracle."""
+    mesh = shaw.Mesh.generate(nth, nr)
+    mesh.set_material("unilayer", MATERIAL)
+    dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
+    src = mesh.map_source(640.0, 0.0)
+    rcv = [mesh.map_receiver(float(a)) for a in range(181)]
+    f = shaw.Fom(mesh, 1, 1)
+    f.set_sources([src], "gaussDer", 60.0, 180.0)
+    f.set_receivers(rcv, 1, n)
+    f.run(dt, n)  # warm-up (graph instantiation)
+    f.reset()
+    l0 = f.kernel_launches
+    t = _timed(torch, f.stream, lambda: f.advance(dt, n))
+    f.synchronize()
+    launches = f.kernel_launches - l0
+    seis = f.seismogram()
+    vp, sp = f.get_state()
+    f.close()
+    _, om = oracle_mesh(nth, nr)
+    ref = om.fom_run(1, n, dt, [src], [2], [60.0], [180.0], rcv, 1, 0, 0)
+    return {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t, "steps": n,
+            "us_per_step": t / n * 1e6, "launches": launches,
+            "max_rel_err_vs_oracle": {"seismogram": _relerr(np, seis, ref["seis"]),
+                                      "state_vp": _relerr(np, vp, ref["final_vp"]),
+                                      "state_sp": _relerr(np, sp, ref["final_sp"]),
+                                      "compared": "the timed 2000-step run, 181 receivers every step"}}
+
+
 def extra_workloads(np, torch, shaw):
-    """The other configurations, each timed with CUDA events on its handle's stream."""
+    """The other configurations, each timed with CUDA events on its handle's stream, each
+    FP64 result with its error against the oracle, each mixed result with its error
+    against an FP64-grade form over the configured number of steps."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    oracle_lib.build()
     out = {}
-    # config 1: FOM rank-1 FP64, 101 theta x 201 r, one gaussDer source at 640 km on the axis
+    # config 1 as worded (101 theta x 201 r) and on the reference fixture's orientation
+    out["fom_rank1_101x201"] = fom_rank1_config1(np, torch, shaw, 101, 201)
+    out["fom_rank1_fixture_201x101"] = fom_rank1_config1(np, torch, shaw, 201, 101)
     mesh = shaw.Mesh.generate(101, 201)
     mesh.set_material("unilayer", MATERIAL)
     dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
-    n = 2000
-    f = shaw.Fom(mesh, 1, 1)
-    f.set_sources([mesh.map_source(640.0, 0.0)], "gaussDer", 60.0, 180.0)
-    f.set_receivers([mesh.map_receiver(float(a)) for a in range(181)], 1, n)
-    f.run(dt, n)  # warm-up (graph instantiation)
-    f.reset()
-    t = _timed(torch, f.stream, lambda: f.advance(dt, n))
-    f.synchronize()
-    out["fom_rank1_101x201"] = {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t,
-                                "steps": n, "us_per_step": t / n * 1e6}
-    f.close()
-    # the same job on the reference's fixture orientation (tests/fullMesh101x201: 201 theta x 101 r)
-    fx = shaw.Mesh.generate(201, 101)
-    fx.set_material("unilayer", MATERIAL)
-    dtx = 0.25 * min(fx.info[5], fx.info[4] * fx.info[2]) / (2.0 ** 0.5 * 7300.0)
-    f = shaw.Fom(fx, 1, 1)
-    f.set_sources([fx.map_source(640.0, 0.0)], "gaussDer", 60.0, 180.0)
-    f.set_receivers([fx.map_receiver(float(a)) for a in range(181)], 1, n)
-    f.run(dtx, n)
-    f.reset()
-    t = _timed(torch, f.stream, lambda: f.advance(dtx, n))
-    f.synchronize()
-    out["fom_rank1_fixture_201x101"] = {"metric": "FOM DOF-updates/s", "value": (fx.nvp + fx.nsp) * n / t,
-                                        "steps": n, "us_per_step": t / n * 1e6}
-    f.close()
     basis = pod_basis(np, shaw, mesh, dt)
     rcv = [mesh.map_receiver(float(a)) for a in range(181)]
     rho_inv = mesh.arrays()["rho_inv_vp"]
@@ -268,55 +350,92 @@ def extra_workloads(np, torch, shaw):
         r.reset()
         t = _timed(torch, r.stream, lambda: r.advance(dt, n))
         r.synchronize()
-        res[prec] = (t, r.seismogram())
+        res[prec] = (t, r.seismogram(), r.get_state())
         r.close()
+    ref = oracle_lib.rom_run(av, as_, b.reshape(k, 1), n, dt, [2], [period], [180.0], freq_vp=1)
+    ref_seis = np.einsum("rk,kt->rt", rows, ref["snaps_vp"][:, :, 0])[:, :, None]
     out["rom_rank1_k256"] = {"metric": "ROM forcing-steps/s", "steps": n,
                              "fp64": n / res[shaw.FP64][0], "mixed_fp32": n / res[shaw.MIXED_FP32][0],
                              "speedup": res[shaw.FP64][0] / res[shaw.MIXED_FP32][0],
                              "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
                              "seismogram_max_abs": float(np.max(np.abs(res[shaw.FP64][1]))),
+                             "fp64_max_rel_err_vs_oracle": {
+                                 "seismogram": _relerr(np, res[shaw.FP64][1], ref_seis),
+                                 "state_vp": _relerr(np, res[shaw.FP64][2][0][:, 0], ref["final_vp"][:, 0]),
+                                 "state_sp": _relerr(np, res[shaw.FP64][2][1][:, 0], ref["final_sp"][:, 0]),
+                                 "compared": "the timed 20000-step run (oracle: the reference's GEMV loop)"},
                              "forcing": {"depth_km": depth, "period_s": period, "delay_s": 180.0},
                              "cpu_oracle": rom_cpu_oracle(np, av, as_, b, 2000, dt, period),
                              "basis": basis["info"]}
-    # config 4: ROM rank-2, k = 512, M = 4096 forcings; FP64 (DGEMM) vs tensor-core forms
-    k, M, n = 512, 4096, 100
+    out["rom_rank2_k512_M4096"] = rom_rank2_config4(np, torch, shaw, oracle_lib, mesh, dt, basis, forcing_vectors,
+                                                    rcv)
+    out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
+    out["fom_rank2_2000x4000_M64"] = fom_fp64_vs_fp32(np, torch, shaw)
+    return out
+
+
+def rom_rank2_config4(np, torch, shaw, oracle_lib, mesh, dt, basis, forcing_vectors, rcv, k=512, M=4096, n=100,
+                      n_long=20000, n_cross=2000, n_oracle_cols=256):
+    """Config 4: k = 512, M = 4096 forcings.  Throughput of each form over n steps; FP64
+    forms against the oracle (first n_oracle_cols columns, n steps); the mixed form over the
+    configured n_long steps against the FP64-grade Ozaki form, which is itself checked
+    against the DGEMM path over n_cross steps (seismograms every 100 steps)."""
     rng = np.random.default_rng(SEED + 4)
     depths, periods = rng.uniform(200.0, 700.0, M), rng.uniform(30.0, 90.0, M)
     av, as_ = basis["av"][:k, :k], basis["as"][:k, :k]
     b = forcing_vectors(k, [mesh.map_source(float(d), 0.0) for d in depths])
-    rows = basis["phi_v"][rcv, :k]
+    rows = np.ascontiguousarray(basis["phi_v"][rcv, :k])
     res = {}
     for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.OZAKI_FP64, shaw.MIXED_TF32X3):
         r = shaw.Rom(av, as_, b, rank=2, precision=prec)
         r.set_signals("gaussDer", periods, 180.0)
-        r.set_snapshots(n // 4, n // 4, n)
         r.reset()
         r.advance(dt, 2 if prec == shaw.FP64 else n)  # warm-up
         r.synchronize()
         r.reset()
         t = _timed(torch, r.stream, lambda: r.advance(dt, n))
         r.synchronize()
-        snaps = r.snapshots()[0]
-        res[prec] = (t, np.einsum("rk,ktm->rtm", rows, snaps), r.get_state()[0])
+        res[prec] = (t, r.get_state())
         r.close()
+    ref = oracle_lib.rom_run(av, as_, b[:, :n_oracle_cols], n, dt, [2] * n_oracle_cols, periods[:n_oracle_cols],
+                             [180.0] * n_oracle_cols)
+
+    def vs_oracle(state):
+        return {"state_vp": _relerr(np, state[0][:, :n_oracle_cols], ref["final_vp"]),
+                "state_sp": _relerr(np, state[1][:, :n_oracle_cols], ref["final_sp"])}
+
+    def long_seis(prec, nsteps, freq=100):
+        r = shaw.Rom(av, as_, b, rank=2, precision=prec)
+        r.set_signals("gaussDer", periods, 180.0)
+        r.set_receivers(rows, freq, nsteps)
+        r.run(dt, nsteps)
+        s = r.seismogram()
+        r.close()
+        return s
+
+    s_oz_long, s_f64_long = long_seis(shaw.MIXED_OZAKI_BF16, n_long), long_seis(shaw.OZAKI_FP64, n_long)
+    s_f64_cross, s_dgemm_cross = long_seis(shaw.OZAKI_FP64, n_cross), long_seis(shaw.FP64, n_cross)
     t64 = res[shaw.FP64][0]
-    out["rom_rank2_k512_M4096"] = {
+    return {
         "metric": "ROM forcing-steps/s", "steps": n, "fp64": M * n / t64,
         "ozaki_bf16": M * n / res[shaw.MIXED_OZAKI_BF16][0], "ozaki_fp64": M * n / res[shaw.OZAKI_FP64][0],
-        "tf32x3": M * n / res[shaw.MIXED_TF32X3][0],
+        "tf32x3_experimental": M * n / res[shaw.MIXED_TF32X3][0],
         "speedup_ozaki": t64 / res[shaw.MIXED_OZAKI_BF16][0], "speedup_ozaki_fp64": t64 / res[shaw.OZAKI_FP64][0],
-        "speedup_tf32x3": t64 / res[shaw.MIXED_TF32X3][0],
-        "seismogram_rel_err_ozaki": _relerr(np, res[shaw.MIXED_OZAKI_BF16][1], res[shaw.FP64][1]),
-        "seismogram_rel_err_ozaki_fp64": _relerr(np, res[shaw.OZAKI_FP64][1], res[shaw.FP64][1]),
-        "state_rel_err_ozaki_fp64": _relerr(np, res[shaw.OZAKI_FP64][2], res[shaw.FP64][2]),
-        "seismogram_rel_err_tf32x3": _relerr(np, res[shaw.MIXED_TF32X3][1], res[shaw.FP64][1]),
         "algorithmic_tflops_ozaki": 4.0 * k * k * M * n / res[shaw.MIXED_OZAKI_BF16][0] / 1e12,
         "algorithmic_tflops_ozaki_fp64": 4.0 * k * k * M * n / res[shaw.OZAKI_FP64][0] / 1e12,
+        "fp64_max_rel_err_vs_oracle": dict(vs_oracle(res[shaw.FP64][1]), compared=
+                                           "final states after the timed %d steps, first %d of %d columns"
+                                           % (n, n_oracle_cols, M)),
+        "ozaki_fp64_max_rel_err_vs_oracle": dict(vs_oracle(res[shaw.OZAKI_FP64][1]), compared=
+                                                 "final states after the timed %d steps, first %d of %d columns"
+                                                 % (n, n_oracle_cols, M)),
+        "ozaki_fp64_seismogram_rel_err_vs_dgemm": {"value": _relerr(np, s_f64_cross, s_dgemm_cross),
+                                                   "steps": n_cross, "samples_every": 100},
+        "ozaki_bf16_seismogram_rel_err_vs_ozaki_fp64": {"value": _relerr(np, s_oz_long, s_f64_long),
+                                                        "steps": n_long, "samples_every": 100},
+        "tf32x3_state_rel_err_vs_fp64": _relerr(np, res[shaw.MIXED_TF32X3][1][0], res[shaw.FP64][1][0]),
         "cpu_oracle": rom_cpu_oracle(np, av, as_, b[:, :64], 60, dt, periods[:64]),
         "basis": "leading 512 modes of the POD basis of config 3"}
-    out["rom_batch_64_uneven"] = batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv)
-    out["fom_rank2_2000x4000_M64"] = fom_fp64_vs_fp32(np, torch, shaw)
-    return out
 
 
 def rom_cpu_oracle(np, av, as_, b, nsteps, dt, periods):
@@ -359,11 +478,19 @@ def fom_fp64_vs_fp32(np, torch, shaw, nth=2000, nr=4000, M=64, n_time=20, n_err=
         f.reset()
         t = _timed(torch, f.stream, lambda: f.advance(dt, n_time))
         f.synchronize()
+        timed_state = f.get_state() if prec == shaw.FP64 else None
         f.run(dt, n_err)
-        res[prec] = (t, f.seismogram())
+        res[prec] = (t, f.seismogram(), timed_state)
         f.close()
+    _, om = oracle_mesh(nth, nr)
+    ref = om.fom_run(2, n_time, dt, gids, [2] * M, periods, [180.0] * M, [], 0, 0, 0)
+    vp, sp = res[shaw.FP64][2]
+    err64 = {"state_vp": _relerr(np, vp, ref["final_vp"]), "state_sp": _relerr(np, sp, ref["final_sp"]),
+             "compared": "final state of the timed %d-step FP64 run from rest, all %d columns" % (n_time, M)}
+    del ref, vp, sp, om
     v64, v32 = dofs * n_time / res[shaw.FP64][0], dofs * n_time / res[shaw.MIXED_FP32][0]
     return {"metric": "FOM DOF-updates/s", "grid": [nth, nr], "forcings": M, "fp64": v64, "mixed_fp32": v32,
+            "fp64_max_rel_err_vs_oracle": err64,
             "speedup": v32 / v64, "timed_steps": n_time,
             "trace_rel_err_fp32": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
             "error_probe": "velocity at the 64 source points and 7 km above them, every step",
@@ -403,11 +530,15 @@ def pod_basis(np, shaw, mesh, dt, kmax=1024, n_train=8):
     return {"phi_v": phi_v, "phi_s": phi_s, "av": av, "as": as_, "info": info}
 
 
-def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_inst=64, seed=20261205):
+def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_inst=64, seed=20261205,
+                     n_long=20000, n_cross=100, seis_freq=500):
     """64 reduced systems, k ~ U{64, 128, ..., 1024}, M ~ U[16, 2048] (seeded), each the
     leading k modes of the POD basis with its own M axis sources (depth U[200,700] km,
     period U[30,90] s), advanced together: FP64 (cuBLAS DGEMM per instance) vs the Ozaki
-    tensor-core batch (one persistent launch, autotuned tile widths and schedule)."""
+    tensor-core batch (one persistent launch, autotuned tile widths and schedule).
+    Errors: the mixed form against the FP64-grade form over the configured n_long steps,
+    and the FP64-grade form against the DGEMM batch over n_cross steps (seismograms of 37
+    receivers, every 5 degrees, every seis_freq / 100 steps)."""
     rng = np.random.default_rng(seed)
     ks = rng.integers(1, 17, n_inst) * 64
     Ms = rng.integers(16, 2049, n_inst)
@@ -419,79 +550,87 @@ def batched_workload(np, torch, shaw, mesh, dt, basis, forcing_vectors, rcv, n_i
                           kind="gaussDer", period=rng.uniform(30.0, 90.0, M), delay=180.0))
     flops = float(sum(4.0 * k * k * M for k, M in zip(ks, Ms)))
     cols = int(Ms.sum())
-    dtr, n64, n_oz, n_cmp = dt, 6, 120, 6
-    rows = {i: basis["phi_v"][rcv, :int(ks[i])] for i in range(n_inst)}
+    n64, n_oz = 6, 120
+    rows = {i: np.ascontiguousarray(basis["phi_v"][rcv[::5], :int(ks[i])]) for i in range(n_inst)}
     res = {}
     for prec in (shaw.FP64, shaw.MIXED_OZAKI_BF16, shaw.OZAKI_FP64):
         bt = shaw.RomBatch(insts, precision=prec)
-        report = bt.tune(dtr, 4) if prec != shaw.FP64 else ""
+        report = bt.tune(dt, 4) if prec != shaw.FP64 else ""
         bt.reset()
-        bt.advance(dtr, 2)  # warm-up
+        bt.advance(dt, 2)  # warm-up
         bt.synchronize()
         bt.reset()
         n = n64 if prec == shaw.FP64 else n_oz
         l0 = bt.kernel_launches
-        t = _timed(torch, bt.stream, lambda: bt.advance(dtr, n))
+        t = _timed(torch, bt.stream, lambda: bt.advance(dt, n))
         bt.synchronize()
         launches = bt.kernel_launches - l0
-        # states after n_cmp steps for the accuracy comparison
-        bt.reset()
-        bt.advance(dtr, n_cmp)
-        bt.synchronize()
-        seis = [rows[i] @ bt.get_state(i)[0] for i in range(n_inst)]
-        res[prec] = dict(t=t, n=n, seis=seis, describe=bt.describe(), report=report, launches=launches)
+        res[prec] = dict(t=t, n=n, describe=bt.describe(), report=report, launches=launches)
         bt.close()
+
+    def seismograms(prec, nsteps, freq):
+        bt = shaw.RomBatch(insts, precision=prec)
+        for i in range(n_inst):
+            bt.set_receivers(i, rows[i], freq, nsteps)
+        bt.run(dt, nsteps)
+        out = [bt.seismogram(i) for i in range(n_inst)]
+        bt.close()
+        return out
+
+    t0 = time.perf_counter()
+    s_oz, s_f64 = seismograms(shaw.MIXED_OZAKI_BF16, n_long, seis_freq), seismograms(shaw.OZAKI_FP64, n_long, seis_freq)
+    err_long = max(_relerr(np, a, b) for a, b in zip(s_oz, s_f64))
+    del s_oz, s_f64
+    c_f64, c_dgemm = seismograms(shaw.OZAKI_FP64, n_cross, 1), seismograms(shaw.FP64, n_cross, 1)
+    err_cross = max(_relerr(np, a, b) for a, b in zip(c_f64, c_dgemm))
+    t_err = time.perf_counter() - t0
     r64, roz, rof = res[shaw.FP64], res[shaw.MIXED_OZAKI_BF16], res[shaw.OZAKI_FP64]
-    err = max(_relerr(np, a, b) for a, b in zip(roz["seis"], r64["seis"]))
-    err_f = max(_relerr(np, a, b) for a, b in zip(rof["seis"], r64["seis"]))
     v64, voz, vof = cols * r64["n"] / r64["t"], cols * roz["n"] / roz["t"], cols * rof["n"] / rof["t"]
     return {"metric": "ROM forcing-steps/s", "instances": n_inst, "total_forcings": cols,
             "k_range": [int(ks.min()), int(ks.max())], "M_range": [int(Ms.min()), int(Ms.max())],
             "fp64": v64, "ozaki_bf16": voz, "speedup_ozaki": voz / v64,
-            "ozaki_fp64": vof, "speedup_ozaki_fp64": vof / v64, "seismogram_rel_err_ozaki_fp64": err_f,
+            "ozaki_fp64": vof, "speedup_ozaki_fp64": vof / v64,
             "algorithmic_tflops_ozaki_fp64": flops * rof["n"] / rof["t"] / 1e12, "tiling_ozaki_fp64": rof["describe"],
             "fp64_steps": r64["n"], "ozaki_steps": roz["n"], "ozaki_launches": roz["launches"],
             "algorithmic_tflops_fp64": flops * r64["n"] / r64["t"] / 1e12,
             "algorithmic_tflops_ozaki": flops * roz["n"] / roz["t"] / 1e12,
-            "seismogram_rel_err_ozaki": err, "error_after_steps": n_cmp,
+            "ozaki_bf16_seismogram_rel_err_vs_ozaki_fp64": {"value": err_long, "steps": n_long,
+                                                            "samples_every": seis_freq, "receivers": len(rcv[::5]),
+                                                            "instances": n_inst},
+            "ozaki_fp64_seismogram_rel_err_vs_dgemm": {"value": err_cross, "steps": n_cross, "samples_every": 1,
+                                                       "receivers": len(rcv[::5]), "instances": n_inst},
+            "error_legs_seconds": t_err,
             "tiling": roz["describe"], "autotuner": roz["report"].strip().split("\n")}
 
 
 def run_reference(args):
+    """The reference arm: the oracle's restatement of the reference's CRS leapfrog (the
+    reference's Kokkos build cannot be made here) on the host cores, on the same workload
+    as our arm (mesh, material, sources, receivers built by the oracle; the product library
+    is never loaded).  Rank 0 alone runs it."""
     import numpy as np
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    per_step_budget = max(2.0, min(20.0, 150.0 / max(1, args.steps + args.warmup)))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
-    import shaw_gb300 as shaw
-    oracle_lib.build()
-    shaw.build()
-    mesh = shaw.Mesh.generate(NTH, NR)
-    with tempfile.TemporaryDirectory() as d:
-        mesh.write(d)
-        om = oracle_lib.OracleMesh(d)
-    om.set_material("unilayer", [(MATERIAL[0:3], MATERIAL[3:6])])
-    threads = oracle_lib.lib().orc_num_threads(0)
-    ms = 16
-    xv = np.zeros((om.nvp, ms))
-    xs = np.random.default_rng(1).standard_normal((om.nsp, ms))
-    for _ in range(args.warmup):
-        om.fom_advance(xv, xs, 1, 0.01)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        om.fom_advance(xv, xs, 1, 0.01)
-    el = time.perf_counter() - t0
-    value = (om.nvp + om.nsp) * ms * args.steps / el
-    sample = "each step: one leapfrog step of %d of the 256 forcing columns on the 1000x2000 grid" % ms
+    omp = omp_binding()
+    orc, om, gids, periods, rcv, dt = oracle_workload(np, world)
+    threads = orc.lib().orc_num_threads(0)
+    steps, el = oracle_steps(np, om, gids, periods, rcv, dt, args.warmup, steps=args.steps)
+    dofs = (om.nvp + om.nsp) * M
+    value = dofs * steps / el
+    sample = ("%d full leapfrog steps of all %d forcing columns on the 1000x2000 grid after %d warm-up steps, "
+              "forcing and 181-receiver gather every step" % (steps, M, args.warmup))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3 * (M / ms),
+            "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings": M, "sample_forcings": ms,
+            "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings": M, "dt": dt,
+                       "receivers": len(rcv), "seismogram_freq": 1,
                        "l2": "inputs larger than L2 (state 12 GB)"},
+            "same_config": True,
             "cpu_baseline": {"value": value, "unit": "DOF-updates/s", "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "cpu": host_cpu(), "omp": omp,
+                             "build": "g++ -O3 -fopenmp -ffp-contract=off (portable flags: the same objects "
+                                      "build and give the same results on x86_64 and aarch64)"},
             "e2e": {"value": value, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "host": platform.machine(), "cpu_threads": threads}
     print(json.dumps(line), flush=True)
@@ -543,6 +682,9 @@ def run_ours(args):
     barrier()
     ms = e0.elapsed_time(e1)
     launches = f.kernel_launches - launches0
+    # the timed run's result, for the comparison with the oracle after every GPU leg
+    timed_seis = f.seismogram()
+    timed_vp, timed_sp = f.get_state()
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -597,36 +739,58 @@ def run_ours(args):
         return
     hbm, peak_kind = measured_peaks()
     fp64_peak = dgemm_tflops(torch)
-    # dominant kernel: the stress half-step (nsp ~ 2 nvp).  Algorithmic bytes per launch:
-    # read + write every sp value, read every vp value once: (2*nsp + nvp) * M * 8.
-    bytes_s = (2 * mesh.nsp + mesh.nvp) * M * 8
-    bytes_v = (2 * mesh.nvp + mesh.nsp) * M * 8
-    ach = bytes_s / t_s / 1e9
+    # Algorithmic bytes: 16 B per DOF-update (one read and one write of every FP64 state
+    # value per leapfrog step).  Per launch of the two-pass schedule: nsp*M*16 for the
+    # stress half-step, nvp*M*16 for the velocity half-step; the schedule itself moves
+    # (3*nvp + 3*nsp)*M*8 = 24 B per DOF-update.
+    canon_step = (mesh.nvp + mesh.nsp) * M * 16
+    canon_s, canon_v = mesh.nsp * M * 16, mesh.nvp * M * 16
+    two_pass_step = 3 * (mesh.nvp + mesh.nsp) * M * 8
+    ms_step = ms / args.steps
+    ach_step = canon_step / (ms_step / 1e3) / 1e9
+    ach_s = canon_s / t_s / 1e9
+    fp64_flops_step = (8 * (mesh.nvp - 2 * mesh.nr) + 4 * mesh.nsp) * M
+    fp64_tflops = fp64_flops_step / (ms_step / 1e3) / 1e12
+    fp64_frac = fp64_tflops / fp64_peak
+    bound = "fp64" if fp64_frac > ach_step / hbm else "hbm"
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nth": NTH, "nr": NR, "forcings_per_gpu": M, "dt": dt,
                    "receivers": len(rcv), "seismogram_freq": 1,
                    "l2": "inputs larger than L2 (state 12.3 GB per GPU), no flush needed",
                    "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU",
                    "seismogram_columns_gathered": gathered},
-        "roofline": {"bound": "hbm", "kernel": "fom_stress_kernel", "achieved": ach, "peak": hbm,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / hbm,
+        "roofline": {"bound": bound, "kernel": "fom_stress_kernel (dominant: nsp = 2 nvp)",
+                     "achieved": ach_s, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach_s / hbm,
                      "traffic": TRAFFIC_STRESS_PER_FORCING * M,
-                     "algorithmic_bytes_per_launch": bytes_s, "launch_ms": t_s * 1e3,
-                     "velocity_kernel": {"launch_ms": t_v * 1e3, "achieved": bytes_v / t_v / 1e9,
-                                         "frac": bytes_v / t_v / 1e9 / hbm},
-                     # GB300's FP64 rate is the tighter roof: 2 FMAs per sp update, 4 per interior vp update
-                     "fp64": {"achieved_tflops": 4.0 * mesh.nsp * M / t_s / 1e12,
+                     "algorithmic_bytes_per_launch": canon_s, "launch_ms": t_s * 1e3,
+                     "bytes_per_dof_update": 16,
+                     "per_step": {"algorithmic_bytes": canon_step, "ms": ms_step, "achieved": ach_step,
+                                  "frac": ach_step / hbm},
+                     "velocity_kernel": {"launch_ms": t_v * 1e3, "algorithmic_bytes": canon_v,
+                                         "achieved": canon_v / t_v / 1e9, "frac": canon_v / t_v / 1e9 / hbm},
+                     "schedule_bytes_vs_algorithmic": two_pass_step / canon_step,
+                     # GB300's FP64 rate: 2 FMAs per sp update, 4 per interior vp update
+                     "fp64": {"achieved_tflops": fp64_tflops, "flops_per_step": fp64_flops_step,
                               "peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM 8192^3)",
-                              "frac": 4.0 * mesh.nsp * M / t_s / 1e12 / fp64_peak},
-                     "fp64_flops_per_step": (8 * (mesh.nvp - 2 * mesh.nr) + 4 * mesh.nsp) * M},
+                              "frac": fp64_frac}},
         "e2e": {"value": e2e_value, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    # the timed run against the oracle (host cores, after every GPU timing)
+    orc, om, ogids, operiods, orcv, odt = oracle_workload(np, world)
+    assert list(ogids) == list(gids) and list(orcv) == list(rcv) and odt == dt
+    ref = om.fom_run(2, total_steps, dt, gids, [2] * M, periods, [180.0] * M, rcv, 1, 0, 0)
+    line["max_rel_err_vs_oracle"] = {
+        "seismogram": _relerr(np, timed_seis, ref["seis"]), "state_vp": _relerr(np, timed_vp, ref["final_vp"]),
+        "state_sp": _relerr(np, timed_sp, ref["final_sp"]),
+        "compared": "the timed run (%d warm-up + %d timed steps from rest, all %d columns): final state and "
+                    "181-receiver seismogram" % (args.warmup, args.steps, M)}
+    del ref, timed_vp, timed_sp, om
     if world == 1 and not args.no_extra:  # the other configurations: single-GPU runs only
         line["other_configs"] = extra_workloads(np, torch, shaw)
     if world == 1 and not args.no_cpu_baseline:
@@ -640,6 +804,7 @@ def run_ours(args):
 def main():
     global M, WORKLOAD
     args = parse()
+    omp_binding()  # before any OpenMP runtime of this process starts
     if args.forcings != M:
         M = args.forcings
         WORKLOAD = "FOM rank-2 FP64, 1000 theta x 2000 r grid, M=%d forcings" % M

@@ -14,6 +14,8 @@
 //   * ROM leapfrog        src/kokkos/rom_run_rank_one.hpp:112-151,
 //                         src/kokkos/torevise/run_rom_rank_two_forcing.hpp:149-188
 //   * checkers            src/shared/checkers/check_cfl.hpp, check_dispersion_criterion.hpp
+//   * full-mesh files     meshing/helpers/full_mesh_utils.py:8-89, build_graph_impl.py:7-172,
+//                         write_files.py:10-119, create_single_mesh.py:24-60 (two variable groups)
 // The sparse products follow Kokkos-Kernels 3.5.00's CRS row kernel: per row,
 // sum = sum_k val[k]*x[ind[k]] in entry order, then y = y + alpha*sum.
 // Parity: pinned against the reference's golden vectors (tests/golden).
@@ -525,8 +527,17 @@ int orc_fom_run(const void* h, int rank, int M, uint64_t nsteps, double dt,
       ++cSp;
     }
   }
-  if (finalVp) for (int j = 0; j < M; ++j) for (uint64_t i = 0; i < m.nvp; ++i) finalVp[i + m.nvp * j] = xv[i * M + j];
-  if (finalSp) for (int j = 0; j < M; ++j) for (uint64_t i = 0; i < m.nsp; ++i) finalSp[i + m.nsp * j] = xs[i * M + j];
+  // LayoutLeft copies of the final states (rows split over the threads)
+  if (finalVp) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)m.nvp; ++i)
+      for (int j = 0; j < M; ++j) finalVp[i + m.nvp * j] = xv[i * M + j];
+  }
+  if (finalSp) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)m.nsp; ++i)
+      for (int j = 0; j < M; ++j) finalSp[i + m.nsp * j] = xs[i * M + j];
+  }
   return 0;
 }
 
@@ -539,6 +550,33 @@ int orc_fom_advance(const void* h, int M, uint64_t nsteps, double dt, double* xv
   setThreads(nthreads);
   for (uint64_t s = 0; s < nsteps; ++s) {
     crsUpdate(m.ptrVp, m.indVp, m.valVp, m.nvp, M, dt, xs, xv);
+    crsUpdate(m.ptrSp, m.indSp, m.valSp, m.nsp, M, dt, xv, xs);
+  }
+  return 0;
+}
+
+// The rank-2 leapfrog of orc_fom_run continued from a row-major state after step0
+// completed steps: forcing of every column (AddForcingRank2 order), and the receiver
+// gather of every step into seisRow (R x M, overwritten each step; may be null): the
+// whole per-step work of the FOM benchmark, for the CPU timing of the reference path.
+int orc_fom_advance_forced(const void* h, int M, uint64_t step0, uint64_t nsteps, double dt, const uint64_t* srcGid,
+                           const int32_t* kind, const double* period, const double* delay, int R,
+                           const uint64_t* rcvGid, double* seisRow, double* xv, double* xs, int nthreads) {
+  const Mesh& m = *static_cast<const Mesh*>(h);
+  if (!m.assembled) { g_err = "material not set"; return 1; }
+  setThreads(nthreads);
+  std::vector<double> f(M, 0.0);
+  for (uint64_t s = 0; s < nsteps; ++s) {
+    const double t = (double)(step0 + s) * dt;
+    for (int j = 0; j < M; ++j) f[j] = signal(kind[j], delay[j], period[j], t);
+    crsUpdate(m.ptrVp, m.indVp, m.valVp, m.nvp, M, dt, xs, xv);
+    for (int j = 0; j < M; ++j) {
+      const uint64_t g = srcGid[j];
+      xv[g * M + j] += m.rhoInvVp[g] * f[j] * dt;
+    }
+    if (seisRow)
+      for (int r = 0; r < R; ++r)
+        for (int j = 0; j < M; ++j) seisRow[r + (uint64_t)R * j] = xv[rcvGid[r] * M + j];
     crsUpdate(m.ptrSp, m.indSp, m.valSp, m.nsp, M, dt, xv, xs);
   }
   return 0;
@@ -654,6 +692,62 @@ void orc_rom_seismogram(const double* phiVp, uint64_t nvp, uint64_t kv, int R, c
       for (uint64_t i = 0; i < kv; ++i) sum += phiVp[rcvGid[r] + nvp * i] * X[i + kv * t];
       S[r + (uint64_t)R * t] = sum;
     }
+}
+
+// ---- the reference mesher's full mesh with two variable groups, written as files ----
+// Cells are visited j-major (r), i-minor (theta); each cell holds its vp point, an srp
+// point above it (j < nr-1) and an stp point to its right (i < nth-1), numbered in that
+// order (meshing/helpers/full_mesh_utils.py:8-89, unit_cell.py:58-66).  Graphs and the
+// boundary factors of the vp stencil follow build_graph_impl.py:58-127; the files use the
+// mesher's formats (write_files.py: "%.20f" floats, "%.1f" factors, a trailing space).
+int orc_write_full_mesh(uint64_t nth, uint64_t nr, double thLDeg, double thRDeg, double rCmb, double rSurf,
+                        const char* dir) {
+  if (nth < 2 || nr < 2 || !dir) { g_err = "bad mesh arguments"; return 1; }
+  const double pi = 3.14159265358979311600;  // numpy.pi
+  const double thL = thLDeg * pi / 180., thR = thRDeg * pi / 180.;
+  const double dth = (thR - thL) / (double)(nth - 1), dr = (rSurf - rCmb) / (double)(nr - 1);
+  const uint64_t nvp = nth * nr, nsp = (nr - 1) * nth + nr * (nth - 1), row = 2 * nth - 1;
+  auto srp = [&](uint64_t j, uint64_t i) { return j * row + 2 * i; };
+  auto stp = [&](uint64_t j, uint64_t i) { return (j + 1 < nr) ? j * row + 2 * i + 1 : j * row + i; };
+  const std::string d(dir);
+  FILE* fi = std::fopen((d + "/mesh_info.dat").c_str(), "w");
+  FILE* fv = std::fopen((d + "/graph_vp.dat").c_str(), "w");
+  FILE* fc = std::fopen((d + "/coeff_vp.dat").c_str(), "w");
+  FILE* fs = std::fopen((d + "/graph_sp.dat").c_str(), "w");
+  if (!fi || !fv || !fc || !fs) {
+    for (FILE* f : {fi, fv, fc, fs}) if (f) std::fclose(f);
+    g_err = "cannot write mesh files in " + d;
+    return 1;
+  }
+  std::fprintf(fi, "thL   %.20f\nthR   %.20f\nrCmb  %.20f\nrSurf %.20f\ndth   %.20f\ndr    %.20f\n", thLDeg, thRDeg,
+               rCmb, rSurf, dth, dr);
+  std::fprintf(fi, "numPtsVp %llu\nnumPtsSp %llu\nnth %llu\nnr %llu\n", (unsigned long long)nvp,
+               (unsigned long long)nsp, (unsigned long long)nth, (unsigned long long)nr);
+  // sp points are written in gid order, which is the cell order: srp then stp per cell
+  for (uint64_t j = 0; j < nr; ++j) {
+    for (uint64_t i = 0; i < nth; ++i) {
+      const uint64_t p = j * nth + i;
+      const double th = thL + (double)i * dth, r = rCmb + (double)j * dr;
+      const int onSym = (i == 0 || i == nth - 1) ? 1 : 0;
+      const uint64_t W = i >= 1 ? stp(j, i - 1) : stp(j, i), E = i + 1 < nth ? stp(j, i) : stp(j, i - 1);
+      const uint64_t N = j + 1 < nr ? srp(j, i) : srp(j - 1, i), S = j >= 1 ? srp(j - 1, i) : srp(j, i);
+      double c[4] = {i >= 1 ? 1. : 0., j + 1 < nr ? 1. : -1., i + 1 < nth ? 1. : 0., j >= 1 ? 1. : -1.};
+      if (onSym) c[0] = c[1] = c[2] = c[3] = 0.;
+      std::fprintf(fv, "%llu %d %.20f %.20f %llu %llu %llu %llu \n", (unsigned long long)p, onSym, th, r,
+                   (unsigned long long)W, (unsigned long long)N, (unsigned long long)E, (unsigned long long)S);
+      std::fprintf(fc, "%llu %.1f %.1f %.1f %.1f \n", (unsigned long long)p, c[0], c[1], c[2], c[3]);
+      if (j + 1 < nr)
+        std::fprintf(fs, "%llu 1 %d %.20f %.20f %llu %llu \n", (unsigned long long)srp(j, i), onSym, th, r + dr * 0.5,
+                     (unsigned long long)((j + 1) * nth + i), (unsigned long long)p);
+      if (i + 1 < nth)
+        std::fprintf(fs, "%llu 2 0 %.20f %.20f %llu %llu \n", (unsigned long long)stp(j, i), th + dth * 0.5, r,
+                     (unsigned long long)p, (unsigned long long)(p + 1));
+    }
+  }
+  int bad = 0;
+  for (FILE* f : {fi, fv, fc, fs}) bad |= std::fclose(f) != 0;
+  if (bad) { g_err = "error writing mesh files in " + d; return 1; }
+  return 0;
 }
 
 }  // extern "C"

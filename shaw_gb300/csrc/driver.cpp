@@ -2,6 +2,7 @@
 // semantics), the FOM/ROM problem drivers (src/kokkos/fom_problem_rank_{one,two}.hpp,
 // src/kokkos/rom_problem_rank_one.hpp) and the output writers
 // (src/shared/io/matrix_write.hpp).  All stepping goes through the C ABI.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -279,10 +280,42 @@ struct FomGuard {
   ~FomGuard() { shaw_fom_destroy(h); }
 };
 
-void print_perf(uint64_t nsteps, double seconds, double dofUpdates) {
-  std::printf("\nloopTime = %.10f\n", seconds);
-  std::printf("aveTime(ms) = %7.4f \n", seconds / (double)nsteps * 1000.0);
-  std::printf("dofUpdatesPerSec = %.6e \n", dofUpdates / seconds);
+// The reference's cost model of one leapfrog step (fom_complexities.hpp:57-137 with the
+// Spmv / Spmm / Mult formulas of src/shared/complexities/: FP64 values, size_t ordinals)
+// and its log lines (print_perf.hpp:57-84), which the reference's scaling scripts parse.
+// nnz(Jvp) = 4 nvp - 2 nth - 2 nr (merged CMB/surface and axis entries), nnz(Jsp) = 2 nsp.
+void print_perf(int rank, uint64_t M, const shaw_mesh_s& mesh, uint64_t nsteps, const double perf[3]) {
+  const double sc = sizeof(double), ord = sizeof(uint64_t), MB = 1024.0 * 1024.0;
+  const double nvp = (double)mesh.nvp, nsp = (double)mesh.nsp;
+  const double nnzVp = 4.0 * nvp - 2.0 * (double)mesh.nth - 2.0 * (double)mesh.nr, nnzSp = 2.0 * nsp;
+  const double k = (double)M;
+  auto sparse = [&](double nnz, double rows, double& mem, double& fl) {  // spmv (k == 1) / spmm
+    mem = (nnz * (sc + ord) + rows * ord + nnz * k * sc + 2.0 * rows * k * sc) / MB;
+    fl = 2.0 * nnz * k + rows * k;
+  };
+  double m0, f0, m2, f2, m1, f1;
+  sparse(nnzVp, nvp, m0, f0);
+  sparse(nnzSp, nsp, m2, f2);
+  if (rank == 1) { m1 = 4.0 * nvp * sc / MB; f1 = 3.0 * nvp; }  // mult with beta = 1
+  else { m1 = 4.0 * k * sc / MB; f1 = 3.0 * k; }                // the rank-2 forcing loop
+  const double memMB = m0 + m1 + m2, flops = f0 + f1 + f2;
+  const double minT = perf[0], maxT = perf[1], tot = perf[2], ave = tot / (double)nsteps;
+  const double GB = memMB / 1024.;
+  std::cout << "flops = " << flops << std::endl;
+  std::cout << "memMB = " << memMB << std::endl;
+  std::cout << "flops/bytes = " << flops / (memMB * MB) << std::endl;
+  std::printf("aveBandwidth(GB/s) = %8.2lf \n", GB / ave);
+  std::printf("minBandwidth(GB/s) = %8.2lf \n", GB / maxT);
+  std::printf("maxBandwidth(GB/s) = %8.2lf \n", GB / minT);
+  std::printf("aveGFlop = %7.4lf \n", flops / ave / 1e9);
+  std::printf("minGFlop = %7.4lf \n", flops / maxT / 1e9);
+  std::printf("maxGFlop = %7.4lf \n", flops / minT / 1e9);
+  std::printf("totTime(se) = %7.4lf \n", tot);
+  std::printf("aveTime(ms) = %7.4lf \n", ave * 1000);
+  std::printf("maxTime(ms) = %7.4lf \n", maxT * 1000);
+  std::printf("minTime(ms) = %7.4lf \n", minT * 1000);
+  std::printf("dofUpdatesPerSec = %.6e \n", (nvp + nsp) * k / ave);
+  std::fflush(stdout);
 }
 
 }  // namespace
@@ -315,12 +348,26 @@ int run_fom_set(const Input& in, const shaw_mesh_s& mesh, int rank, const std::v
     if ((rc = shaw_fom_set_snapshots(g.h, in.snapFreqVp, in.snapFreqSp, in.nsteps, snapVp.data(), snapSp.data())))
       return rc;
   }
+  // runFom: the steps run in chunks (multiples of the 64-step CUDA-graph chunk, at most
+  // about 64 chunks), each timed on the host after its work completes; the per-step
+  // min / max / total of the reference's log come from the chunks' per-step averages.
+  if ((rc = shaw_fom_reset(g.h))) return rc;
+  const uint64_t chunk = std::max<uint64_t>(64, (in.nsteps / 64 + 63) / 64 * 64);
+  double perf[3] = {1e32, 0.0, 0.0};
   const auto t0 = std::chrono::steady_clock::now();
-  rc = shaw_fom_run(g.h, in.dt, in.nsteps);
-  const auto t1 = std::chrono::steady_clock::now();
-  if (rc) return rc;
-  print_perf(in.nsteps, std::chrono::duration<double>(t1 - t0).count(),
-             (double)(mesh.nvp + mesh.nsp) * M * (double)in.nsteps);
+  for (uint64_t done = 0; done < in.nsteps;) {
+    const uint64_t c = std::min(chunk, in.nsteps - done);
+    const auto c0 = std::chrono::steady_clock::now();
+    if ((rc = shaw_fom_advance(g.h, in.dt, c))) return rc;
+    if ((rc = shaw_fom_synchronize(g.h))) return rc;
+    const double per = std::chrono::duration<double>(std::chrono::steady_clock::now() - c0).count() / (double)c;
+    perf[0] = std::min(perf[0], per);
+    perf[1] = std::max(perf[1], per);
+    perf[2] += per * (double)c;
+    done += c;
+  }
+  const double loop = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::printf("\nloopTime = %.10f", loop);
   // release the page-locked snapshot registration before writing
   if (in.snapEnabled && (rc = shaw_fom_set_snapshots(g.h, 0, 0, 0, nullptr, nullptr))) return rc;
   const std::string id = "_" + std::to_string(runId);
@@ -332,10 +379,19 @@ int run_fom_set(const Input& in, const shaw_mesh_s& mesh, int rank, const std::v
                              in.snapBinary, true)))
       return rc;
   }
+  // dataCollectionTime: the observers' host work outside the device loop (the sampled
+  // snapshot columns arrive during the loop; the seismogram is read back once here)
+  const auto d0 = std::chrono::steady_clock::now();
+  std::vector<double> seis;
+  if (in.seisEnabled) {
+    seis.resize(rcvGids.size() * (in.nsteps / in.seisFreq) * M);
+    if ((rc = shaw_fom_get_seismogram(g.h, seis.data()))) return rc;
+  }
+  std::printf("\ndataCollectionTime = %.10f\n",
+              std::chrono::duration<double>(std::chrono::steady_clock::now() - d0).count());
+  print_perf(rank, M, mesh, in.nsteps, perf);
   if (in.seisEnabled) {
     const uint64_t T = in.nsteps / in.seisFreq;
-    std::vector<double> seis(rcvGids.size() * T * M);
-    if ((rc = shaw_fom_get_seismogram(g.h, seis.data()))) return rc;
     if ((rc = write_observed(in.seisFile + id, seis.data(), rcvGids.size(), T, M, in.seisBinary, false))) return rc;
   }
   return SHAW_OK;
@@ -402,8 +458,18 @@ int run_input_file(const std::string& path) {
   Input in;
   int rc = parse_input(path, in);
   if (rc) return rc;
+  // ParserGeneralSection::print (parser_general_section.hpp:127-134)
+  std::cout << "\nmeshDir = " << in.meshDir << " \n"
+            << "checkDispersion = " << std::boolalpha << in.checkDispersion << " \n"
+            << "timeStep = " << in.dt << " \n"
+            << "finalT = " << in.finalTime << " \n"
+            << "numSteps = " << in.nsteps << " \n"
+            << "exploitForcingSparsity " << true << " \n" << std::noboolalpha;
   shaw_mesh_s mesh;
   if ((rc = host::load_mesh(in.meshDir, mesh))) return rc;
+  // MeshInfo's log lines (mesh_info.hpp:196-212)
+  std::cout << "numGptVp = " << mesh.nvp << "\nnumGptSp = " << mesh.nsp << "\nnth = " << mesh.nth
+            << "\nnr = " << mesh.nr << std::endl;
   if (in.matKind == kMaterialCustom)
     return fail(SHAW_ERR_UNSUPPORTED,
                 "custom material: supply per-point arrays through shaw_mesh_set_material_arrays");

@@ -930,14 +930,17 @@ namespace {
 template <typename T>
 int copy_state_t(shaw_fom_t h, double* host, const double* chost, uint64_t N, void* dev, bool to_host) {
   std::vector<T> tmp(N * h->M);
+  const uint32_t M = h->M;
   if (to_host) {
     SHAW_CUDA(cudaMemcpyAsync(tmp.data(), dev, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost, h->stream));
     SHAW_CUDA(cudaStreamSynchronize(h->stream));
-    for (uint64_t n = 0; n < N; ++n)
-      for (uint32_t m = 0; m < h->M; ++m) host[n + N * m] = (double)tmp[n * h->M + m];
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < (int64_t)N; ++n)
+      for (uint32_t m = 0; m < M; ++m) host[n + N * m] = (double)tmp[n * M + m];
   } else {
-    for (uint64_t n = 0; n < N; ++n)
-      for (uint32_t m = 0; m < h->M; ++m) tmp[n * h->M + m] = (T)chost[n + N * m];
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < (int64_t)N; ++n)
+      for (uint32_t m = 0; m < M; ++m) tmp[n * M + m] = (T)chost[n + N * m];
     SHAW_CUDA(cudaMemcpyAsync(dev, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, h->stream));
     SHAW_CUDA(cudaStreamSynchronize(h->stream));
   }

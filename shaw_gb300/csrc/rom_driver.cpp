@@ -3,6 +3,7 @@
 // src/shared/io/read_basis.hpp), GPU projection of the reduced operators, the
 // forcing vector phiVpRhoInv, the checkers, the ROM leapfrog and the reduced
 // snapshots written like the reference's StateObserver.
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -110,7 +111,11 @@ int run_rom(const Input& in, const shaw_mesh_s& mesh) {
     host::operator_desc(mesh, d);
     FomGuard f;
     if ((rc = shaw_fom_create(&d, 1, 1, SHAW_FP64, &f.h))) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
     if ((rc = shaw_rom_project(f.h, phiVp.data(), kv, phiSp.data(), ks, Av.data(), As.data()))) return rc;
+    // the log line of computeRomOperatorsUsingFomJacsWithMatProp (rom_compute_jacobians.hpp:107-108)
+    std::printf("romJac time: %.10f\n",
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
   }
   // RankOneForcing source mapping and phiVpRhoInv (rom_problem_rank_one.hpp:133-147)
   uint64_t src = 0;

@@ -78,6 +78,11 @@ def lib():
                                   ctypes.c_uint64, ctypes.c_uint64, _dp, _dp, _dp, _dp, ctypes.c_int]
         L.orc_rom_seismogram.argtypes = [_dp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, _u64p,
                                          _dp, ctypes.c_uint64, _dp]
+        L.orc_fom_advance_forced.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                             ctypes.c_double, _u64p, _i32p, _dp, _dp, ctypes.c_int, _u64p, _dp,
+                                             _dp, _dp, ctypes.c_int]
+        L.orc_write_full_mesh.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_char_p]
         _lib = L
     return _lib
 
@@ -95,6 +100,12 @@ def material_params(kind, layers):
         p[7:7 + len(rho)] = rho
         p[10:10 + len(vs)] = vs
     return p
+
+
+def write_full_mesh(nth, nr, directory, th_left=0.0, th_right=180.0, r_cmb=3480.0, r_surf=6371.0):
+    """The reference mesher's full mesh (two variable groups) written into `directory`."""
+    if lib().orc_write_full_mesh(nth, nr, th_left, th_right, r_cmb, r_surf, directory.encode()) != 0:
+        raise RuntimeError(lib().orc_error().decode())
 
 
 class OracleMesh:
@@ -196,6 +207,26 @@ class OracleMesh:
         r = lib().orc_fom_advance(self.h, M, nsteps, dt, _ptr(xv, _dp), _ptr(xs, _dp), nthreads)
         if r != 0:
             raise RuntimeError(lib().orc_error().decode())
+
+    def fom_advance_forced(self, xv, xs, step0, nsteps, dt, src_gids, kinds, periods, delays, rcv_gids=None,
+                           nthreads=0):
+        """The rank-2 leapfrog continued in place from step0 completed steps (row-major
+        states nvp x M, nsp x M) with the forcing of every column and, when rcv_gids is
+        given, the receiver gather of every step.  Returns the last step's receiver row."""
+        M = xv.shape[1]
+        src = np.ascontiguousarray(src_gids, np.uint64)
+        kinds = np.ascontiguousarray(kinds, np.int32)
+        periods = np.ascontiguousarray(np.broadcast_to(periods, (M,)), np.float64)
+        delays = np.ascontiguousarray(np.broadcast_to(delays, (M,)), np.float64)
+        rcv = None if rcv_gids is None else np.ascontiguousarray(rcv_gids, np.uint64)
+        R = 0 if rcv is None else len(rcv)
+        row = np.zeros((R, M), order="F") if R else None
+        r = lib().orc_fom_advance_forced(self.h, M, step0, nsteps, dt, _ptr(src, _u64p), _ptr(kinds, _i32p),
+                                         _ptr(periods, _dp), _ptr(delays, _dp), R, _ptr(rcv, _u64p),
+                                         _ptr(row, _dp), _ptr(xv, _dp), _ptr(xs, _dp), nthreads)
+        if r != 0:
+            raise RuntimeError(lib().orc_error().decode())
+        return row
 
     def rom_operators(self, phi_vp, phi_sp, nthreads=0):
         phi_vp = np.asfortranarray(phi_vp, dtype=np.float64)

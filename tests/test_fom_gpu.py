@@ -117,6 +117,15 @@ def test_input_file_driver_matches_reference_golds(shaw, oracle, case, tmp_path)
                 tol = 1e-10 if name == "snaps_sp" else 1e-13
                 assert np.allclose(mine, golds[key], atol=tol, rtol=0)
     assert (tmp_path / "coords_vp.txt").exists() and (tmp_path / "coords_sp.txt").exists()
+    # the reference's log lines, in the forms its scaling scripts parse
+    # (python_scripts_revise/log_file_extractor.py:9-114)
+    import re
+    for key in ("aveBandwidth", "minBandwidth", "maxBandwidth"):
+        assert float(re.search(key + r"(\D+)\d+.\d+", r.stdout).group().split()[2]) > 0, key
+    for key in ("aveGFlop", "aveTime", "flops/bytes", "loopTime", "dataCollectionTime"):
+        assert re.search(re.escape(key) + r"(\D+)\d+.\d+", r.stdout), key
+    assert int(re.search(r"numGptVp = \d+", r.stdout).group().split()[2]) == m.nvp
+    assert int(re.search(r"numSteps(\D+)\d+", r.stdout).group().split()[2]) == c["nsteps"]
 
 
 @pytest.mark.parametrize("grid", ["small", "large"])

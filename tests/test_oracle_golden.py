@@ -160,3 +160,17 @@ def test_every_reference_gold_file(oracle):
                 assert np.max(np.abs(mine - gold)) <= 1e-12 * np.abs(gold).max(), f
                 n += 1
     assert n >= 60
+
+
+def test_oracle_mesher_writes_reference_mesh_files_byte_for_byte(oracle):
+    """The oracle's own restatement of the mesher (used where the product library must not
+    be loaded, e.g. the benchmark's reference arm) against the reference mesher's files."""
+    import hashlib
+    import tempfile
+    digests = json.load(open(os.path.join(GOLDEN, "mesh_sha256.json")))
+    for name, info in digests.items():
+        with tempfile.TemporaryDirectory() as d:
+            oracle.write_full_mesh(info["nth"], info["nr"], d, info["thL"], info["thR"], info["rCmb"], info["rSurf"])
+            for f in ("mesh_info.dat", "graph_vp.dat", "graph_sp.dat", "coeff_vp.dat"):
+                h = hashlib.sha256(open(os.path.join(d, f), "rb").read()).hexdigest()
+                assert h == info[f], (name, f)
