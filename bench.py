@@ -52,6 +52,8 @@ def parse():
                         "for --steps steps, for profiler captures")
     p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32"],
                    help="only run the FOM on the 1000x2000 grid with --forcings columns for --steps steps")
+    p.add_argument("--schedule", default="auto", choices=["auto", "two-pass", "sweep-fp64-fma"],
+                   help="FOM schedule of --profile-fom")
     return p.parse_args()
 
 
@@ -131,6 +133,9 @@ class ClockSampler:
 # DRAM bytes (read + write) of one fom_stress_kernel launch per forcing column, from the
 # ncu capture summarised in profiles/fom_kernels_rank2_1000x2000.md (M = 16, scaled by M).
 TRAFFIC_STRESS_PER_FORCING = (831.617024e6 + 461.196032e6) / 16
+# DRAM bytes (read + write) of one fom_sweep_kernel launch per forcing column (FP64 state), from
+# the ncu capture summarised in profiles/ (M = 32, scaled by M); None until that capture exists.
+TRAFFIC_SWEEP_PER_FORCING = None
 
 
 def dgemm_tflops(torch):
@@ -256,7 +261,11 @@ def _timed(torch, stream_ptr, fn):
 
 
 def _relerr(np, a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    """max |a - b| / max |b|; the absolute difference where b is all zero (e.g. surface
+    receivers that the wave has not reached yet)."""
+    scale = float(np.max(np.abs(b)))
+    diff = float(np.max(np.abs(a - b)))
+    return diff / scale if scale > 0 else diff
 
 
 def stable_rom(np, k, seed, smin, smax):
@@ -691,20 +700,30 @@ def run_ours(args):
         ms = float(t.item())
     value = world * dofs * args.steps / (ms / 1e3)
 
-    # ---- per-kernel durations (CUDA events on the launching stream) -----------------
-    kv, ks = [], []
-    for _ in range(6):
-        a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        a.record(stream)
-        f.update_velocity(dt, total_steps)
-        b.record(stream)
-        f.update_stress(dt)
-        c.record(stream)
-        c.synchronize()
-        kv.append(a.elapsed_time(b))
-        ks.append(b.elapsed_time(c))
-    kv, ks = sorted(kv)[1:-1], sorted(ks)[1:-1]
-    t_v, t_s = sum(kv) / len(kv) / 1e3, sum(ks) / len(ks) / 1e3
+    # ---- single launches of each schedule (CUDA events on the launching stream) ---------
+    def timed_ms(fn, reps=6):
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        ts = sorted(ts)[1:-1]
+        return sum(ts) / len(ts) / 1e3
+
+    sweep = M % 32 == 0
+    f.set_receivers([], 0, 0)
+    sched = {}
+    if sweep:
+        sched["sweep"] = timed_ms(lambda: f.advance(dt, 1))            # one fom_sweep_kernel launch
+        f.set_schedule(shaw.SCHEDULE_SWEEP_FP64_FMA)
+        sched["sweep_fp64_fma"] = timed_ms(lambda: f.advance(dt, 1))
+    f.set_schedule(shaw.SCHEDULE_TWO_PASS)
+    t_v = timed_ms(lambda: f.update_velocity(dt, total_steps))
+    t_s = timed_ms(lambda: f.update_stress(dt))
+    sched["two_pass_velocity"], sched["two_pass_stress"] = t_v, t_s
     f.close()
 
     # ---- end to end through the C ABI from host buffers -------------------------------
@@ -744,15 +763,24 @@ def run_ours(args):
     # stress half-step, nvp*M*16 for the velocity half-step; the schedule itself moves
     # (3*nvp + 3*nsp)*M*8 = 24 B per DOF-update.
     canon_step = (mesh.nvp + mesh.nsp) * M * 16
-    canon_s, canon_v = mesh.nsp * M * 16, mesh.nvp * M * 16
+    canon_s = mesh.nsp * M * 16
     two_pass_step = 3 * (mesh.nvp + mesh.nsp) * M * 8
     ms_step = ms / args.steps
     ach_step = canon_step / (ms_step / 1e3) / 1e9
-    ach_s = canon_s / t_s / 1e9
-    fp64_flops_step = (8 * (mesh.nvp - 2 * mesh.nr) + 4 * mesh.nsp) * M
-    fp64_tflops = fp64_flops_step / (ms_step / 1e3) / 1e12
-    fp64_frac = fp64_tflops / fp64_peak
-    bound = "fp64" if fp64_frac > ach_step / hbm else "hbm"
+    dofs_step = (mesh.nvp + mesh.nsp) * M
+    if sweep:
+        # one launch per step: the dominant (only) kernel; FP64 instructions: 2 adds per DOF-update
+        kern, launch_s, canon_launch = "fom_sweep_kernel (FP64 state, double-float products)", sched["sweep"], canon_step
+        fp64_instr = 2 * dofs_step
+        sched_bytes = canon_step
+    else:
+        kern, launch_s, canon_launch = "fom_stress_kernel (dominant: nsp = 2 nvp)", t_s, canon_s
+        fp64_instr = (4 * (mesh.nvp - 2 * mesh.nr) + 2 * mesh.nsp) * M
+        sched_bytes = two_pass_step
+    ach = canon_launch / launch_s / 1e9
+    # FP64 pipe: instructions per second against the DGEMM's FMA rate (peak flop/s / 2)
+    fp64_pipe_frac = fp64_instr / (ms_step / 1e3) / (fp64_peak * 1e12 / 2)
+    bound = "fp64" if fp64_pipe_frac > ach_step / hbm else "hbm"
     line = {
         "metric": METRIC, "value": value, "unit": "DOF-updates/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -762,20 +790,18 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (state 12.3 GB per GPU), no flush needed",
                    "parallelism": "forcing columns sharded across GPUs" if world > 1 else "single GPU",
                    "seismogram_columns_gathered": gathered},
-        "roofline": {"bound": bound, "kernel": "fom_stress_kernel (dominant: nsp = 2 nvp)",
-                     "achieved": ach_s, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": ach_s / hbm,
-                     "traffic": TRAFFIC_STRESS_PER_FORCING * M,
-                     "algorithmic_bytes_per_launch": canon_s, "launch_ms": t_s * 1e3,
+        "roofline": {"bound": bound, "kernel": kern, "achieved": ach, "peak": hbm, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": ach / hbm,
+                     "traffic": ((TRAFFIC_SWEEP_PER_FORCING * M if TRAFFIC_SWEEP_PER_FORCING else None)
+                                 if sweep else TRAFFIC_STRESS_PER_FORCING * M),
+                     "algorithmic_bytes_per_launch": canon_launch, "launch_ms": launch_s * 1e3,
                      "bytes_per_dof_update": 16,
                      "per_step": {"algorithmic_bytes": canon_step, "ms": ms_step, "achieved": ach_step,
                                   "frac": ach_step / hbm},
-                     "velocity_kernel": {"launch_ms": t_v * 1e3, "algorithmic_bytes": canon_v,
-                                         "achieved": canon_v / t_v / 1e9, "frac": canon_v / t_v / 1e9 / hbm},
-                     "schedule_bytes_vs_algorithmic": two_pass_step / canon_step,
-                     # GB300's FP64 rate: 2 FMAs per sp update, 4 per interior vp update
-                     "fp64": {"achieved_tflops": fp64_tflops, "flops_per_step": fp64_flops_step,
-                              "peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM 8192^3)",
-                              "frac": fp64_frac}},
+                     "schedule_bytes_vs_algorithmic": sched_bytes / canon_step,
+                     "fp64_pipe": {"instructions_per_step": fp64_instr, "frac": fp64_pipe_frac,
+                                   "peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM 8192^3)"},
+                     "schedules_ms_per_launch": {k: v * 1e3 for k, v in sched.items()}},
         "e2e": {"value": e2e_value, "unit": "DOF-updates/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps, "seconds": e2e_s},
         "gpu_launches": launches,
@@ -838,6 +864,8 @@ def main():
         gids, periods, rcv, dt = workload_inputs(np, mesh)
         m = args.forcings
         f = shaw.Fom(mesh, 2, m, precision=shaw.FP64 if args.profile_fom == "fp64" else shaw.MIXED_FP32)
+        f.set_schedule({"auto": shaw.SCHEDULE_AUTO, "two-pass": shaw.SCHEDULE_TWO_PASS,
+                        "sweep-fp64-fma": shaw.SCHEDULE_SWEEP_FP64_FMA}[args.schedule])
         f.set_sources(gids[:m], "gaussDer", periods[:m], 180.0)
         f.reset()
         f.advance(dt, args.steps)

@@ -41,6 +41,7 @@ SIGNAL = {"ricker": 0, "sinusoid": 1, "gaussDer": 2}
 MATERIAL = {"unilayer": 0, "bilayer": 1, "prem": 2}
 # MIXED_TF32X3 is experimental: it does not meet the 1e-6 mixed-precision bar (see the C header).
 FP64, MIXED_TF32X3, MIXED_FP32, MIXED_OZAKI_BF16, OZAKI_FP64 = 0, 1, 3, 4, 5
+SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP_FP64_FMA = 0, 1, 2
 
 
 class ShawError(RuntimeError):
@@ -89,6 +90,7 @@ SIGNATURES = [
     ("shaw_fom_get_state", ctypes.c_int, [_vp, _dp, _dp]),
     ("shaw_fom_set_state", ctypes.c_int, [_vp, _dp, _dp]),
     ("shaw_fom_stream", _vp, [_vp]),
+    ("shaw_fom_set_schedule", ctypes.c_int, [_vp, ctypes.c_int]),
     ("shaw_fom_kernel_launches", ctypes.c_uint64, [_vp]),
     ("shaw_rom_project", ctypes.c_int, [_vp, _dp, ctypes.c_uint64, _dp, ctypes.c_uint64, _dp, _dp]),
     ("shaw_rom_project_noalloc", ctypes.c_int, [_vp, _vp, ctypes.c_uint64, _vp, ctypes.c_uint64, _vp, _vp, _vp]),
@@ -347,6 +349,10 @@ class Fom:
         vp = np.asfortranarray(vp, np.float64).reshape((self.nvp, self.M), order="F")
         sp = np.asfortranarray(sp, np.float64).reshape((self.nsp, self.M), order="F")
         _check(lib().shaw_fom_set_state(self.h, _p(vp, _dp), _p(sp, _dp)))
+
+    def set_schedule(self, schedule):
+        """SCHEDULE_AUTO, SCHEDULE_TWO_PASS or SCHEDULE_SWEEP_FP64_FMA (see shaw_fom_set_schedule)."""
+        _check(lib().shaw_fom_set_schedule(self.h, schedule))
 
     @property
     def stream(self):

@@ -28,6 +28,7 @@
 #include <string>
 #include <vector>
 
+#include "fom_sweep.h"
 #include "shaw_internal.h"
 
 namespace shaw {
@@ -58,11 +59,8 @@ namespace {
 constexpr int kThreads = 256;
 constexpr uint32_t kGraphChunk = 64;  // leapfrog steps per captured CUDA graph
 
-struct FomCtl {
-  unsigned long long step_base;  // steps completed before the current chunk
-  unsigned int nonfinite;        // set when a gathered receiver value is NaN/Inf
-  unsigned int pad;
-};
+using shaw::FomCtl;
+namespace sweep = shaw::sweep;
 
 // Arguments shared by both half-step kernels (passed by value, < 4 KB).  The state
 // and the folded stencil values are FP64 (SHAW_FP64) or FP32 (SHAW_MIXED_FP32).
@@ -346,6 +344,23 @@ __global__ void fom_fold_kernel(const double* raw, T* folded, double dt, size_t 
     folded[k] = (T)(dt * raw[k]);
 }
 
+// Point-major copies of the folded stencil values for the single sweep:
+// out[(shift + p) * planes + c] = dt * raw[c * n + p] in the sweep's format (FP64, FP32, or an
+// FP32 pair (hi, lo) with hi + lo within 2^-48 of the FP64 value).
+__device__ __forceinline__ void fold_to(double c, double& o) { o = c; }
+__device__ __forceinline__ void fold_to(double c, float& o) { o = (float)c; }
+__device__ __forceinline__ void fold_to(double c, float2& o) {
+  const float hi = __double2float_rn(c);
+  o = make_float2(hi, __double2float_rn(c - (double)hi));
+}
+template <typename T>
+__global__ void fom_fold_aos_kernel(const double* raw, T* out, double dt, size_t n, uint32_t planes, size_t shift) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n * planes; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = k / planes, c = k - p * planes;
+    fold_to(dt * raw[c * n + p], out[(shift + p) * planes + c]);
+  }
+}
+
 __global__ void fom_advance_base_kernel(FomCtl* ctl, unsigned int by) { ctl->step_base += by; }
 __global__ void fom_set_base_kernel(FomCtl* ctl, unsigned long long v) { ctl->step_base = v; }
 
@@ -404,6 +419,20 @@ struct shaw_fom_s {
   // graph cache
   cudaGraphExec_t graph = nullptr;
   double graph_dt = std::nan("");
+  // single-sweep path (M a multiple of 32): the state alternates between two buffers each
+  // step; xv / xs above always point at the current one, xvb[cur] / xsb[cur]
+  bool sweep = false;                // the sweep is in use
+  bool sweep_ok = false;             // its buffers exist (M a multiple of 32)
+  sweep::Form form = sweep::kF64;
+  void* xvb[2] = {nullptr, nullptr};
+  void* xsb[2] = {nullptr, nullptr};
+  int cur = 0;
+  CUtensorMap tv[2], ts[2];          // tensor maps over the buffers (v box: strip + 1, sp box)
+  void* cv4 = nullptr;               // point-major folded stencil values of the sweep (8 bytes per value
+  void* cs2 = nullptr;               // for FP64 handles: FP64 or an FP32 pair; 4 for FP32 handles)
+  int sms = 0;
+  cudaGraphExec_t sweep_graph[2] = {nullptr, nullptr};  // 64 steps starting from buffer 0 / 1
+  double sweep_graph_dt[2] = {std::nan(""), std::nan("")};
 };
 
 namespace {
@@ -503,9 +532,112 @@ int ensure_folded(H* h, double dt) {
     fom_fold_kernel<double><<<1024, 256, 0, h->stream>>>(h->csp_raw, (double*)h->csp, dt, 2 * h->nsp);
   }
   h->launches += 2;
+  if (h->sweep) {
+    if (h->form == sweep::kF64Emu) {
+      fom_fold_aos_kernel<float2><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (float2*)h->cv4, dt, h->nvp, 4, 0);
+      fom_fold_aos_kernel<float2><<<1024, 256, 0, h->stream>>>(h->csp_raw, (float2*)h->cs2, dt, h->nsp, 2, 1);
+    } else if (h->form == sweep::kF64) {
+      fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (double*)h->cv4, dt, h->nvp, 4, 0);
+      fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->csp_raw, (double*)h->cs2, dt, h->nsp, 2, 1);
+    } else {
+      fom_fold_aos_kernel<float><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (float*)h->cv4, dt, h->nvp, 4, 0);
+      fom_fold_aos_kernel<float><<<1024, 256, 0, h->stream>>>(h->csp_raw, (float*)h->cs2, dt, h->nsp, 2, 1);
+    }
+    h->launches += 2;
+  }
   SHAW_CUDA(cudaGetLastError());
   h->folded_dt = dt;
   return SHAW_OK;
+}
+
+// ---- the single-sweep path --------------------------------------------------------------
+
+sweep::Params sweep_params(const H* h, double dt, int from) {
+  sweep::Params p;
+  std::memset(&p, 0, sizeof(p));
+  p.xv_new = h->xvb[from ^ 1];
+  p.xs_new = h->xsb[from ^ 1];
+  p.xv_old = h->xvb[from];
+  p.cvp = h->cv4;
+  p.csp = h->cs2;
+  p.rho_inv = h->rho_inv;
+  p.src = h->src;
+  p.kind = h->kind;
+  p.period = h->period;
+  p.delay = h->delay;
+  p.rcv = h->rcv;
+  p.seis = h->seis;
+  p.ctl = h->ctl;
+  p.dt = dt;
+  p.nth = (uint32_t)h->nth;
+  p.nr = (uint32_t)h->nr;
+  p.M = h->M;
+  p.sp_row = (uint32_t)(2 * h->nth - 1);
+  p.R = h->R;
+  p.seis_freq = (uint32_t)h->seis_freq;
+  p.seis_T = (uint32_t)h->seis_T;
+  p.rank2 = h->rank == 2 ? 1 : 0;
+  sweep::plan(p, h->sms, (uint32_t)h->esz);
+  return p;
+}
+
+// One leapfrog step from buffer `from` into the other one.
+int launch_sweep(H* h, double dt, int from, uint32_t k_local, unsigned long long host_step) {
+  const sweep::Params p = sweep_params(h, dt, from);
+  int rc = sweep::launch(h->form, h->tv[from], h->ts[from], p, k_local, host_step, h->stream, true);
+  if (rc) return rc;
+  h->launches++;
+  return SHAW_OK;
+}
+
+void set_current(H* h, int cur) {
+  h->cur = cur;
+  h->xv = h->xvb[cur];
+  h->xs = h->xsb[cur];
+}
+
+// The seismogram of the current step (the sweep records step n - 1 during step n).
+int flush_gather(H* h, double dt) {
+  if (!h->R || !h->seis_freq || h->step == 0) return SHAW_OK;
+  const sweep::Params p = sweep_params(h, dt, h->cur);
+  int rc = sweep::launch_gather(h->form, p, h->xv, h->step, h->stream);
+  if (rc) return rc;
+  h->launches++;
+  return SHAW_OK;
+}
+
+// Graph of kGraphChunk sweep steps starting from buffer `from` (an even count, so it ends
+// on the same buffer), step numbers read from ctl->step_base.
+int ensure_sweep_graph(H* h, double dt, int from) {
+  if (h->sweep_graph[from] && h->sweep_graph_dt[from] == dt) return SHAW_OK;
+  if (h->sweep_graph[from]) {
+    cudaGraphExecDestroy(h->sweep_graph[from]);
+    h->sweep_graph[from] = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  SHAW_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  const uint64_t before = h->launches;
+  int rc = SHAW_OK;
+  for (uint32_t k = 0; k < kGraphChunk && rc == SHAW_OK; ++k) rc = launch_sweep(h, dt, from ^ (int)(k & 1), k, 0);
+  if (rc == SHAW_OK) fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, kGraphChunk);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  h->launches = before;
+  if (rc != SHAW_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaStreamEndCapture (sweep)");
+  e = cudaGraphInstantiate(&h->sweep_graph[from], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGraphInstantiate (sweep)");
+  h->sweep_graph_dt[from] = dt;
+  return SHAW_OK;
+}
+
+void drop_graphs(H* h) {
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  for (int b = 0; b < 2; ++b)
+    if (h->sweep_graph[b]) { cudaGraphExecDestroy(h->sweep_graph[b]); h->sweep_graph[b] = nullptr; }
 }
 
 // Copy the current vp (dof 0) or sp (dof 1) state into column `col` of the host snapshot matrix.
@@ -721,6 +853,30 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
   SHAW_TRY(cudaMemsetAsync(h->ctl, 0, sizeof(FomCtl), h->stream));
   SHAW_TRY(cudaMemsetAsync(h->xv, 0, nvp * M * h->esz, h->stream));
   SHAW_TRY(cudaMemsetAsync(h->xs, 0, nsp * M * h->esz, h->stream));
+  // the single sweep: every column block of 32 forcings is a tile column
+  h->xvb[0] = h->xv;
+  h->xsb[0] = h->xs;
+  if (M % sweep::kTM == 0) {
+    int dev = 0;
+    SHAW_TRY(cudaGetDevice(&dev));
+    SHAW_TRY(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev));
+    SHAW_TRY(cudaMalloc(&h->xvb[1], nvp * M * h->esz));
+    SHAW_TRY(cudaMalloc(&h->xsb[1], nsp * M * h->esz));
+    SHAW_TRY(cudaMemsetAsync(h->xvb[1], 0, nvp * M * h->esz, h->stream));
+    SHAW_TRY(cudaMemsetAsync(h->xsb[1], 0, nsp * M * h->esz, h->stream));
+    h->form = precision == SHAW_MIXED_FP32 ? sweep::kF32 : sweep::kF64Emu;
+    const size_t cv_bytes = (nvp + sweep::kCoefPadV) * 4 * h->esz, cs_bytes = (1 + nsp + sweep::kCoefPadS) * 2 * h->esz;
+    SHAW_TRY(cudaMalloc(&h->cv4, cv_bytes));
+    SHAW_TRY(cudaMalloc(&h->cs2, cs_bytes));
+    SHAW_TRY(cudaMemsetAsync(h->cv4, 0, cv_bytes, h->stream));
+    SHAW_TRY(cudaMemsetAsync(h->cs2, 0, cs_bytes, h->stream));
+    for (int b = 0; b < 2; ++b) {
+      int rc = sweep::encode_map(&h->tv[b], h->xvb[b], nvp, M, (uint32_t)h->esz, sweep::kRowsV);
+      if (rc == SHAW_OK) rc = sweep::encode_map(&h->ts[b], h->xsb[b], nsp, M, (uint32_t)h->esz, sweep::kRowsS);
+      if (rc) return bail(rc);
+    }
+    h->sweep = h->sweep_ok = true;
+  }
   SHAW_TRY(cudaStreamSynchronize(h->stream));
 #undef SHAW_TRY
   *out = h;
@@ -730,11 +886,13 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
 void shaw_fom_destroy(shaw_fom_t h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->graph) cudaGraphExecDestroy(h->graph);
+  drop_graphs(h);
   if (h->host_vp) cudaHostUnregister(h->host_vp);
   if (h->host_sp) cudaHostUnregister(h->host_sp);
-  void* bufs[] = {h->xv, h->xs, h->cvp_raw, h->csp_raw, h->cvp, h->csp, h->rho_inv, h->src, h->kind,
-                  h->period, h->delay, h->rcv, h->seis, h->staging, h->ctl};
+  if (!h->xvb[0]) { h->xvb[0] = h->xv; h->xsb[0] = h->xs; }
+  void* bufs[] = {h->xvb[0], h->xsb[0], h->xvb[1], h->xsb[1], h->cvp_raw, h->csp_raw, h->cvp, h->csp,
+                  h->cv4, h->cs2, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
+                  h->staging, h->ctl};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -767,7 +925,7 @@ int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* gid, uint32_t R, uint64
   if (h->rcv) { cudaFree(h->rcv); h->rcv = nullptr; }
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->seis_freq = 0; h->seis_T = 0; h->seis_nsteps = 0;
-  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  drop_graphs(h);
   if (R == 0) return SHAW_OK;
   if (!gid) return shaw::fail(SHAW_ERR_INVALID_ARG, "null receiver gids");
   if (freq == 0) return shaw::fail(SHAW_ERR_INVALID_ARG, "cannot have seismoFreq <=0 ");
@@ -843,6 +1001,34 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
   if ((rc = ensure_folded(h, dt))) return rc;
   const bool snaps = h->snap_fvp != 0;
   uint64_t done = 0;
+  if (h->sweep) {
+    if (!snaps && nsteps >= kGraphChunk) {
+      if ((rc = ensure_sweep_graph(h, dt, h->cur))) return rc;
+      if ((rc = set_step_base(h))) return rc;
+      const uint64_t per = kGraphChunk + 1;
+      while (nsteps - done >= kGraphChunk) {
+        SHAW_CUDA(cudaGraphLaunch(h->sweep_graph[h->cur], h->stream));
+        h->launches += per;
+        done += kGraphChunk;
+        h->step += kGraphChunk;
+      }
+    }
+    for (; done < nsteps; ++done) {
+      const unsigned long long n = h->step + 1;
+      if ((rc = launch_sweep(h, dt, h->cur, 0, n))) return rc;
+      set_current(h, h->cur ^ 1);
+      h->step++;
+      if (snaps && n % h->snap_fvp == 0) {
+        if ((rc = snapshot_copy(h, 0, h->snap_cvp))) return rc;
+        h->snap_cvp++;
+      }
+      if (snaps && n % h->snap_fsp == 0) {
+        if ((rc = snapshot_copy(h, 1, h->snap_csp))) return rc;
+        h->snap_csp++;
+      }
+    }
+    return flush_gather(h, dt);
+  }
   if (!snaps && nsteps >= kGraphChunk) {
     // Graph replay: the graph reads its step numbers from ctl->step_base.
     if ((rc = ensure_graph(h, dt))) return rc;
@@ -878,7 +1064,13 @@ int shaw_fom_synchronize(shaw_fom_t h) {
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   FomCtl c;
   SHAW_CUDA(cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  if (c.error & 1u)
+    return shaw::fail(SHAW_ERR_CUDA, "a bounded wait of the FOM sweep kernel ran out (a tile copy never arrived)");
   if (c.nonfinite) return shaw::fail(SHAW_ERR_NONFINITE, "NaN/Inf in a sampled velocity (seismogram)");
+  if (c.error & 2u)
+    return shaw::fail(SHAW_ERR_NONFINITE,
+                      "a state value became non-finite or reached 2^128 in magnitude (beyond the FP32 exponent "
+                      "range of the FP64 sweep's double-float products)");
   return SHAW_OK;
 }
 
@@ -977,6 +1169,24 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp) {
   int rc = SHAW_OK;
   if (vp && (rc = copy_state(h, nullptr, vp, h->nvp, h->xv, false))) return rc;
   if (sp && (rc = copy_state(h, nullptr, sp, h->nsp, h->xs, false))) return rc;
+  return SHAW_OK;
+}
+
+int shaw_fom_set_schedule(shaw_fom_t h, int schedule) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown FOM schedule");
+  if (schedule != SHAW_FOM_SCHEDULE_TWO_PASS && !h->sweep_ok)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the single sweep needs a multiple of 32 forcing columns");
+  if (schedule == SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA && h->precision != SHAW_FP64)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the FP64-FMA sweep needs an SHAW_FP64 handle");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  drop_graphs(h);
+  h->folded_dt = std::nan("");  // fold the stencil values of the new form on the next step
+  h->sweep = schedule != SHAW_FOM_SCHEDULE_TWO_PASS;
+  if (h->sweep_ok)
+    h->form = h->precision == SHAW_MIXED_FP32 ? sweep::kF32
+              : schedule == SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA ? sweep::kF64 : sweep::kF64Emu;
   return SHAW_OK;
 }
 
