@@ -1,7 +1,7 @@
 """The single-sweep FOM leapfrog (one kernel per step, TMA-staged tiles, alternating
 state buffers) against the oracle and against the two half-step kernels.
 
-  * SHAW_FP64, default schedule: FP64 state, double-float stencil products: 1e-12
+  * SHAW_FP64, SHAW_FOM_SCHEDULE_SWEEP: FP64 state, double-float stencil products: 1e-12
     relative to the oracle (max |gpu - oracle| / max |oracle| per array).
   * SHAW_FP64 with the FP64-FMA sweep, and SHAW_MIXED_FP32: the same FMAs in the same
     order as the two half-step kernels, so the states and seismograms are bit-identical
@@ -63,6 +63,7 @@ def test_sweep_fp64_matches_oracle(shaw, oracle, nth, nr, M):
     delays = list(rng.uniform(0.0, 20.0 * dt, M))
     rcv = [0, nth - 1, (nr - 1) * nth, m.nvp - 1] + gids[8:16]
     f = shaw.Fom(m, 2, M)
+    f.set_schedule(shaw.SCHEDULE_SWEEP)
     f.set_sources(gids, kinds, periods, delays)
     f.set_receivers(rcv, 1, n)
     f.run(dt, n)
@@ -95,7 +96,7 @@ def test_sweep_equals_two_half_steps_bitwise(shaw, oracle, nth, nr, prec, M):
     rcv = [0, nth - 1, (nr - 1) * nth + 1, m.nvp - 1] + gids[:6]
     precision = shaw.FP64 if prec == "fp64_fma" else shaw.MIXED_FP32
     out = []
-    for sched in (shaw.SCHEDULE_TWO_PASS, shaw.SCHEDULE_SWEEP_FP64_FMA if prec == "fp64_fma" else shaw.SCHEDULE_AUTO):
+    for sched in (shaw.SCHEDULE_TWO_PASS, shaw.SCHEDULE_SWEEP_FP64_FMA if prec == "fp64_fma" else shaw.SCHEDULE_SWEEP):
         f = shaw.Fom(m, 2, M, precision=precision)
         f.set_schedule(sched)
         f.set_sources(gids, "ricker", periods, 10 * dt)
@@ -118,6 +119,7 @@ def test_sweep_pieces_graphs_and_snapshots(shaw, oracle):
     periods = np.linspace(30, 80, M) * dt
     rcv = [m.map_receiver(float(a)) for a in range(0, 181, 15)] + gids[:4]
     f = shaw.Fom(m, 2, M)
+    f.set_schedule(shaw.SCHEDULE_SWEEP)
     f.set_sources(gids, "gaussDer", periods, 15 * dt)
     f.set_receivers(rcv, 1, n)
     f.run(dt, n)
