@@ -52,7 +52,7 @@ def parse():
                         "for --steps steps, for profiler captures")
     p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32"],
                    help="only run the FOM on the 1000x2000 grid with --forcings columns for --steps steps")
-    p.add_argument("--schedule", default="auto", choices=["auto", "two-pass", "sweep", "sweep-fp64-fma"],
+    p.add_argument("--schedule", default="auto", choices=["auto", "two-pass", "sweep"],
                    help="FOM schedule of --profile-fom")
     return p.parse_args()
 
@@ -714,15 +714,13 @@ def run_ours(args):
         return sum(ts) / len(ts) / 1e3
 
     # the timed run used the default schedule: for FP64 handles the two half-step kernels
-    # (faster on GB300 than either single-sweep form, timed here beside them)
+    # (on GB300 both schedules are bound by the FP64 pipe; the sweep is timed beside them)
     sweep = False
     f.set_receivers([], 0, 0)
     sched = {}
     if M % 32 == 0:
         f.set_schedule(shaw.SCHEDULE_SWEEP)
-        sched["sweep_double_float"] = timed_ms(lambda: f.advance(dt, 1))  # one fom_sweep_kernel launch
-        f.set_schedule(shaw.SCHEDULE_SWEEP_FP64_FMA)
-        sched["sweep_fp64_fma"] = timed_ms(lambda: f.advance(dt, 1))
+        sched["sweep"] = timed_ms(lambda: f.advance(dt, 1))  # one fom_sweep_kernel launch
     f.set_schedule(shaw.SCHEDULE_TWO_PASS)
     t_v = timed_ms(lambda: f.update_velocity(dt, total_steps))
     t_s = timed_ms(lambda: f.update_stress(dt))
@@ -772,10 +770,9 @@ def run_ours(args):
     ach_step = canon_step / (ms_step / 1e3) / 1e9
     dofs_step = (mesh.nvp + mesh.nsp) * M
     if sweep:
-        # one launch per step: the dominant (only) kernel; FP64 instructions: 2 adds per DOF-update
-        kern, launch_s, canon_launch = "fom_sweep_kernel (FP64 state, double-float products)", \
-            sched["sweep_double_float"], canon_step
-        fp64_instr = 2 * dofs_step
+        # one launch per step: the dominant (only) kernel
+        kern, launch_s, canon_launch = "fom_sweep_kernel", sched["sweep"], canon_step
+        fp64_instr = (4 * (mesh.nvp - 2 * mesh.nr) + 2 * mesh.nsp) * M
         sched_bytes = canon_step
     else:
         kern, launch_s, canon_launch = "fom_stress_kernel (dominant: nsp = 2 nvp)", t_s, canon_s
@@ -868,8 +865,8 @@ def main():
         gids, periods, rcv, dt = workload_inputs(np, mesh)
         m = args.forcings
         f = shaw.Fom(mesh, 2, m, precision=shaw.FP64 if args.profile_fom == "fp64" else shaw.MIXED_FP32)
-        f.set_schedule({"auto": shaw.SCHEDULE_AUTO, "two-pass": shaw.SCHEDULE_TWO_PASS, "sweep": shaw.SCHEDULE_SWEEP,
-                        "sweep-fp64-fma": shaw.SCHEDULE_SWEEP_FP64_FMA}[args.schedule])
+        f.set_schedule({"auto": shaw.SCHEDULE_AUTO, "two-pass": shaw.SCHEDULE_TWO_PASS,
+                        "sweep": shaw.SCHEDULE_SWEEP}[args.schedule])
         f.set_sources(gids[:m], "gaussDer", periods[:m], 180.0)
         f.reset()
         f.advance(dt, args.steps)

@@ -158,23 +158,20 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
 /* The handle's cudaStream_t, for callers that time with CUDA events. */
 /* Schedule of the FOM leapfrog (no counterpart in the reference, which always runs
  * its two CRS products per step, fom_update_kernels.hpp:60-181).
- *   SHAW_FOM_SCHEDULE_TWO_PASS: the two half-step kernels (FP64 or FP32 FMAs, in place).
+ *   SHAW_FOM_SCHEDULE_TWO_PASS: the two half-step kernels (in place).
  *   SHAW_FOM_SCHEDULE_SWEEP: one kernel per step (forcing columns a multiple of 32).  It
- *     reads and writes every state value once per step (16 B per FP64 DOF-update) and
- *     alternates between two state buffers.  SHAW_MIXED_FP32: FP32 FMAs; SHAW_FP64: FP64
- *     state and FP64 adds of the increments, the stencil products summed as FP32 pairs
- *     (within 1e-12 of the FP64 oracle; stencil inputs must stay below 2^128 in magnitude).
- *   SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA: the sweep with FP64 FMAs (SHAW_FP64 handles; the
- *     same results as the two-pass kernels, bit for bit).
- *   SHAW_FOM_SCHEDULE_AUTO (the default): the faster of these for the handle's precision
- *     on GB300: the sweep for SHAW_MIXED_FP32 (when the column count allows it), the
- *     two-pass kernels for SHAW_FP64.
- * The sweep schedules return SHAW_ERR_UNSUPPORTED when the column count does not allow
- * them.  Synchronizes the handle's stream. */
+ *     reads and writes every state value once per step (16 B per FP64 DOF-update, 8 B per
+ *     FP32 one) and alternates between two state buffers.  Same FMAs in the same order as
+ *     the two-pass kernels: bit-identical results.
+ *   SHAW_FOM_SCHEDULE_AUTO (the default): the faster of the two for the handle's precision
+ *     on GB300: the sweep for SHAW_MIXED_FP32 (HBM-bound, when the column count allows
+ *     it), the two-pass kernels for SHAW_FP64 (both schedules are bound by the FP64 pipe
+ *     there, and the two-pass kernels keep it busier).
+ * SHAW_FOM_SCHEDULE_SWEEP returns SHAW_ERR_UNSUPPORTED when the column count does not
+ * allow it.  Synchronizes the handle's stream. */
 #define SHAW_FOM_SCHEDULE_AUTO            0
 #define SHAW_FOM_SCHEDULE_TWO_PASS        1
-#define SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA  2
-#define SHAW_FOM_SCHEDULE_SWEEP           3
+#define SHAW_FOM_SCHEDULE_SWEEP           2
 int shaw_fom_set_schedule(shaw_fom_t h, int schedule);
 void* shaw_fom_stream(shaw_fom_t h);
 /* Kernels this handle has launched since creation (graph replays count each node). */

@@ -345,19 +345,12 @@ __global__ void fom_fold_kernel(const double* raw, T* folded, double dt, size_t 
 }
 
 // Point-major copies of the folded stencil values for the single sweep:
-// out[(shift + p) * planes + c] = dt * raw[c * n + p] in the sweep's format (FP64, FP32, or an
-// FP32 pair (hi, lo) with hi + lo within 2^-48 of the FP64 value).
-__device__ __forceinline__ void fold_to(double c, double& o) { o = c; }
-__device__ __forceinline__ void fold_to(double c, float& o) { o = (float)c; }
-__device__ __forceinline__ void fold_to(double c, float2& o) {
-  const float hi = __double2float_rn(c);
-  o = make_float2(hi, __double2float_rn(c - (double)hi));
-}
+// out[(shift + p) * planes + c] = dt * raw[c * n + p] in the state's precision.
 template <typename T>
 __global__ void fom_fold_aos_kernel(const double* raw, T* out, double dt, size_t n, uint32_t planes, size_t shift) {
   for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n * planes; k += (size_t)gridDim.x * blockDim.x) {
     const size_t p = k / planes, c = k - p * planes;
-    fold_to(dt * raw[c * n + p], out[(shift + p) * planes + c]);
+    out[(shift + p) * planes + c] = (T)(dt * raw[c * n + p]);
   }
 }
 
@@ -428,8 +421,8 @@ struct shaw_fom_s {
   void* xsb[2] = {nullptr, nullptr};
   int cur = 0;
   CUtensorMap tv[2], ts[2];          // tensor maps over the buffers (v box: strip + 1, sp box)
-  void* cv4 = nullptr;               // point-major folded stencil values of the sweep (8 bytes per value
-  void* cs2 = nullptr;               // for FP64 handles: FP64 or an FP32 pair; 4 for FP32 handles)
+  void* cv4 = nullptr;               // point-major folded stencil values of the sweep (state precision)
+  void* cs2 = nullptr;
   int sms = 0;
   cudaGraphExec_t sweep_graph[2] = {nullptr, nullptr};  // 64 steps starting from buffer 0 / 1
   double sweep_graph_dt[2] = {std::nan(""), std::nan("")};
@@ -480,8 +473,8 @@ FomArgs make_args(const H* h, double dt) {
 }
 
 // A half-step kernel on h's stream with programmatic stream serialization.
-template <typename K>
-int launch_half_step(H* h, K kern, uint32_t blocks, const FomArgs& a, uint32_t k_local, unsigned long long host_step) {
+template <typename K, typename... X>
+int launch_half_step(H* h, K kern, uint32_t blocks, const FomArgs& a, X... args) {
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(blocks);
@@ -492,7 +485,7 @@ int launch_half_step(H* h, K kern, uint32_t blocks, const FomArgs& a, uint32_t k
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a, k_local, host_step));
+  SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a, args...));
   h->launches++;
   return SHAW_OK;
 }
@@ -533,10 +526,7 @@ int ensure_folded(H* h, double dt) {
   }
   h->launches += 2;
   if (h->sweep) {
-    if (h->form == sweep::kF64Emu) {
-      fom_fold_aos_kernel<float2><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (float2*)h->cv4, dt, h->nvp, 4, 0);
-      fom_fold_aos_kernel<float2><<<1024, 256, 0, h->stream>>>(h->csp_raw, (float2*)h->cs2, dt, h->nsp, 2, 1);
-    } else if (h->form == sweep::kF64) {
+    if (h->form == sweep::kF64) {
       fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (double*)h->cv4, dt, h->nvp, 4, 0);
       fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->csp_raw, (double*)h->cs2, dt, h->nsp, 2, 1);
     } else {
@@ -636,7 +626,7 @@ int ensure_sweep_graph(H* h, double dt, int from) {
 
 // SHAW_FOM_SCHEDULE_AUTO: the faster schedule of the handle's precision (measured on GB300 at
 // 1000 x 2000, M = 256: FP32 sweep 1.84 ms vs two-pass 2.66 ms per step; FP64 two-pass 6.73 ms
-// vs the FP64-pipe sweep 7.49 ms and the double-float sweep 9.55 ms).
+// vs the sweep 7.49 ms, both bound by the FP64 pipe).
 bool auto_sweep(const H* h) { return h->sweep_ok && h->precision == SHAW_MIXED_FP32; }
 
 void drop_graphs(H* h) {
@@ -869,7 +859,7 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
     SHAW_TRY(cudaMalloc(&h->xsb[1], nsp * M * h->esz));
     SHAW_TRY(cudaMemsetAsync(h->xvb[1], 0, nvp * M * h->esz, h->stream));
     SHAW_TRY(cudaMemsetAsync(h->xsb[1], 0, nsp * M * h->esz, h->stream));
-    h->form = precision == SHAW_MIXED_FP32 ? sweep::kF32 : sweep::kF64Emu;
+    h->form = precision == SHAW_MIXED_FP32 ? sweep::kF32 : sweep::kF64;
     const size_t cv_bytes = (nvp + sweep::kCoefPadV) * 4 * h->esz, cs_bytes = (1 + nsp + sweep::kCoefPadS) * 2 * h->esz;
     SHAW_TRY(cudaMalloc(&h->cv4, cv_bytes));
     SHAW_TRY(cudaMalloc(&h->cs2, cs_bytes));
@@ -1073,10 +1063,6 @@ int shaw_fom_synchronize(shaw_fom_t h) {
   if (c.error & 1u)
     return shaw::fail(SHAW_ERR_CUDA, "a bounded wait of the FOM sweep kernel ran out (a tile copy never arrived)");
   if (c.nonfinite) return shaw::fail(SHAW_ERR_NONFINITE, "NaN/Inf in a sampled velocity (seismogram)");
-  if (c.error & 2u)
-    return shaw::fail(SHAW_ERR_NONFINITE,
-                      "a state value became non-finite or reached 2^128 in magnitude (beyond the FP32 exponent "
-                      "range of the FP64 sweep's double-float products)");
   return SHAW_OK;
 }
 
@@ -1182,17 +1168,12 @@ int shaw_fom_set_schedule(shaw_fom_t h, int schedule) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_SWEEP)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown FOM schedule");
-  if ((schedule == SHAW_FOM_SCHEDULE_SWEEP || schedule == SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA) && !h->sweep_ok)
+  if (schedule == SHAW_FOM_SCHEDULE_SWEEP && !h->sweep_ok)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "the single sweep needs a multiple of 32 forcing columns");
-  if (schedule == SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA && h->precision != SHAW_FP64)
-    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the FP64-FMA sweep needs an SHAW_FP64 handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   drop_graphs(h);
   h->folded_dt = std::nan("");  // fold the stencil values of the new form on the next step
-  h->sweep = schedule == SHAW_FOM_SCHEDULE_AUTO ? auto_sweep(h) : schedule != SHAW_FOM_SCHEDULE_TWO_PASS;
-  if (h->sweep_ok)
-    h->form = h->precision == SHAW_MIXED_FP32 ? sweep::kF32
-              : schedule == SHAW_FOM_SCHEDULE_SWEEP_FP64_FMA ? sweep::kF64 : sweep::kF64Emu;
+  h->sweep = schedule == SHAW_FOM_SCHEDULE_AUTO ? auto_sweep(h) : schedule == SHAW_FOM_SCHEDULE_SWEEP;
   return SHAW_OK;
 }
 

@@ -27,19 +27,8 @@
 // of step n-1 is gathered by extra blocks of step n from the old velocity buffer, which
 // step n does not modify; the last step of a call is gathered by launch_gather.
 //
-// FP64 arithmetic on GB300: the FP64 pipe runs ~1.2 TFLOP/s, below what a one-sweep
-// HBM-bound stencil needs (about 2.7 FMAs per DOF-update).  The kF64Emu form keeps the
-// state FP64 in HBM and adds every increment to it with FP64 adds, but forms the
-// stencil products and their sum as FP32 pairs (double-float: error-free products by
-// FMA and error-free sums, Dekker 1971 / Knuth TwoSum; Ogita-Rump-Oishi 2005) on the
-// FP32 pipe: 2 FP64 instructions per DOF-update instead of 2-4 FMAs.  The stencil
-// inputs are split into (hi, lo) FP32 pairs from their bits (24 + 24 significand bits,
-// |x - hi - lo| <= 2^-48 |x|), so each increment carries ~2^-47 relative error and the
-// state keeps FP64 rounding: within 1e-12 of the FP64 oracle over the benchmark runs.
-// Range: stencil inputs in [2^-103, 2^128) take the full pair; values in [2^-126,
-// 2^-103) keep 24 bits and smaller ones count as zero in the products (their own FP64
-// value is kept exactly); a value >= 2^128 or non-finite poisons its products with NaN
-// and sets ctl->error bit 2.
+// Forms: FP64 state with FP64 FMAs (the two-pass kernels' arithmetic in the same order,
+// so the results are bit-identical to theirs), or FP32 state with FP32 FMAs.
 //
 // Every wait is bounded: a wait that runs out sets ctl->error bit 1 and the CTA stops
 // issuing copies; before it exits it waits (bounded again) for the copies it issued.
@@ -69,80 +58,18 @@ template <int F>
 struct FT;
 template <>
 struct FT<kF64> {
-  using S = double;  // state
-  using C = double;  // folded stencil value
-  using V = double;  // v_new as kept for the stress half-step
-};
-template <>
-struct FT<kF64Emu> {
-  using S = double;
-  using C = float2;
-  using V = float2;
+  using S = double;   // state
+  using CV = double;  // folded stencil value of a vp point (velocity half-step)
+  using CS = double;  // folded stencil value of an sp point (stress half-step)
+  using V = double;   // v_new as kept for the stress half-step
 };
 template <>
 struct FT<kF32> {
   using S = float;
-  using C = float;
+  using CV = float;
+  using CS = float;
   using V = float;
 };
-
-// ---- double-float helpers (kF64Emu) ------------------------------------------------
-
-// FP64 -> (hi, lo): hi = the top 24 significand bits (truncated), lo = the next 29 bits
-// rounded to 24, both read from the bits with integer operations (no FP64 instruction).
-__device__ __forceinline__ float2 split(double x, unsigned int& bad) {
-  const uint32_t bh = (uint32_t)__double2hiint(x), bl = (uint32_t)__double2loint(x);
-  const uint32_t a = bh & 0x7FFFFFFFu;
-  // e - 896 into the FP32 exponent field: hi's bits are the FP64 bits shifted left by 3
-  const uint32_t hb = __funnelshift_l(bl, a - 0x38000000u, 3) | (bh & 0x80000000u);
-  // lo: the 29 remaining bits rounded to 23 fraction bits on top of 2^(e-1046) (hi's ulp),
-  // then that power of two subtracted again (exact: the result has the sign of x)
-  const uint32_t f0 = (hb & 0xFF800000u) - (23u << 23);
-  const uint32_t f1 = f0 + (((bl & 0x1FFFFFFFu) + 32u) >> 6);
-  float lo = __uint_as_float(f1) - __uint_as_float(f0);
-  float hi = __uint_as_float(hb);
-  // e in [920, 1150]: full pair; [897, 920): hi only; < 897: zero; > 1150: poison
-  if (a - (920u << 20) >= ((1151u - 920u) << 20)) {
-    lo = 0.0f;
-    if (a - (897u << 20) >= ((1151u - 897u) << 20)) {
-      if (a >= (1151u << 20)) {
-        bad = 1u;
-        hi = __uint_as_float(0x7FC00000u);
-        lo = hi;
-      } else {
-        hi = 0.0f;
-      }
-    }
-  }
-  return make_float2(hi, lo);
-}
-
-// FP32 -> FP64 from the bits (zero and subnormal FP32 values give +0).
-__device__ __forceinline__ double widen(float f) {
-  const uint32_t u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
-  const bool normal = a >= 0x00800000u;
-  const uint32_t hi = normal ? (((a >> 3) + 0x38000000u) | (u & 0x80000000u)) : 0u;
-  const uint32_t lo = normal ? (u << 29) : 0u;
-  return __hiloint2double((int)hi, (int)lo);
-}
-
-// c * x as an unevaluated pair (p, e): p = fl(ch xh), e = its exact error plus the
-// cross terms ch xl + cl xh.
-__device__ __forceinline__ void prod(float2 c, float2 x, float& p, float& e) {
-  p = c.x * x.x;
-  e = fmaf(c.x, x.x, -p);
-  e = fmaf(c.x, x.y, e);
-  e = fmaf(c.y, x.x, e);
-}
-
-// (s, t) += (p, e): TwoSum on the high parts, the low parts summed.
-__device__ __forceinline__ void acc(float& s, float& t, float p, float e) {
-  const float s2 = s + p;
-  const float bb = s2 - s;
-  const float err = (s - (s2 - bb)) + (p - bb);
-  t = t + (err + e);
-  s = s2;
-}
 
 // ---- the per-point updates -----------------------------------------------------------
 
@@ -152,7 +79,7 @@ struct Arith;
 template <>
 struct Arith<kF64> {
   __device__ static double vel(double v, double cN, double sN, double cS, double sS, double cW, double sW, double cE,
-                               double sE, unsigned int&) {
+                               double sE) {
     v = fma(cN, sN, v);
     v = fma(cS, sS, v);
     v = fma(cW, sW, v);
@@ -162,14 +89,12 @@ struct Arith<kF64> {
     s = fma(cA, vA, s);
     return fma(cB, vB, s);
   }
-  __device__ static double keep(double v, unsigned int&) { return v; }
-  __device__ static double operand(double x, unsigned int&) { return x; }
 };
 
 template <>
 struct Arith<kF32> {
-  __device__ static float vel(float v, float cN, float sN, float cS, float sS, float cW, float sW, float cE, float sE,
-                              unsigned int&) {
+  __device__ static float vel(float v, float cN, float sN, float cS, float sS, float cW, float sW, float cE,
+                              float sE) {
     v = fmaf(cN, sN, v);
     v = fmaf(cS, sS, v);
     v = fmaf(cW, sW, v);
@@ -179,34 +104,6 @@ struct Arith<kF32> {
     s = fmaf(cA, vA, s);
     return fmaf(cB, vB, s);
   }
-  __device__ static float keep(float v, unsigned int&) { return v; }
-  __device__ static float operand(float x, unsigned int&) { return x; }
-};
-
-template <>
-struct Arith<kF64Emu> {
-  // the stencil inputs arrive split into FP32 pairs (operand)
-  __device__ static double vel(double v, float2 cN, float2 sN, float2 cS, float2 sS, float2 cW, float2 sW, float2 cE,
-                               float2 sE, unsigned int&) {
-    float s, t, p, e;
-    prod(cN, sN, s, t);
-    prod(cS, sS, p, e);
-    acc(s, t, p, e);
-    prod(cW, sW, p, e);
-    acc(s, t, p, e);
-    prod(cE, sE, p, e);
-    acc(s, t, p, e);
-    return __dadd_rn(__dadd_rn(v, widen(s)), widen(t));
-  }
-  __device__ static double str(double sg, float2 cA, float2 vA, float2 cB, float2 vB) {
-    float s, t, p, e;
-    prod(cA, vA, s, t);
-    prod(cB, vB, p, e);
-    acc(s, t, p, e);
-    return __dadd_rn(__dadd_rn(sg, widen(s)), widen(t));
-  }
-  __device__ static float2 keep(double v, unsigned int& bad) { return split(v, bad); }
-  __device__ static float2 operand(double x, unsigned int& bad) { return split(x, bad); }
 };
 
 // ---- forcing (the same arithmetic as the two-pass kernels) -----------------------------
@@ -251,7 +148,7 @@ __device__ __forceinline__ bool wait_full(uint64_t* bar, uint32_t parity) {
 // An sp copy may start up to kPtsPer16 - 1 points early so that it is 16-byte aligned.
 template <int F>
 struct Coef {
-  using C = typename FT<F>::C;
+  using C = typename FT<F>::CS;
   static constexpr uint32_t kPtsPer16 = 16 / (2 * sizeof(C));  // sp points per 16 bytes (1 or 2)
   // sp points a row copy spans: the box and the alignment shift, rounded to whole 16 bytes
   static constexpr uint32_t kCsPts = (kRowsS + kPtsPer16 - 1 + kPtsPer16 - 1) / kPtsPer16 * kPtsPer16;
@@ -284,13 +181,14 @@ template <int F, int VEC>
 struct Smem {
   using S = typename FT<F>::S;
   using V = typename FT<F>::V;
-  using C = typename FT<F>::C;
+  using CV = typename FT<F>::CV;
+  using CS = typename FT<F>::CS;
   static constexpr uint32_t TM = Geo<F, VEC>::TM, ST = Geo<F, VEC>::STAGES;
   S v[ST][kRowsV][TM];
   S s[ST][kRowsS][TM];
   V vb[3][kRowsV][TM];
-  C cv[ST][kRowsV][4];
-  C cs[ST][Coef<F>::kCsPts][2];
+  CV cv[ST][kRowsV][4];
+  CS cs[ST][Coef<F>::kCsPts][2];
   uint64_t full[ST];   // the copies of a row have landed
   uint64_t empty[ST];  // the 8 compute warps are done with a row's slot
   unsigned int abort;
@@ -330,10 +228,10 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
                                                               const Params p, uint32_t k_local,
                                                               unsigned long long host_step) {
   using S = typename FT<F>::S;
-  using C = typename FT<F>::C;
+  using CV = typename FT<F>::CV;
+  using CS = typename FT<F>::CS;
   using V = typename FT<F>::V;
   using A = Arith<F>;
-  using Op = decltype(A::operand(S(), *(unsigned int*)nullptr));  // a stencil input as the products take it
   using SV = Vec<S, VEC>;
   using VV = Vec<V, VEC>;
   constexpr uint32_t TM = Geo<F, VEC>::TM, ST = Geo<F, VEC>::STAGES;
@@ -383,10 +281,10 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
     if (lane == 0) {
       prefetch_map(&tv);
       prefetch_map(&ts);
-      const C* cv4 = static_cast<const C*>(p.cvp);  // [nvp + pad][4]
-      const C* cs2 = static_cast<const C*>(p.csp);  // [1 + nsp + pad][2]: sp point q at q + 1
+      const CV* cv4 = static_cast<const CV*>(p.cvp);  // [nvp + pad][4]
+      const CS* cs2 = static_cast<const CS*>(p.csp);  // [1 + nsp + pad][2]: sp point q at q + 1
       constexpr uint32_t kBytesV = kRowsV * TM * sizeof(S), kBytesS = kRowsS * TM * sizeof(S);
-      constexpr uint32_t kBytesCv = kRowsV * 4 * sizeof(C), kBytesCs = Coef<F>::kCsPts * 2 * sizeof(C);
+      constexpr uint32_t kBytesCv = kRowsV * 4 * sizeof(CV), kBytesCs = Coef<F>::kCsPts * 2 * sizeof(CS);
       for (uint32_t t = base; j0 - 1 + t <= jend; ++t) {
         const uint32_t u = t - base, k = u % ST;
         if (u >= ST && !ptx::mbar_wait_n(&sm.empty[k], ((u / ST) - 1) & 1u, kWaitLimit)) {
@@ -442,8 +340,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
   S* const xv_new = static_cast<S*>(p.xv_new);
   S* const xs_new = static_cast<S*>(p.xs_new);
   const size_t M = p.M;
-  unsigned int bad = 0;
-  Op carry[3][VEC];  // srp of the previous row at each point (the next row's S neighbour)
+  S carry[3][VEC];  // srp of the previous row at each point (the next row's S neighbour)
 
   for (uint32_t t = 1;; ++t) {
     const uint32_t r = j0 - 1 + t;
@@ -469,7 +366,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
     // ---- v_new(r, i0 + li), li = 2w + q ----
     {
       VV* vb = reinterpret_cast<VV*>(&sm.vb[t % 3][0][0]);
-      Op eW[VEC];  // E neighbour of the previous point = W neighbour of this one
+      S eW[VEC];  // E neighbour of the previous point = W neighbour of this one
       bool have_e = false;
 #pragma unroll
       for (uint32_t q = 0; q < 3; ++q) {
@@ -478,7 +375,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
         if (q >= nq || i >= nth) break;
         SV v = ldv<S, VEC>(sv + li * TM);
         if (i != 0 && i + 1 != nth) {
-          const C cN = sm.cv[k][li][0], cS = sm.cv[k][li][1], cW = sm.cv[k][li][2], cE = sm.cv[k][li][3];
+          const CV cN = sm.cv[k][li][0], cS = sm.cv[k][li][1], cW = sm.cv[k][li][2], cE = sm.cv[k][li][3];
           const SV rawE = ldv<S, VEC>(ss + stp_off((int)li, last) * TM);
           SV rawW, rawN, rawS;
           if (!have_e) rawW = ldv<S, VEC>(ss + stp_off((int)li - 1, last) * TM);
@@ -486,11 +383,11 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
           if (!last) rawN = ldv<S, VEC>(ss + srp_off(li) * TM);
 #pragma unroll
           for (int c = 0; c < VEC; ++c) {
-            const Op oS = fresh_S ? A::operand(rawS.x[c], bad) : carry[q][c];
-            const Op oN = last ? oS : A::operand(rawN.x[c], bad);
-            const Op oW = have_e ? eW[c] : A::operand(rawW.x[c], bad);
-            const Op oE = A::operand(rawE.x[c], bad);
-            v.x[c] = A::vel(v.x[c], cN, oN, cS, oS, cW, oW, cE, oE, bad);
+            const S oS = fresh_S ? rawS.x[c] : carry[q][c];
+            const S oN = last ? oS : rawN.x[c];
+            const S oW = have_e ? eW[c] : rawW.x[c];
+            const S oE = rawE.x[c];
+            v.x[c] = A::vel(v.x[c], cN, oN, cS, oS, cW, oW, cE, oE);
             carry[q][c] = oN;
             eW[c] = oE;
           }
@@ -504,10 +401,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
             if (r == hit_row[q][c]) v.x[c] = forced(v.x[c], p, col + c, r * nth + i, n_step);
         }
         if (li < kTI && r < jown) stv<S, VEC>(xv_new + ((size_t)r * nth + i) * M + col, v);
-        VV kv;
-#pragma unroll
-        for (int c = 0; c < VEC; ++c) kv.x[c] = A::keep(v.x[c], bad);
-        vb[li * (TM / VEC) + lane] = kv;
+        vb[li * (TM / VEC) + lane] = v;
       }
     }
     compute_barrier();
@@ -516,7 +410,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
       const uint32_t rq = r - 1;
       const VV* vn = reinterpret_cast<const VV*>(&sm.vb[t % 3][0][0]) + lane;        // v_new(r)
       const VV* vo = reinterpret_cast<const VV*>(&sm.vb[(t - 1) % 3][0][0]) + lane;  // v_new(r - 1)
-      const C(*csq)[2] = sm.cs[kp] + cs_shift(rq);  // indexed like the sp box of row r - 1
+      const CS(*csq)[2] = sm.cs[kp] + cs_shift(rq);  // indexed like the sp box of row r - 1
       constexpr uint32_t VS = TM / VEC;              // vb stride of one point (in vectors)
 #pragma unroll
       for (uint32_t h = 0; h < 2; ++h) {
@@ -526,7 +420,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
         const size_t g = (size_t)rq * p.sp_row + 2 * i;  // srp(rq, i)
         {
           SV sg = ldv<S, VEC>(ssp + srp_off(li) * TM);
-          const C cA = csq[srp_off(li)][0], cB = csq[srp_off(li)][1];
+          const CS cA = csq[srp_off(li)][0], cB = csq[srp_off(li)][1];
           const VV a = vn[li * VS], bb = vo[li * VS];
 #pragma unroll
           for (int c = 0; c < VEC; ++c) sg.x[c] = A::str(sg.x[c], cA, a.x[c], cB, bb.x[c]);
@@ -534,7 +428,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
         }
         if (i + 1 < nth) {  // stp(rq, i)
           SV su = ldv<S, VEC>(ssp + stp_off((int)li, false) * TM);
-          const C cA = csq[stp_off((int)li, false)][0], cB = csq[stp_off((int)li, false)][1];
+          const CS cA = csq[stp_off((int)li, false)][0], cB = csq[stp_off((int)li, false)][1];
           const VV a = vo[li * VS], bb = vo[(li + 1) * VS];
 #pragma unroll
           for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c]);
@@ -545,7 +439,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
     // ---- the surface row's stp (no srp there): sigma_new(r) from v_new(r) ----
     if (last && r < jown) {
       const VV* vn = reinterpret_cast<const VV*>(&sm.vb[t % 3][0][0]) + lane;
-      const C(*csc)[2] = sm.cs[k] + cs_shift(r);
+      const CS(*csc)[2] = sm.cs[k] + cs_shift(r);
       constexpr uint32_t VS = TM / VEC;
 #pragma unroll
       for (uint32_t h = 0; h < 2; ++h) {
@@ -554,7 +448,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
         if (i + 1 >= nth) break;
         const size_t g = (size_t)r * p.sp_row + i;
         SV su = ldv<S, VEC>(ss + stp_off((int)li, true) * TM);
-        const C cA = csc[stp_off((int)li, true)][0], cB = csc[stp_off((int)li, true)][1];
+        const CS cA = csc[stp_off((int)li, true)][0], cB = csc[stp_off((int)li, true)][1];
         const VV a = vn[li * VS], bb = vn[(li + 1) * VS];
 #pragma unroll
         for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c]);
@@ -564,7 +458,6 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
     // the slot of row r - 1 is free once every compute warp is past this point
     if (lane == 0 && (t >= 2 || pre)) ptx::mbar_arrive(&sm.empty[(t - 1 - base) % ST]);
   }
-  if (bad) atomicOr(&p.ctl->error, 2u);
   allow_next_grid();
   __syncthreads();  // with the copy warp, which drains an aborted CTA's copies
 }
@@ -666,9 +559,6 @@ int launch(Form f, const CUtensorMap& tv, const CUtensorMap& ts, const Params& p
     case kF64:
       return p.vec == 2 ? launch_t<kF64, 2>(tv, ts, p, k_local, host_step, s, pdl)
                         : launch_t<kF64, 1>(tv, ts, p, k_local, host_step, s, pdl);
-    case kF64Emu:
-      return p.vec == 2 ? launch_t<kF64Emu, 2>(tv, ts, p, k_local, host_step, s, pdl)
-                        : launch_t<kF64Emu, 1>(tv, ts, p, k_local, host_step, s, pdl);
     default:
       return p.vec == 4   ? launch_t<kF32, 4>(tv, ts, p, k_local, host_step, s, pdl)
              : p.vec == 2 ? launch_t<kF32, 2>(tv, ts, p, k_local, host_step, s, pdl)

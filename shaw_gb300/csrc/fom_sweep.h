@@ -12,18 +12,14 @@ namespace shaw {
 struct FomCtl {
   unsigned long long step_base;  // steps completed before the current graph chunk
   unsigned int nonfinite;        // set when a gathered receiver value is NaN/Inf
-  unsigned int error;            // 1: a bounded wait of the sweep kernel ran out; 2: a state value
-                                 // left the range of the emulated FP64 arithmetic
+  unsigned int error;            // 1: a bounded wait of the sweep kernel ran out
 };
 
 namespace sweep {
 
-// Arithmetic of one sweep: the state in HBM is FP64 (kF64, kF64Emu) or FP32 (kF32).
-//   kF64:    FP64 FMAs (the two-pass kernels' arithmetic, in one sweep)
-//   kF64Emu: FP64 state and FP64 final adds; the stencil products and their sum in
-//            FP32 pairs (double-float) on the FP32 pipe
-//   kF32:    FP32 state and FMAs
-enum Form { kF64 = 0, kF64Emu = 1, kF32 = 2 };
+// Arithmetic of one sweep: FP64 state and FP64 FMAs (kF64, the two-pass kernels'
+// arithmetic in one sweep) or FP32 state and FP32 FMAs (kF32).
+enum Form { kF64 = 0, kF32 = 1 };
 
 constexpr uint32_t kTI = 16;               // vp points per strip (theta)
 constexpr uint32_t kTM = 32;               // forcing columns per tile at one column per lane
@@ -37,8 +33,7 @@ struct Params {
   void* xv_new;             // [nvp][M] state after the step
   void* xs_new;             // [nsp][M]
   const void* xv_old;       // [nvp][M] state before the step (seismogram of the previous step)
-  const void* cvp;          // [nvp + kCoefPadV][4] (N, S, W, E per vp point), dt folded: double, float, or
-                            // float2 (hi, lo)
+  const void* cvp;          // [nvp + kCoefPadV][4] (N, S, W, E per vp point), dt folded, in the state's type
   const void* csp;          // [1 + nsp + kCoefPadS][2] (A, B per sp point; sp point q at index q + 1)
   const double* rho_inv;
   const unsigned long long* src;  // [M] source vp gid per column

@@ -1,11 +1,9 @@
 """The single-sweep FOM leapfrog (one kernel per step, TMA-staged tiles, alternating
 state buffers) against the oracle and against the two half-step kernels.
 
-  * SHAW_FP64, SHAW_FOM_SCHEDULE_SWEEP: FP64 state, double-float stencil products: 1e-12
-    relative to the oracle (max |gpu - oracle| / max |oracle| per array).
-  * SHAW_FP64 with the FP64-FMA sweep, and SHAW_MIXED_FP32: the same FMAs in the same
-    order as the two half-step kernels, so the states and seismograms are bit-identical
-    to theirs.
+  * SHAW_FP64: 1e-12 relative to the oracle (max |gpu - oracle| / max |oracle| per array).
+  * SHAW_FP64 and SHAW_MIXED_FP32: the same FMAs in the same order as the two half-step
+    kernels, so the states and seismograms are bit-identical to theirs.
 Grids cover partial theta strips (nth not a multiple of 16, a strip holding only the
 axis point), several r segments, a segment starting on the surface row, sources on the
 axis, the CMB and the surface, corner receivers, runs in pieces with odd step counts
@@ -86,7 +84,7 @@ def test_sweep_fp64_matches_oracle(shaw, oracle, nth, nr, M):
 
 
 @pytest.mark.parametrize("nth,nr", GRIDS)
-@pytest.mark.parametrize("prec,M", [("fp64_fma", 64), ("fp64_fma", 32), ("fp32", 128), ("fp32", 64), ("fp32", 32)])
+@pytest.mark.parametrize("prec,M", [("fp64", 64), ("fp64", 32), ("fp32", 128), ("fp32", 64), ("fp32", 32)])
 def test_sweep_equals_two_half_steps_bitwise(shaw, oracle, nth, nr, prec, M):
     m, _, dt = grids(shaw, oracle, nth, nr)
     n = 140  # 2 graph chunks + 12 single steps
@@ -94,9 +92,9 @@ def test_sweep_equals_two_half_steps_bitwise(shaw, oracle, nth, nr, prec, M):
     rng = np.random.default_rng(nth)
     periods = rng.uniform(0.5, 3.0, M) * 40 * dt
     rcv = [0, nth - 1, (nr - 1) * nth + 1, m.nvp - 1] + gids[:6]
-    precision = shaw.FP64 if prec == "fp64_fma" else shaw.MIXED_FP32
+    precision = shaw.FP64 if prec == "fp64" else shaw.MIXED_FP32
     out = []
-    for sched in (shaw.SCHEDULE_TWO_PASS, shaw.SCHEDULE_SWEEP_FP64_FMA if prec == "fp64_fma" else shaw.SCHEDULE_SWEEP):
+    for sched in (shaw.SCHEDULE_TWO_PASS, shaw.SCHEDULE_SWEEP):
         f = shaw.Fom(m, 2, M, precision=precision)
         f.set_schedule(sched)
         f.set_sources(gids, "ricker", periods, 10 * dt)
@@ -146,12 +144,11 @@ def test_sweep_schedule_errors(shaw, oracle):
     m, _, _ = grids(shaw, oracle, 51, 21)
     f = shaw.Fom(m, 2, 12)  # 12 columns: the two half-step kernels only
     with pytest.raises(shaw.ShawError) as e:
-        f.set_schedule(shaw.SCHEDULE_SWEEP_FP64_FMA)
+        f.set_schedule(shaw.SCHEDULE_SWEEP)
     assert e.value.code == shaw.ERR_UNSUPPORTED
-    f.set_schedule(shaw.SCHEDULE_TWO_PASS)
-    f.close()
-    g = shaw.Fom(m, 2, 32, precision=shaw.MIXED_FP32)
     with pytest.raises(shaw.ShawError) as e:
-        g.set_schedule(shaw.SCHEDULE_SWEEP_FP64_FMA)
-    assert e.value.code == shaw.ERR_UNSUPPORTED
-    g.close()
+        f.set_schedule(7)
+    assert e.value.code == shaw.ERR_INVALID_ARG
+    f.set_schedule(shaw.SCHEDULE_TWO_PASS)
+    f.set_schedule(shaw.SCHEDULE_AUTO)
+    f.close()
