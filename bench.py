@@ -504,6 +504,9 @@ def fom_fp64_vs_fp32(np, torch, shaw, nth=2000, nr=4000, M=64, n_time=20, n_err=
             "trace_rel_err_fp32": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
             "error_probe": "velocity at the 64 source points and 7 km above them, every step",
             "error_after_steps": n_err,
+            "mixed_fp32_schedule": "single sweep (one kernel per step)",
+            "mixed_fp32_hbm_frac": v32 * 8 / 1e9 / measured_peaks()[0],
+            "fp64_hbm_frac": v64 * 16 / 1e9 / measured_peaks()[0],
             "mixed_fp32_bytes_per_dof_update": 8, "fp64_bytes_per_dof_update": 16}
 
 
