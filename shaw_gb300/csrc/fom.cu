@@ -25,6 +25,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -396,7 +397,13 @@ struct shaw_fom_s {
   double* delay = nullptr;
   unsigned long long* rcv = nullptr;
   double* seis = nullptr;
-  double* staging = nullptr;
+  // snapshot copies: two staging buffers ([M][N] FP64 columns) filled on the compute stream,
+  // read back on the copy stream while the time loop goes on
+  double* stage[2] = {nullptr, nullptr};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  bool stage_used[2] = {false, false};
+  int stage_next = 0;
   FomCtl* ctl = nullptr;
   bool sources_set = false;
   // receivers / snapshots
@@ -409,9 +416,10 @@ struct shaw_fom_s {
   double folded_dt = std::nan("");
   uint64_t step = 0;  // completed steps since reset
   uint64_t launches = 0;
-  // graph cache
+  // graph cache (a chunk of graph_len steps)
   cudaGraphExec_t graph = nullptr;
   double graph_dt = std::nan("");
+  uint64_t graph_len = 0;
   // single-sweep path (M a multiple of 32): the state alternates between two buffers each
   // step; xv / xs above always point at the current one, xvb[cur] / xsb[cur]
   bool sweep = false;                // the sweep is in use
@@ -424,8 +432,9 @@ struct shaw_fom_s {
   void* cv4 = nullptr;               // point-major folded stencil values of the sweep (state precision)
   void* cs2 = nullptr;
   int sms = 0;
-  cudaGraphExec_t sweep_graph[2] = {nullptr, nullptr};  // 64 steps starting from buffer 0 / 1
+  cudaGraphExec_t sweep_graph[2] = {nullptr, nullptr};  // a chunk of steps starting from buffer 0 / 1
   double sweep_graph_dt[2] = {std::nan(""), std::nan("")};
+  uint64_t sweep_graph_len[2] = {0, 0};
 };
 
 namespace {
@@ -596,10 +605,10 @@ int flush_gather(H* h, double dt) {
   return SHAW_OK;
 }
 
-// Graph of kGraphChunk sweep steps starting from buffer `from` (an even count, so it ends
-// on the same buffer), step numbers read from ctl->step_base.
-int ensure_sweep_graph(H* h, double dt, int from) {
-  if (h->sweep_graph[from] && h->sweep_graph_dt[from] == dt) return SHAW_OK;
+// Graph of `len` sweep steps starting from buffer `from` (it ends on buffer from ^ (len & 1)),
+// step numbers read from ctl->step_base.
+int ensure_sweep_graph(H* h, double dt, int from, uint64_t len) {
+  if (h->sweep_graph[from] && h->sweep_graph_dt[from] == dt && h->sweep_graph_len[from] == len) return SHAW_OK;
   if (h->sweep_graph[from]) {
     cudaGraphExecDestroy(h->sweep_graph[from]);
     h->sweep_graph[from] = nullptr;
@@ -608,8 +617,8 @@ int ensure_sweep_graph(H* h, double dt, int from) {
   SHAW_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const uint64_t before = h->launches;
   int rc = SHAW_OK;
-  for (uint32_t k = 0; k < kGraphChunk && rc == SHAW_OK; ++k) rc = launch_sweep(h, dt, from ^ (int)(k & 1), k, 0);
-  if (rc == SHAW_OK) fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, kGraphChunk);
+  for (uint32_t k = 0; k < len && rc == SHAW_OK; ++k) rc = launch_sweep(h, dt, from ^ (int)(k & 1), k, 0);
+  if (rc == SHAW_OK) fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, (unsigned int)len);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->launches = before;
   if (rc != SHAW_OK) {
@@ -621,6 +630,7 @@ int ensure_sweep_graph(H* h, double dt, int from) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGraphInstantiate (sweep)");
   h->sweep_graph_dt[from] = dt;
+  h->sweep_graph_len[from] = len;
   return SHAW_OK;
 }
 
@@ -635,26 +645,53 @@ void drop_graphs(H* h) {
     if (h->sweep_graph[b]) { cudaGraphExecDestroy(h->sweep_graph[b]); h->sweep_graph[b] = nullptr; }
 }
 
-// Copy the current vp (dof 0) or sp (dof 1) state into column `col` of the host snapshot matrix.
+// Copy the current vp (dof 0) or sp (dof 1) state into column `col` of the host snapshot
+// matrix (StateObserver::observe, state_observer.hpp:175-203).  The state is transposed
+// (or copied, for one FP64 column) into a staging buffer on the compute stream; the copy to
+// the page-locked host matrix runs on the copy stream, overlapping the next steps.  The two
+// staging buffers alternate; a buffer is refilled only after its previous copy is done.
 int snapshot_copy(H* h, int dof, uint64_t col) {
   const uint64_t N = dof == 0 ? h->nvp : h->nsp;
   const uint64_t T = h->snap_nsteps / (dof == 0 ? h->snap_fvp : h->snap_fsp);
   double* host = dof == 0 ? h->host_vp : h->host_sp;
   const void* dev = dof == 0 ? h->xv : h->xs;
+  const int b = h->stage_next;
+  h->stage_next ^= 1;
+  if (h->stage_used[b]) SHAW_CUDA(cudaStreamWaitEvent(h->stream, h->ev_free[b], 0));
   if (h->M == 1 && h->esz == sizeof(double)) {
-    SHAW_CUDA(cudaMemcpyAsync(host + N * col, dev, N * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    return SHAW_OK;
+    SHAW_CUDA(cudaMemcpyAsync(h->stage[b], dev, N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  } else {
+    dim3 grid((unsigned)((N + 31) / 32), (h->M + 31) / 32);
+    if (h->esz == sizeof(float))
+      fom_transpose_kernel<float><<<grid, dim3(32, 8), 0, h->stream>>>((const float*)dev, h->stage[b], (uint32_t)N,
+                                                                       h->M);
+    else
+      fom_transpose_kernel<double><<<grid, dim3(32, 8), 0, h->stream>>>((const double*)dev, h->stage[b], (uint32_t)N,
+                                                                        h->M);
+    h->launches++;
+    SHAW_CUDA(cudaGetLastError());
   }
-  dim3 grid((unsigned)((N + 31) / 32), (h->M + 31) / 32);
-  if (h->esz == sizeof(float))
-    fom_transpose_kernel<float><<<grid, dim3(32, 8), 0, h->stream>>>((const float*)dev, h->staging, (uint32_t)N, h->M);
-  else
-    fom_transpose_kernel<double><<<grid, dim3(32, 8), 0, h->stream>>>((const double*)dev, h->staging, (uint32_t)N,
-                                                                      h->M);
-  h->launches++;
-  SHAW_CUDA(cudaGetLastError());
-  SHAW_CUDA(cudaMemcpy2DAsync(host + N * col, N * T * sizeof(double), h->staging, N * sizeof(double),
-                              N * sizeof(double), h->M, cudaMemcpyDeviceToHost, h->stream));
+  SHAW_CUDA(cudaEventRecord(h->ev_ready[b], h->stream));
+  SHAW_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_ready[b], 0));
+  SHAW_CUDA(cudaMemcpy2DAsync(host + N * col, N * T * sizeof(double), h->stage[b], N * sizeof(double),
+                              N * sizeof(double), h->M, cudaMemcpyDeviceToHost, h->copy_stream));
+  SHAW_CUDA(cudaEventRecord(h->ev_free[b], h->copy_stream));
+  h->stage_used[b] = true;
+  return SHAW_OK;
+}
+
+// The snapshots of step h->step that fall due.
+int snapshots_due(H* h) {
+  const uint64_t n = h->step;
+  int rc = SHAW_OK;
+  if (n % h->snap_fvp == 0) {
+    if ((rc = snapshot_copy(h, 0, h->snap_cvp))) return rc;
+    h->snap_cvp++;
+  }
+  if (n % h->snap_fsp == 0) {
+    if ((rc = snapshot_copy(h, 1, h->snap_csp))) return rc;
+    h->snap_csp++;
+  }
   return SHAW_OK;
 }
 
@@ -665,10 +702,10 @@ int check_ready(H* h, double dt) {
   return SHAW_OK;
 }
 
-// Build (once per dt) a graph of kGraphChunk steps that reads its step numbers
+// Build (once per dt and length) a graph of `len` steps that reads its step numbers
 // from the device-side step_base and advances it at the end.
-int ensure_graph(H* h, double dt) {
-  if (h->graph && h->graph_dt == dt) return SHAW_OK;
+int ensure_graph(H* h, double dt, uint64_t len) {
+  if (h->graph && h->graph_dt == dt && h->graph_len == len) return SHAW_OK;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -678,12 +715,12 @@ int ensure_graph(H* h, double dt) {
   SHAW_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const uint64_t before = h->launches;
   int rc = SHAW_OK;
-  for (uint32_t k = 0; k < kGraphChunk && rc == SHAW_OK; ++k) {
+  for (uint32_t k = 0; k < len && rc == SHAW_OK; ++k) {
     rc = launch_velocity(h, a, k, 0);
     if (rc == SHAW_OK) rc = launch_stress(h, a, k, 0);
   }
   if (rc == SHAW_OK) {
-    fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, kGraphChunk);
+    fom_advance_base_kernel<<<1, 1, 0, h->stream>>>(h->ctl, (unsigned int)len);
   }
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->launches = before;  // captured launches are counted when the graph is replayed
@@ -696,6 +733,7 @@ int ensure_graph(H* h, double dt) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return shaw::cuda_fail(e, "cudaGraphInstantiate");
   h->graph_dt = dt;
+  h->graph_len = len;
   return SHAW_OK;
 }
 
@@ -882,15 +920,21 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
 void shaw_fom_destroy(shaw_fom_t h) {
   if (!h) return;
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
   drop_graphs(h);
   if (h->host_vp) cudaHostUnregister(h->host_vp);
   if (h->host_sp) cudaHostUnregister(h->host_sp);
   if (!h->xvb[0]) { h->xvb[0] = h->xv; h->xsb[0] = h->xs; }
   void* bufs[] = {h->xvb[0], h->xsb[0], h->xvb[1], h->xsb[1], h->cvp_raw, h->csp_raw, h->cvp, h->csp,
                   h->cv4, h->cs2, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
-                  h->staging, h->ctl};
+                  h->stage[0], h->stage[1], h->ctl};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  for (int b = 0; b < 2; ++b) {
+    if (h->ev_ready[b]) cudaEventDestroy(h->ev_ready[b]);
+    if (h->ev_free[b]) cudaEventDestroy(h->ev_free[b]);
+  }
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -945,6 +989,7 @@ int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
                            double* host_sp) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->copy_stream) SHAW_CUDA(cudaStreamSynchronize(h->copy_stream));
   if (h->host_vp) cudaHostUnregister(h->host_vp);
   if (h->host_sp) cudaHostUnregister(h->host_sp);
   h->host_vp = h->host_sp = nullptr;
@@ -962,14 +1007,29 @@ int shaw_fom_set_snapshots(shaw_fom_t h, uint64_t fvp, uint64_t fsp, uint64_t ns
     cudaHostUnregister(host_vp);
     return shaw::cuda_fail(e, "cudaHostRegister(host_sp)");
   }
-  if ((h->M > 1 || h->esz != sizeof(double)) && !h->staging) {
-    e = cudaMalloc(&h->staging, std::max(h->nvp, h->nsp) * h->M * sizeof(double));
+  if (!h->copy_stream) {
+    e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+      e = cudaEventCreateWithFlags(&h->ev_ready[b], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
       cudaHostUnregister(host_vp);
       cudaHostUnregister(host_sp);
-      return shaw::cuda_fail(e, "cudaMalloc(staging)");
+      return shaw::cuda_fail(e, "snapshot copy stream / events");
     }
   }
+  for (int b = 0; b < 2; ++b) {
+    if (h->stage[b]) continue;
+    e = cudaMalloc(&h->stage[b], std::max(h->nvp, h->nsp) * h->M * sizeof(double));
+    if (e != cudaSuccess) {
+      cudaHostUnregister(host_vp);
+      cudaHostUnregister(host_sp);
+      return shaw::cuda_fail(e, "cudaMalloc(snapshot staging)");
+    }
+  }
+  h->stage_used[0] = h->stage_used[1] = false;
+  h->stage_next = 0;
   h->host_vp = host_vp; h->host_sp = host_sp;
   h->snap_fvp = fvp; h->snap_fsp = fsp; h->snap_nsteps = nsteps;
   return SHAW_OK;
@@ -995,69 +1055,59 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
   if (h->snap_fvp && h->step + nsteps > h->snap_nsteps)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
   if ((rc = ensure_folded(h, dt))) return rc;
+  // Steps run as replays of a captured chunk (64 steps; with snapshots, the steps between
+  // two sample steps, so that every chunk ends on one) and single launches before and after.
+  // The snapshots of a sample step are taken right after it (both half-steps done: the
+  // velocity of step n is not changed by its stress half-step).
   const bool snaps = h->snap_fvp != 0;
-  uint64_t done = 0;
-  if (h->sweep) {
-    if (!snaps && nsteps >= kGraphChunk) {
-      if ((rc = ensure_sweep_graph(h, dt, h->cur))) return rc;
-      if ((rc = set_step_base(h))) return rc;
-      const uint64_t per = kGraphChunk + 1;
-      while (nsteps - done >= kGraphChunk) {
-        SHAW_CUDA(cudaGraphLaunch(h->sweep_graph[h->cur], h->stream));
-        h->launches += per;
-        done += kGraphChunk;
-        h->step += kGraphChunk;
-      }
-    }
-    for (; done < nsteps; ++done) {
-      const unsigned long long n = h->step + 1;
-      if ((rc = launch_sweep(h, dt, h->cur, 0, n))) return rc;
-      set_current(h, h->cur ^ 1);
-      h->step++;
-      if (snaps && n % h->snap_fvp == 0) {
-        if ((rc = snapshot_copy(h, 0, h->snap_cvp))) return rc;
-        h->snap_cvp++;
-      }
-      if (snaps && n % h->snap_fsp == 0) {
-        if ((rc = snapshot_copy(h, 1, h->snap_csp))) return rc;
-        h->snap_csp++;
-      }
-    }
-    return flush_gather(h, dt);
-  }
-  if (!snaps && nsteps >= kGraphChunk) {
-    // Graph replay: the graph reads its step numbers from ctl->step_base.
-    if ((rc = ensure_graph(h, dt))) return rc;
-    if ((rc = set_step_base(h))) return rc;
-    const uint64_t per = 2 * kGraphChunk + 1;
-    while (nsteps - done >= kGraphChunk) {
-      SHAW_CUDA(cudaGraphLaunch(h->graph, h->stream));
-      h->launches += per;
-      done += kGraphChunk;
-      h->step += kGraphChunk;
-    }
-  }
+  const uint64_t len = snaps ? std::gcd(h->snap_fvp, h->snap_fsp) : kGraphChunk;
+  const bool graphs = len >= 4 && len <= 4096;
+  bool base_valid = false;  // ctl->step_base == h->step
   const FomArgs a = make_args(h, dt);
-  for (; done < nsteps; ++done) {
-    const unsigned long long n = h->step + 1;
-    if ((rc = launch_velocity(h, a, 0, n))) return rc;
-    if (snaps && n % h->snap_fvp == 0) {
-      if ((rc = snapshot_copy(h, 0, h->snap_cvp))) return rc;
-      h->snap_cvp++;
+  uint64_t done = 0;
+  while (done < nsteps) {
+    if (graphs && nsteps - done >= len && (!snaps || h->step % len == 0)) {
+      if (h->sweep) {
+        if ((rc = ensure_sweep_graph(h, dt, h->cur, len))) return rc;
+      } else if ((rc = ensure_graph(h, dt, len))) {
+        return rc;
+      }
+      if (!base_valid) {
+        if ((rc = set_step_base(h))) return rc;
+        base_valid = true;
+      }
+      if (h->sweep) {
+        SHAW_CUDA(cudaGraphLaunch(h->sweep_graph[h->cur], h->stream));
+        h->launches += len + 1;
+        set_current(h, h->cur ^ (int)(len & 1));
+      } else {
+        SHAW_CUDA(cudaGraphLaunch(h->graph, h->stream));
+        h->launches += 2 * len + 1;
+      }
+      done += len;
+      h->step += len;
+    } else {
+      const unsigned long long n = h->step + 1;
+      if (h->sweep) {
+        if ((rc = launch_sweep(h, dt, h->cur, 0, n))) return rc;
+        set_current(h, h->cur ^ 1);
+      } else {
+        if ((rc = launch_velocity(h, a, 0, n))) return rc;
+        if ((rc = launch_stress(h, a, 0, n))) return rc;
+      }
+      ++done;
+      ++h->step;
+      base_valid = false;
     }
-    if ((rc = launch_stress(h, a, 0, n))) return rc;
-    if (snaps && n % h->snap_fsp == 0) {
-      if ((rc = snapshot_copy(h, 1, h->snap_csp))) return rc;
-      h->snap_csp++;
-    }
-    h->step++;
+    if (snaps && (rc = snapshots_due(h))) return rc;
   }
-  return SHAW_OK;
+  return h->sweep ? flush_gather(h, dt) : SHAW_OK;
 }
 
 int shaw_fom_synchronize(shaw_fom_t h) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->copy_stream) SHAW_CUDA(cudaStreamSynchronize(h->copy_stream));
   FomCtl c;
   SHAW_CUDA(cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost));
   if (c.error & 1u)
