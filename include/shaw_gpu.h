@@ -172,6 +172,13 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
 #define SHAW_FOM_SCHEDULE_AUTO            0
 #define SHAW_FOM_SCHEDULE_TWO_PASS        1
 #define SHAW_FOM_SCHEDULE_SWEEP           2
+#define SHAW_FOM_SCHEDULE_PERSISTENT      3  /* rank 1, FP64, small grids: all the steps of a
+                                              * call in one cooperative launch (one CTA per SM,
+                                              * each a band of r rows in shared memory, halo
+                                              * rows exchanged through L2 as tagged words);
+                                              * bit-identical to the two-pass kernels; not with
+                                              * snapshots.  AUTO takes it for rank-1 FP64
+                                              * handles whose grid fits. */
 int shaw_fom_set_schedule(shaw_fom_t h, int schedule);
 void* shaw_fom_stream(shaw_fom_t h);
 /* Kernels this handle has launched since creation (graph replays count each node). */

@@ -19,7 +19,7 @@ EXE = os.path.join(BUILD, "shaw_exe")
 POD_EXE = os.path.join(BUILD, "computeThinSVD")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["fom.cu", "fom_sweep.cu", "rom.cu", "rom_tc.cu", "rom_oz.cu", "rom_batch.cu", "pod.cu"]
+CU_SOURCES = ["fom.cu", "fom_sweep.cu", "fom_band.cu", "rom.cu", "rom_tc.cu", "rom_oz.cu", "rom_batch.cu", "pod.cu"]
 CPP_SOURCES = ["host.cpp", "driver.cpp", "rom_driver.cpp", "pod_driver.cpp", "yaml_lite.cpp"]
 
 

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "fom_sweep.h"
+#include "fom_band.h"
 #include "shaw_internal.h"
 
 namespace shaw {
@@ -59,6 +60,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint32_t kGraphChunk = 64;  // leapfrog steps per captured CUDA graph
+constexpr uint64_t kBandSteps = 1 << 16;  // leapfrog steps per persistent band launch
 
 using shaw::FomCtl;
 namespace sweep = shaw::sweep;
@@ -432,6 +434,16 @@ struct shaw_fom_s {
   void* cv4 = nullptr;               // point-major folded stencil values of the sweep (state precision)
   void* cs2 = nullptr;
   int sms = 0;
+  // rank-1 persistent band path (small FP64 grids): bands, rows per band, shared memory
+  bool band_ok = false, use_band = false;
+  uint32_t band_n = 0, band_rows = 0;
+  size_t band_smem = 0;
+  double* ftab = nullptr;                 // [kBandSteps] forcing increments of one band launch
+  unsigned long long* xwords = nullptr;   // halo exchange words, down then up
+  uint32_t band_tag = 0;                  // last tag used in xwords (0: cleared)
+  uint64_t src0 = 0;  // the rank-1 source: gid, kind, period, delay
+  int kind0 = 0;
+  double period0 = 0, delay0 = 0;
   cudaGraphExec_t sweep_graph[2] = {nullptr, nullptr};  // a chunk of steps starting from buffer 0 / 1
   double sweep_graph_dt[2] = {std::nan(""), std::nan("")};
   uint64_t sweep_graph_len[2] = {0, 0};
@@ -911,6 +923,9 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
     h->sweep_ok = true;
     h->sweep = auto_sweep(h);
   }
+  if (rank == 1 && precision == SHAW_FP64)
+    h->band_ok = h->use_band =
+        shaw::band::plan((uint32_t)h->nth, (uint32_t)h->nr, &h->band_n, &h->band_rows, &h->band_smem);
   SHAW_TRY(cudaStreamSynchronize(h->stream));
 #undef SHAW_TRY
   *out = h;
@@ -926,7 +941,7 @@ void shaw_fom_destroy(shaw_fom_t h) {
   if (h->host_sp) cudaHostUnregister(h->host_sp);
   if (!h->xvb[0]) { h->xvb[0] = h->xv; h->xsb[0] = h->xs; }
   void* bufs[] = {h->xvb[0], h->xsb[0], h->xvb[1], h->xsb[1], h->cvp_raw, h->csp_raw, h->cvp, h->csp,
-                  h->cv4, h->cs2, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
+                  h->cv4, h->cs2, h->ftab, h->xwords, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
                   h->stage[0], h->stage[1], h->ctl};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -955,6 +970,10 @@ int shaw_fom_set_sources(shaw_fom_t h, const uint64_t* gid, const int32_t* kind,
   SHAW_CUDA(cudaMemcpyAsync(h->period, period, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_CUDA(cudaMemcpyAsync(h->delay, delay, h->M * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->src0 = gid[0];
+  h->kind0 = kind[0];
+  h->period0 = period[0];
+  h->delay0 = delay[0];
   h->sources_set = true;
   return SHAW_OK;
 }
@@ -1055,6 +1074,56 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
   if (h->snap_fvp && h->step + nsteps > h->snap_nsteps)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
   if ((rc = ensure_folded(h, dt))) return rc;
+  if (h->use_band && h->snap_fvp == 0 && nsteps > 0) {
+    // all the steps of this call in one persistent launch of row bands
+    shaw::band::Args c;
+    std::memset(&c, 0, sizeof(c));
+    c.cvp = static_cast<const double*>(h->cvp);
+    c.csp = static_cast<const double*>(h->csp);
+    c.xv = static_cast<double*>(h->xv);
+    c.xs = static_cast<double*>(h->xs);
+    c.rho_inv = h->rho_inv;
+    c.src = h->src0;
+    c.kind = h->kind0;
+    c.period = h->period0;
+    c.delay = h->delay0;
+    c.dt = dt;
+    c.rcv = h->rcv;
+    c.seis = h->seis;
+    c.ctl = h->ctl;
+    c.nth = (uint32_t)h->nth;
+    c.nr = (uint32_t)h->nr;
+    c.rows = h->band_rows;
+    c.R = h->R;
+    c.seis_freq = (uint32_t)h->seis_freq;
+    c.seis_T = (uint32_t)h->seis_T;
+    const size_t words = shaw::band::exchange_words(h->band_n, (uint32_t)h->nth);
+    if (!h->ftab) {
+      SHAW_CUDA(cudaMalloc(&h->ftab, kBandSteps * sizeof(double)));
+      SHAW_CUDA(cudaMalloc(&h->xwords, 2 * words * sizeof(unsigned long long)));
+      SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, 2 * words * sizeof(unsigned long long), h->stream));
+      h->band_tag = 0;
+    }
+    c.ftab = h->ftab;
+    c.xdown = h->xwords;
+    c.xup = h->xwords + words;
+    // launches of at most kBandSteps steps, each filling the forcing table it reads
+    for (uint64_t done = 0; done < nsteps;) {
+      c.step0 = h->step;
+      c.nsteps = std::min<uint64_t>(kBandSteps, nsteps - done);
+      if ((uint64_t)h->band_tag + c.nsteps >= 0xffffffffull) {  // tags would wrap: clear the words
+        SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, 2 * words * sizeof(unsigned long long), h->stream));
+        h->band_tag = 0;
+      }
+      c.tag0 = h->band_tag + 1;
+      if ((rc = shaw::band::launch(c, h->band_n, h->band_smem, h->stream))) return rc;
+      h->band_tag += (uint32_t)c.nsteps;
+      h->launches += 2;
+      h->step += c.nsteps;
+      done += c.nsteps;
+    }
+    return SHAW_OK;
+  }
   // Steps run as replays of a captured chunk (64 steps; with snapshots, the steps between
   // two sample steps, so that every chunk ends on one) and single launches before and after.
   // The snapshots of a sample step are taken right after it (both half-steps done: the
@@ -1111,7 +1180,9 @@ int shaw_fom_synchronize(shaw_fom_t h) {
   FomCtl c;
   SHAW_CUDA(cudaMemcpy(&c, h->ctl, sizeof(c), cudaMemcpyDeviceToHost));
   if (c.error & 1u)
-    return shaw::fail(SHAW_ERR_CUDA, "a bounded wait of the FOM sweep kernel ran out (a tile copy never arrived)");
+    return shaw::fail(SHAW_ERR_CUDA,
+                      "a bounded wait of a persistent FOM kernel ran out (a tile copy or a neighbour's row never "
+                      "arrived)");
   if (c.nonfinite) return shaw::fail(SHAW_ERR_NONFINITE, "NaN/Inf in a sampled velocity (seismogram)");
   return SHAW_OK;
 }
@@ -1216,14 +1287,19 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp) {
 
 int shaw_fom_set_schedule(shaw_fom_t h, int schedule) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
-  if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_SWEEP)
+  if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_PERSISTENT)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown FOM schedule");
   if (schedule == SHAW_FOM_SCHEDULE_SWEEP && !h->sweep_ok)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "the single sweep needs a multiple of 32 forcing columns");
+  if (schedule == SHAW_FOM_SCHEDULE_PERSISTENT && !h->band_ok)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED,
+                      "the persistent schedule needs a rank-1 FP64 handle on a grid of at least two r rows "
+                      "whose row bands (one per SM) fit a CTA");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   drop_graphs(h);
   h->folded_dt = std::nan("");  // fold the stencil values of the new form on the next step
   h->sweep = schedule == SHAW_FOM_SCHEDULE_AUTO ? auto_sweep(h) : schedule == SHAW_FOM_SCHEDULE_SWEEP;
+  h->use_band = schedule == SHAW_FOM_SCHEDULE_AUTO ? h->band_ok : schedule == SHAW_FOM_SCHEDULE_PERSISTENT;
   return SHAW_OK;
 }
 

@@ -1,0 +1,47 @@
+// fom_band.h -- the rank-1 FOM leapfrog of a small grid as one persistent cooperative
+// launch (fom_band.cu), used by fom.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "fom_sweep.h"
+
+namespace shaw {
+namespace band {
+
+struct Args {
+  const double* cvp;  // 4 planes of nvp (N, S, W, E), dt folded
+  const double* csp;  // 2 planes of nsp (A, B), dt folded
+  double* xv;         // [nvp] state (read at the start, written at the end)
+  double* xs;         // [nsp]
+  const double* rho_inv;
+  unsigned long long src;
+  int kind;
+  double period, delay, dt;
+  const unsigned long long* rcv;
+  double* seis;  // [R x T]
+  double* ftab;  // [nsteps]: the forcing increment of each step (filled by launch)
+  FomCtl* ctl;
+  // halo exchange words: [bands][nth][2] each, a (tag, half of a double) pair per word
+  unsigned long long* xdown;  // band b's lowest v row, read by band b - 1
+  unsigned long long* xup;    // band b's highest srp row, read by band b + 1
+  unsigned long long step0, nsteps;
+  uint32_t tag0;  // tag of the launch's first step (>= 1); step it carries tag0 + it
+  uint32_t nth, nr, rows, R, seis_freq, seis_T;
+};
+
+// Band rows, band count and shared memory for an nth x nr grid; false when the grid does
+// not fit one co-resident band per CTA on this device.
+bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* rows, size_t* smem);
+
+// Exchange words (unsigned long long) that `bands` bands of nth points need per direction.
+inline size_t exchange_words(uint32_t bands, uint32_t nth) { return (size_t)bands * nth * 2; }
+
+// nsteps leapfrog steps of the rank-1 FOM in one cooperative launch on stream s.
+int launch(const Args& a, uint32_t bands, size_t smem, cudaStream_t s);
+
+}  // namespace band
+}  // namespace shaw
