@@ -440,6 +440,7 @@ struct shaw_fom_s {
   size_t band_smem = 0;
   double* ftab = nullptr;                 // [kBandSteps] forcing increments of one band launch
   unsigned long long* xwords = nullptr;   // halo exchange words, down then up
+  unsigned long long* rcv_sorted = nullptr;  // [R][2] (gid, receiver) pairs in gid order
   uint32_t band_tag = 0;                  // last tag used in xwords (0: cleared)
   uint64_t src0 = 0;  // the rank-1 source: gid, kind, period, delay
   int kind0 = 0;
@@ -941,7 +942,7 @@ void shaw_fom_destroy(shaw_fom_t h) {
   if (h->host_sp) cudaHostUnregister(h->host_sp);
   if (!h->xvb[0]) { h->xvb[0] = h->xv; h->xsb[0] = h->xs; }
   void* bufs[] = {h->xvb[0], h->xsb[0], h->xvb[1], h->xsb[1], h->cvp_raw, h->csp_raw, h->cvp, h->csp,
-                  h->cv4, h->cs2, h->ftab, h->xwords, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
+                  h->cv4, h->cs2, h->ftab, h->xwords, h->rcv_sorted, h->rho_inv, h->src, h->kind, h->period, h->delay, h->rcv, h->seis,
                   h->stage[0], h->stage[1], h->ctl};
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -982,6 +983,7 @@ int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* gid, uint32_t R, uint64
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   if (h->rcv) { cudaFree(h->rcv); h->rcv = nullptr; }
+  if (h->rcv_sorted) { cudaFree(h->rcv_sorted); h->rcv_sorted = nullptr; }
   if (h->seis) { cudaFree(h->seis); h->seis = nullptr; }
   h->R = 0; h->seis_freq = 0; h->seis_T = 0; h->seis_nsteps = 0;
   drop_graphs(h);
@@ -998,6 +1000,20 @@ int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* gid, uint32_t R, uint64
   SHAW_CUDA(cudaMalloc(&h->rcv, R * sizeof(unsigned long long)));
   SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
   SHAW_CUDA(cudaMemcpyAsync(h->rcv, gid, R * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+  if (h->band_ok) {  // (gid, receiver) pairs in gid order: each row band reads a contiguous range
+    std::vector<unsigned long long> pairs(2 * (size_t)R);
+    std::vector<uint32_t> order(R);
+    for (uint32_t r = 0; r < R; ++r) order[r] = r;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return gid[x] < gid[y]; });
+    for (uint32_t q = 0; q < R; ++q) {
+      pairs[2 * (size_t)q] = gid[order[q]];
+      pairs[2 * (size_t)q + 1] = order[q];
+    }
+    SHAW_CUDA(cudaMalloc(&h->rcv_sorted, 2 * (size_t)R * sizeof(unsigned long long)));
+    SHAW_CUDA(cudaMemcpyAsync(h->rcv_sorted, pairs.data(), 2 * (size_t)R * sizeof(unsigned long long),
+                              cudaMemcpyHostToDevice, h->stream));
+    SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  }
   SHAW_CUDA(cudaMemsetAsync(h->seis, 0, (size_t)R * T * h->M * sizeof(double), h->stream));
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   h->R = R; h->seis_freq = freq; h->seis_T = T; h->seis_nsteps = nsteps;
@@ -1088,7 +1104,7 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
     c.period = h->period0;
     c.delay = h->delay0;
     c.dt = dt;
-    c.rcv = h->rcv;
+    c.rcv_sorted = h->rcv_sorted;
     c.seis = h->seis;
     c.ctl = h->ctl;
     c.nth = (uint32_t)h->nth;
@@ -1097,22 +1113,23 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
     c.R = h->R;
     c.seis_freq = (uint32_t)h->seis_freq;
     c.seis_T = (uint32_t)h->seis_T;
-    const size_t words = shaw::band::exchange_words(h->band_n, (uint32_t)h->nth);
+    const size_t dw = shaw::band::down_words(h->band_n, (uint32_t)h->nth);
+    const size_t words = dw + shaw::band::up_words(h->band_n, (uint32_t)h->nth);
     if (!h->ftab) {
       SHAW_CUDA(cudaMalloc(&h->ftab, kBandSteps * sizeof(double)));
-      SHAW_CUDA(cudaMalloc(&h->xwords, 2 * words * sizeof(unsigned long long)));
-      SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, 2 * words * sizeof(unsigned long long), h->stream));
+      SHAW_CUDA(cudaMalloc(&h->xwords, words * sizeof(unsigned long long)));
+      SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, words * sizeof(unsigned long long), h->stream));
       h->band_tag = 0;
     }
     c.ftab = h->ftab;
     c.xdown = h->xwords;
-    c.xup = h->xwords + words;
+    c.xup = h->xwords + dw;
     // launches of at most kBandSteps steps, each filling the forcing table it reads
     for (uint64_t done = 0; done < nsteps;) {
       c.step0 = h->step;
       c.nsteps = std::min<uint64_t>(kBandSteps, nsteps - done);
       if ((uint64_t)h->band_tag + c.nsteps >= 0xffffffffull) {  // tags would wrap: clear the words
-        SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, 2 * words * sizeof(unsigned long long), h->stream));
+        SHAW_CUDA(cudaMemsetAsync(h->xwords, 0, words * sizeof(unsigned long long), h->stream));
         h->band_tag = 0;
       }
       c.tag0 = h->band_tag + 1;

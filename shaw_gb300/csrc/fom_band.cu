@@ -4,24 +4,31 @@
 // DOFs) does a fraction of a microsecond of FP64 work per step spread over the GPU, so
 // the two half-step launches, not arithmetic, bound the step.  Here one cooperative grid
 // (all CTAs co-resident, one per SM) runs all the steps of a call.  CTA b owns a band of
-// `rows` r rows and keeps in shared memory its velocity rows plus the row above (a halo),
-// its srp rows plus the row below (a halo), its stp rows, and the folded stencil values
-// of all of them.  Per step:
-//   1. v of the band (the two-pass velocity kernel's FMAs, same order) and the forcing;
-//      the band's lowest v row goes straight from the registers to band b - 1;
-//   2. wait for the halo v row from band b + 1; the receivers of the band;
-//   3. sigma of the band (the stress kernel's FMAs, same order); the band's highest srp
-//      row goes straight to band b + 1;
-//   4. wait for the halo srp row from band b - 1.
+// `rows` r rows j0 .. j1 - 1 and keeps in shared memory its velocity rows plus v(j1), its
+// srp rows plus srp(j0 - 1) and srp(j1), its stp rows plus stp(j1, .), and the folded
+// stencil values of all of them.  Row j1 belongs to band b + 1, which computes the same
+// v(j1) from the same inputs; computing it here too spares one exchange per step.
+//
+// The step is ordered so that only what a neighbour waits for lies between receiving and
+// sending.  The "edge" velocity rows are those that read a received row: j0 (when a band
+// exists below) and j1 (when one exists above); all other velocity rows are "interior".
+//   1. v of the edge rows (the two-pass velocity kernel's FMAs, same order, and the
+//      forcing);
+//   2. sigma of the srp rows and of the stp row j0 (the stress kernel's FMAs, same order);
+//      the band's lowest srp and stp rows go straight from the registers to band b - 1,
+//      its highest srp row to band b + 1;
+//   3. while those rows travel: sigma of the other stp rows, the receivers of the band,
+//      and v of the interior rows for the NEXT step (they read only this band's rows);
+//   4. wait for srp(j1) and stp(j1, .) from band b + 1 and srp(j0 - 1) from band b - 1.
 // Rows travel through L2 as self-validating 8-byte words: each carries 32 bits of the
 // double and a 32-bit tag naming the step, so a reader polls the data itself; no flag,
 // fence or second round trip follows the data.  Each 8-byte word is written and read by
 // single-copy-atomic accesses, so a word is never seen half old and half new.  Tags grow
 // monotonically over the life of the buffers (the host clears them before the 32-bit tag
-// would wrap), so a word left by an earlier step or launch never matches.  One word pair
-// per point and direction suffices: band b overwrites its row of step n only after it
-// has received the neighbour's row of step n - 1, which that neighbour sends after it has
-// consumed b's row of step n - 1.
+// would wrap), so a word left by an earlier step or launch never matches.  Each direction
+// has two slots, by step parity: band b writes its rows of step n + 2 into the slot of step
+// n only after it has received the neighbour's rows of step n + 1, which that neighbour
+// sends after it has read b's rows of step n.
 // Results are bit-identical to the two half-step kernels.  Every wait is bounded: a wait
 // that runs out sets ctl->error bit 1 and the CTA leaves the loop; its neighbours' waits
 // then run out in turn, so the launch always ends.
@@ -35,14 +42,14 @@
 namespace shaw {
 namespace band {
 
-constexpr uint32_t kThreads = 256;
-constexpr int kBatch = 4;                      // elements of a phase per thread, processed side by side
-constexpr uint32_t kPollLimit = 1u << 22;      // polls of one word pair before a wait gives up (about a second)
+constexpr uint32_t kThreads = 512;
+constexpr int kBatch = 2;                      // elements of a set per thread, processed side by side
+constexpr uint32_t kPollLimit = 1u << 22;      // polling rounds before a wait gives up (about a second)
 
 // Doubles of shared memory a CTA with `rows` rows needs.
 inline size_t smem_doubles(uint32_t nth, uint32_t rows) {
-  return (size_t)(rows + 1) * nth * 2 + (size_t)rows * (nth - 1) + (size_t)4 * rows * nth + (size_t)2 * rows * nth +
-         (size_t)2 * rows * (nth - 1);
+  return (size_t)(rows + 1) * nth + (size_t)(rows + 2) * nth + (size_t)(rows + 1) * (nth - 1) +
+         (size_t)4 * (rows + 1) * nth + (size_t)2 * rows * nth + (size_t)2 * rows * (nth - 1);
 }
 
 namespace {
@@ -56,19 +63,6 @@ __device__ __forceinline__ void put(unsigned long long* w, uint32_t tag, double 
                "l"(t | (u & 0xffffffffull))
                : "memory");
 }
-// Bounded wait for the point tagged `tag`; false when the poll limit runs out.
-__device__ __forceinline__ bool get(const unsigned long long* w, uint32_t tag, double* v) {
-  for (uint32_t k = 0; k < kPollLimit; ++k) {
-    unsigned long long hi, lo;
-    asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(hi), "=l"(lo) : "l"(w) : "memory");
-    if ((uint32_t)(hi >> 32) == tag && (uint32_t)(lo >> 32) == tag) {
-      *v = __longlong_as_double((long long)((hi << 32) | (lo & 0xffffffffull)));
-      return true;
-    }
-  }
-  return false;
-}
-
 // The forcing increments of the steps of a launch: ftab[s] = (dt rhoInv[src]) f(t) at
 // t = (step0 + s) dt, rounded as KokkosBlas::mult(1, x, dt, rhoInv, f) forms them, so the
 // kernel adds each with one FP64 add (the same roundings as the half-step kernels).
@@ -79,183 +73,326 @@ __global__ void fom_band_forcing_kernel(Args a) {
   a.ftab[s] = __dmul_rn(__dmul_rn(a.dt, a.rho_inv[a.src]), f);
 }
 
+// A set of velocity points of this thread: p = place in V (-1 when absent) and a packed
+// word m: bit 0 = interior theta point (the stencil applies), bit 1 = N is srp(j) (else
+// srp(j - 1), at the surface), bit 2 = S is srp(j - 1) (else srp(j), at the CMB), bits 3..
+// = the local row rl.  In SRP, srp(j) is at p + nth and srp(j - 1) at p; in STP,
+// stp(j, i - 1) is at p - rl - 1 and stp(j, i) follows.
+struct VelSet {
+  int p[kBatch], m[kBatch];
+};
+
+// updateVelocity of a set (fom_velocity_kernel's FMAs, same order), plus the forcing of the
+// source point when FORCE: only the warp holding the source runs that form, so the other
+// warps issue no FP64 add on the narrow FP64 pipe.
+template <bool FORCE>
+__device__ __forceinline__ void velocity(const VelSet& e, double* V, const double* SRP, const double* STP,
+                                         const double* CV, uint32_t nv, uint32_t nth, int src_p, double fdt) {
+#pragma unroll
+  for (int k = 0; k < kBatch; ++k) {
+    if (e.p[k] < 0) continue;
+    const int p = e.p[k], m = e.m[k];
+    double v = V[p];
+    if (m & 1) {
+      const int w = p - (m >> 3) - 1;
+      v = fma(CV[p], SRP[(m & 2) ? p + (int)nth : p], v);           // N
+      v = fma(CV[nv + p], SRP[(m & 4) ? p : p + (int)nth], v);      // S
+      v = fma(CV[2 * nv + p], STP[w], v);                           // W
+      v = fma(CV[3 * nv + p], STP[w + 1], v);                       // E
+    }
+    if (FORCE && p == src_p) v = __dadd_rn(v, fdt);  // after the FMAs, as the half-step kernel
+    V[p] = v;
+  }
+}
+
+// The halo rows of a step, points q = t, t + nt, ... (at most kRecvMax) of the received set:
+// first the message from above (srp(j1) when it exists, then stp(j1, .)), then srp(j0 - 1)
+// from below.  Each round issues the loads of all the thread's pending points before it
+// checks any, so their round trips overlap.
+constexpr int kRecvMax = 4;
+__device__ __forceinline__ bool receive(const unsigned long long* recv_above, const unsigned long long* recv_below,
+                                        uint32_t slot, uint32_t tag, size_t down_pts, size_t up_pts,
+                                        uint32_t n_above, uint32_t n_recv, bool srp_above, uint32_t nth,
+                                        uint32_t nrow, double* SRP, double* STP, uint32_t t, uint32_t nt) {
+  const unsigned long long* src[kRecvMax];
+  double* dst[kRecvMax];
+  uint32_t pending = 0;
+#pragma unroll
+  for (int k = 0; k < kRecvMax; ++k) {
+    const uint32_t q = t + k * nt;
+    src[k] = nullptr;
+    dst[k] = nullptr;
+    if (q >= n_recv) continue;
+    pending |= 1u << k;
+    if (q < n_above) {
+      const uint32_t pa = srp_above ? q : q + nth;  // point of the message from above
+      src[k] = recv_above + (size_t)slot * down_pts * 2 + 2 * pa;
+      dst[k] = pa < nth ? SRP + (size_t)(nrow + 1) * nth + pa : STP + (size_t)nrow * (nth - 1) + (pa - nth);
+    } else {
+      const uint32_t pb = q - n_above;
+      src[k] = recv_below + (size_t)slot * up_pts * 2 + 2 * pb;
+      dst[k] = SRP + pb;
+    }
+  }
+  for (uint32_t round = 0; pending && round < kPollLimit; ++round) {
+    unsigned long long hi[kRecvMax], lo[kRecvMax];
+#pragma unroll
+    for (int k = 0; k < kRecvMax; ++k)
+      if (pending & (1u << k))
+        asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(hi[k]), "=l"(lo[k]) : "l"(src[k]) : "memory");
+#pragma unroll
+    for (int k = 0; k < kRecvMax; ++k)
+      if ((pending & (1u << k)) && (uint32_t)(hi[k] >> 32) == tag && (uint32_t)(lo[k] >> 32) == tag) {
+        *dst[k] = __longlong_as_double((long long)((hi[k] << 32) | (lo[k] & 0xffffffffull)));
+        pending &= ~(1u << k);
+      }
+  }
+  return pending == 0;
+}
+
 __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
   const uint32_t b = blockIdx.x;
   const uint32_t nth = a.nth, nr = a.nr, rows = a.rows;
   const uint32_t j0 = b * rows, j1 = min(nr, j0 + rows), nrow = j1 - j0;  // plan: every band owns rows
-  const bool up = j1 < nr;   // a band above exists (halo row v(j1) from it, srp row j1 - 1 to it)
-  const bool down = j0 > 0;  // a band below exists (halo row srp(j0 - 1) from it, v row j0 to it)
+  const bool up = j1 < nr;   // a band above exists: v(j1) computed here, srp(j1), stp(j1, .) from it
+  const bool down = j0 > 0;  // a band below exists: srp(j0 - 1) from it
+  const bool srp_above = j1 + 1 < nr;  // srp(j1) exists
+  const uint32_t vrows = nrow + (up ? 1 : 0);
   const uint32_t sp_row = 2 * nth - 1;
   const size_t nvp = (size_t)nth * nr, nsp = (size_t)(nr - 1) * nth + (size_t)nr * (nth - 1);
   extern __shared__ __align__(16) double sm[];
-  double* const V = sm;                                // (rows + 1) x nth: v rows j0 .. j1
-  double* const SRP = V + (size_t)(rows + 1) * nth;    // (rows + 1) x nth: srp rows j0 - 1 .. j1 - 1
-  double* const STP = SRP + (size_t)(rows + 1) * nth;  // rows x (nth - 1)
-  double* const CV = STP + (size_t)rows * (nth - 1);   // 4 x rows x nth
-  double* const CSR = CV + (size_t)4 * rows * nth;     // 2 x rows x nth (srp rows j0 .. j1 - 1)
-  double* const CST = CSR + (size_t)2 * rows * nth;    // 2 x rows x (nth - 1)
-  const uint32_t nv = rows * nth, ns = rows * (nth - 1);
-  unsigned long long* const send_down = a.xdown + (size_t)b * nth * 2;
-  unsigned long long* const send_up = a.xup + (size_t)b * nth * 2;
-  const unsigned long long* const recv_above = up ? a.xdown + (size_t)(b + 1) * nth * 2 : nullptr;
-  const unsigned long long* const recv_below = down ? a.xup + (size_t)(b - 1) * nth * 2 : nullptr;
+  double* const V = sm;                                     // (rows + 1) x nth: v rows j0 .. j1
+  double* const SRP = V + (size_t)(rows + 1) * nth;         // (rows + 2) x nth: srp rows j0 - 1 .. j1
+  double* const STP = SRP + (size_t)(rows + 2) * nth;       // (rows + 1) x (nth - 1): stp rows j0 .. j1
+  double* const CV = STP + (size_t)(rows + 1) * (nth - 1);  // 4 x (rows + 1) x nth: rows j0 .. j1
+  double* const CSR = CV + (size_t)4 * (rows + 1) * nth;    // 2 x rows x nth: srp rows j0 .. j1 - 1
+  double* const CST = CSR + (size_t)2 * rows * nth;         // 2 x rows x (nth - 1)
+  const uint32_t nv = (rows + 1) * nth, nsr = rows * nth, ns = rows * (nth - 1);
+  // messages: down = srp(j0, .) then stp(j0, .) (2 nth - 1 points), up = srp(j1 - 1, .) (nth)
+  const size_t down_pts = 2 * (size_t)nth - 1, up_pts = nth;
+  unsigned long long* const send_down = a.xdown + (size_t)b * 2 * down_pts * 2;  // + slot * down_pts * 2
+  unsigned long long* const send_up = a.xup + (size_t)b * 2 * up_pts * 2;
+  const unsigned long long* const recv_above = up ? a.xdown + (size_t)(b + 1) * 2 * down_pts * 2 : nullptr;
+  const unsigned long long* const recv_below = down ? a.xup + (size_t)(b - 1) * 2 * up_pts * 2 : nullptr;
 
   // the band, its halos and its stencil values
-  for (uint32_t e = threadIdx.x; e < (nrow + (up ? 1 : 0)) * nth; e += kThreads) V[e] = a.xv[(size_t)j0 * nth + e];
-  for (uint32_t e = threadIdx.x; e < (rows + 1) * nth; e += kThreads) {
+  for (uint32_t e = threadIdx.x; e < vrows * nth; e += kThreads) V[e] = a.xv[(size_t)j0 * nth + e];
+  for (uint32_t e = threadIdx.x; e < (nrow + 2) * nth; e += kThreads) {
     const uint32_t rl = e / nth, i = e - rl * nth;
     const int j = (int)j0 - 1 + (int)rl;  // srp row
-    SRP[e] = (j >= 0 && j + 1 < (int)nr && j < (int)j1) ? a.xs[(size_t)j * sp_row + 2 * i] : 0.0;
+    SRP[e] = (j >= 0 && j + 1 < (int)nr && j <= (int)j1) ? a.xs[(size_t)j * sp_row + 2 * i] : 0.0;
   }
-  for (uint32_t e = threadIdx.x; e < nrow * (nth - 1); e += kThreads) {
+  for (uint32_t e = threadIdx.x; e < vrows * (nth - 1); e += kThreads) {
     const uint32_t rl = e / (nth - 1), i = e - rl * (nth - 1), j = j0 + rl;
     const size_t q = (j + 1 < nr) ? (size_t)j * sp_row + 2 * i + 1 : (size_t)j * sp_row + i;
     STP[e] = a.xs[q];
-    CST[e] = a.csp[q];
-    CST[ns + e] = a.csp[nsp + q];
+    if (rl < nrow) {
+      CST[e] = a.csp[q];
+      CST[ns + e] = a.csp[nsp + q];
+    }
   }
-  for (uint32_t e = threadIdx.x; e < nrow * nth; e += kThreads) {
+  for (uint32_t e = threadIdx.x; e < vrows * nth; e += kThreads) {
     const size_t p = (size_t)j0 * nth + e;
     for (int c = 0; c < 4; ++c) CV[c * nv + e] = a.cvp[c * nvp + p];
     const uint32_t rl = e / nth, i = e - rl * nth, j = j0 + rl;
-    if (j + 1 < nr) {
+    if (rl < nrow && j + 1 < nr) {
       const size_t q = (size_t)j * sp_row + 2 * i;
       CSR[e] = a.csp[q];
-      CSR[nv + e] = a.csp[nsp + q];
+      CSR[nsr + e] = a.csp[nsp + q];
     }
   }
-  // This thread's elements, fixed for every step.  Velocity element k is band point
-  // e = t + k kThreads in row order, so the lowest row (sent down) comes first.  Stress
-  // element k counts the rows from the top, so the highest srp row (sent up) comes first.
-  int ev[kBatch], eN[kBatch], eS[kBatch], eW[kBatch], es[kBatch], est[kBatch], estW[kBatch];
-  bool interior[kBatch], send_v[kBatch], send_s[kBatch];
-  int src_k = -1;
+
+  // This thread's elements, fixed for every step.  The velocity rows in band order, edge
+  // rows first: local rows 0 (if down) and nrow (if up) are edge rows; e counts the edge
+  // points, then the interior points.
+  const uint32_t n_edge_rows = (down ? 1 : 0) + (up ? 1 : 0);
+  const uint32_t n_int_rows = vrows - n_edge_rows;
+  const uint32_t stp2_row0 = down ? 1 : 0, n_s2 = (nrow - stp2_row0) * (nth - 1);
+  // Roles while the rows travel.  The received points: srp(j1) (when it exists) and
+  // stp(j1, .) from above, srp(j0 - 1) from below.  When the other work fits the warps
+  // left over, the first warps (one lane per received point) poll from the moment the
+  // band's own rows are sent, and the other warps compute the other stp rows, the
+  // receivers and the next step's interior velocity meanwhile; otherwise every thread
+  // does that work first and polls afterwards.
+  const uint32_t n_above = up ? (srp_above ? nth : 0) + nth - 1 : 0;
+  const uint32_t n_recv = n_above + (down ? nth : 0);
+  const uint32_t poll_threads = min(kThreads, 32 * ((n_recv + 31) / 32));
+  const uint32_t work_threads = kThreads - poll_threads;
+  const bool split = work_threads > 0 && n_s2 <= kBatch * work_threads && n_int_rows * nth <= kBatch * work_threads;
+  const bool poller = !split || threadIdx.x < poll_threads;
+  const bool worker = !split || threadIdx.x >= poll_threads;
+  const uint32_t wt = split ? threadIdx.x - poll_threads : threadIdx.x;  // index among the workers
+  const uint32_t nwt = split ? work_threads : kThreads;
+  const uint32_t npt = split ? poll_threads : kThreads;
+  auto vel_row = [&](bool edge, uint32_t r) -> uint32_t {  // local v row of the r-th edge / interior row
+    if (edge) return (down && r == 0) ? 0 : nrow;
+    return r + (down ? 1 : 0);
+  };
+  VelSet ve, vi;
+  const int src_p = (a.src >= (unsigned long long)j0 * nth && a.src < (unsigned long long)(j0 + vrows) * nth)
+                        ? (int)(a.src - (unsigned long long)j0 * nth)
+                        : -1;
+  bool ve_src = false, vi_src = false;
+#pragma unroll
+  for (int k = 0; k < kBatch; ++k) {
+#pragma unroll
+    for (int set = 0; set < 2; ++set) {
+      VelSet& vs = set ? vi : ve;
+      const uint32_t nrows_set = set ? n_int_rows : n_edge_rows;
+      // the edge rows over all threads, the interior rows over the workers
+      const uint32_t e = set ? (worker ? wt + k * nwt : ~0u) : threadIdx.x + k * kThreads;
+      vs.p[k] = -1;
+      vs.m[k] = 0;
+      if (e < nrows_set * nth) {
+        const uint32_t rl = vel_row(set == 0, e / nth), i = e % nth, j = j0 + rl;
+        const uint32_t pt = rl * nth + i;
+        vs.p[k] = (int)pt;
+        vs.m[k] = (i != 0 && i + 1 != nth ? 1 : 0) | (j + 1 < nr ? 2 : 0) | (j > 0 ? 4 : 0) | (int)(rl << 3);
+        if ((int)pt == src_p) (set ? vi_src : ve_src) = true;
+      }
+    }
+  }
+  // stress, first set: the srp rows, then stp row j0 when it is sent down; second set: the
+  // other stp rows.  Message points: -1 when the element is not sent.
+  const uint32_t n_srp = (up ? nrow : nrow - 1) * nth;  // srp(j) exists for j <= nr - 2
+  const uint32_t n_s1 = n_srp + (down ? nth - 1 : 0);
+  // First set: s1a = place (-1 when absent) and s1m: bit 0 = srp element (else stp),
+  // bit 1 = sent up, bit 2 = sent down, bits 3.. = the message point.  An srp(j0 + rl, i)
+  // element is SRP[s1a + nth] and reads V[s1a], V[s1a + nth]; the stp(j0, i) element is
+  // STP[s1a] and reads V[s1a], V[s1a + 1].  Second set: stp(j, i) at STP[s2a], v(j, i) at V[s2w].
+  int s1a[kBatch], s1m[kBatch], s2a[kBatch], s2w[kBatch];
 #pragma unroll
   for (int k = 0; k < kBatch; ++k) {
     const uint32_t e = threadIdx.x + k * kThreads;
-    ev[k] = es[k] = est[k] = -1;
-    interior[k] = send_v[k] = send_s[k] = false;
-    if (e < nrow * nth) {
-      const uint32_t rl = e / nth, i = e - rl * nth, j = j0 + rl;
-      ev[k] = (int)e;
-      interior[k] = i != 0 && i + 1 != nth;
-      eN[k] = (j + 1 < nr) ? (int)((rl + 1) * nth + i) : (int)(rl * nth + i);  // srp(j) or, at the surface, srp(j - 1)
-      eS[k] = (j > 0) ? (int)(rl * nth + i) : (int)((rl + 1) * nth + i);      // srp(j - 1) or, at the CMB, srp(j)
-      eW[k] = (int)(rl * (nth - 1) + i) - 1;                                   // stp(j, i - 1); stp(j, i) follows
-      send_v[k] = down && rl == 0;
-      if ((unsigned long long)j * nth + i == a.src) src_k = k;
-      const uint32_t rs = nrow - 1 - rl;  // stress: the same point set, rows counted from the top
-      if (j0 + rs + 1 < nr) {
-        es[k] = (int)(rs * nth + i);  // srp(j0 + rs, i) is SRP[es + nth]; v(j0 + rs, i) is V[es]
-        send_s[k] = up && rs == nrow - 1;
-      }
+    s1a[k] = s2a[k] = -1;
+    s1m[k] = 0;
+    if (e < n_srp) {  // srp(j0 + rl, i), rows from the top so that srp(j1 - 1) leads
+      const uint32_t rl = n_srp / nth - 1 - e / nth, i = e % nth;
+      s1a[k] = (int)(rl * nth + i);
+      s1m[k] = 1 | (up && j0 + rl == j1 - 1 ? 2 : 0) | (down && rl == 0 ? 4 : 0) | (int)(i << 3);
+    } else if (e < n_s1) {  // stp(j0, i), sent down
+      const uint32_t i = e - n_srp;
+      s1a[k] = (int)i;
+      s1m[k] = 4 | (int)((nth + i) << 3);
     }
-    if (e < nrow * (nth - 1)) {
-      const uint32_t rs = nrow - 1 - e / (nth - 1), i = e % (nth - 1);
-      est[k] = (int)(rs * (nth - 1) + i);
-      estW[k] = (int)(rs * nth + i);  // v(j, i) in V; v(j, i + 1) follows
+    const uint32_t e2 = worker ? wt + k * nwt : ~0u;  // the other stp rows over the workers
+    if (e2 < n_s2) {
+      const uint32_t rl = stp2_row0 + e2 / (nth - 1), i = e2 % (nth - 1);
+      s2a[k] = (int)(rl * (nth - 1) + i);
+      s2w[k] = (int)(rl * nth + i);  // v(j, i) in V; v(j, i + 1) follows
     }
   }
-  __syncthreads();
+  // the warps that hold the source run the forcing form of their velocity set
+  const bool ve_force = __any_sync(0xffffffffu, ve_src), vi_force = __any_sync(0xffffffffu, vi_src);
 
+  // the band's receivers: a range of the gid-ordered list; the sampling phase and the
+  // sample count before the launch's first step (step step0 + 1)
+  __shared__ uint32_t s_rcv[2];
+  if (threadIdx.x < 2) {
+    const unsigned long long key = (unsigned long long)(threadIdx.x ? j1 : j0) * nth;
+    uint32_t lo = 0, hi = a.R;  // first entry with gid >= key
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (a.rcv_sorted[2 * (size_t)mid] < key) lo = mid + 1; else hi = mid;
+    }
+    s_rcv[threadIdx.x] = lo;
+  }
+  uint32_t phase = a.seis_freq ? (uint32_t)(a.step0 % a.seis_freq) : 0;
+  uint32_t sample = 0;  // clamped at seis_T: samples past the seismogram's length are dropped
+  if (a.seis_freq) {
+    const unsigned long long s0 = a.step0 / a.seis_freq;
+    sample = s0 < a.seis_T ? (uint32_t)s0 : a.seis_T;
+  }
+  __syncthreads();
+  const uint32_t rcv_lo = s_rcv[0], rcv_hi = s_rcv[1];
+
+  // the interior velocity rows of the first step
+  if (a.nsteps > 0) {
+    if (vi_force) velocity<true>(vi, V, SRP, STP, CV, nv, nth, src_p, a.ftab[0]);
+    else velocity<false>(vi, V, SRP, STP, CV, nv, nth, -1, 0.0);
+  }
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
-    const unsigned long long n = a.step0 + it + 1;
     const uint32_t tag = a.tag0 + (uint32_t)it;
-    // 1. velocity (each thread reads and writes only its own v elements in this phase)
+    const uint32_t slot = (uint32_t)(it & 1);
+    // 1. velocity of the edge rows (each thread reads and writes only its own v elements)
+    if (ve_force) velocity<true>(ve, V, SRP, STP, CV, nv, nth, src_p, a.ftab[it]);
+    else velocity<false>(ve, V, SRP, STP, CV, nv, nth, -1, 0.0);
+    __syncthreads();
+    // 2. stress of the rows a neighbour waits for; each goes out as soon as it is computed
+    //    (each thread reads and writes only its own stress elements; v is fixed)
     {
-      double v[kBatch], c[kBatch][4], x[kBatch][4];
+      unsigned long long* const sd = send_down + (size_t)slot * down_pts * 2;
+      unsigned long long* const su = send_up + (size_t)slot * up_pts * 2;
 #pragma unroll
       for (int k = 0; k < kBatch; ++k) {
-        if (ev[k] < 0) continue;
-        v[k] = V[ev[k]];
-        if (interior[k]) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) c[k][q] = CV[q * nv + ev[k]];
-          x[k][0] = SRP[eN[k]];
-          x[k][1] = SRP[eS[k]];
-          x[k][2] = STP[eW[k]];
-          x[k][3] = STP[eW[k] + 1];
+        if (s1a[k] < 0) continue;
+        const int e = s1a[k], m = s1m[k];
+        double y;
+        if (m & 1) {
+          y = SRP[e + nth];
+          y = fma(CSR[e], V[e + nth], y);  // north v(j + 1, i)
+          y = fma(CSR[nsr + e], V[e], y);  // south v(j, i)
+          SRP[e + nth] = y;
+        } else {
+          y = STP[e];
+          y = fma(CST[e], V[e], y);           // west v(j0, i)
+          y = fma(CST[ns + e], V[e + 1], y);  // east v(j0, i + 1)
+          STP[e] = y;
         }
-      }
-      const double fdt = src_k >= 0 ? a.ftab[it] : 0.0;
-#pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (ev[k] < 0) continue;
-        if (interior[k]) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) v[k] = fma(c[k][q], x[k][q], v[k]);
-        }
-        if (k == src_k) v[k] = __dadd_rn(v[k], fdt);
-        if (send_v[k]) put(send_down + 2 * ev[k], tag, v[k]);
-        V[ev[k]] = v[k];
+        if (m & 2) put(su + 2 * (m >> 3), tag, y);
+        if (m & 4) put(sd + 2 * (m >> 3), tag, y);
       }
     }
-    // 2. the halo v row j1 from the band above
+    // 3. while the rows travel: the other stp rows, the receivers, the next interior velocity
+    //    (workers); 4. srp(j1), stp(j1, .) from the band above and srp(j0 - 1) from below
+    //    (pollers).  Work and polls touch different rows: the polls write only the halo rows.
+    const bool sampling = a.seis_freq && ++phase == a.seis_freq;
+    if (sampling) phase = 0;
     bool ok = true;
-    if (up)
-      for (uint32_t i = threadIdx.x; i < nth; i += kThreads) {
-        double x;
-        if (get(recv_above + 2 * i, tag, &x))
-          V[(size_t)nrow * nth + i] = x;
-        else
-          ok = false;
-      }
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
-      break;
+    if (split && poller) {
+      asm volatile("bar.arrive 1, %0;" ::"r"(kThreads) : "memory");  // this thread's reads of v are done
+      ok = receive(recv_above, recv_below, slot, tag, down_pts, up_pts, n_above, n_recv, srp_above, nth, nrow,
+                   SRP, STP, threadIdx.x, npt);
     }
-    // the receivers of the band (Seismogram::storeVelocitySignalAtReceivers)
-    if (a.seis_freq && n % a.seis_freq == 0) {
-      const unsigned long long cnt = n / a.seis_freq - 1;
-      for (uint32_t r = threadIdx.x; r < a.R; r += kThreads) {
-        const unsigned long long g = a.rcv[r];
-        if (g >= (unsigned long long)j0 * nth && g < (unsigned long long)j1 * nth && cnt < a.seis_T) {
+    if (worker) {
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) {
+        if (s2a[k] < 0) continue;
+        const int e = s2a[k];
+        double y = STP[e];
+        y = fma(CST[e], V[s2w[k]], y);
+        y = fma(CST[ns + e], V[s2w[k] + 1], y);
+        STP[e] = y;
+      }
+      // the receivers of the band (Seismogram::storeVelocitySignalAtReceivers)
+      if (sampling && sample < a.seis_T) {
+        for (uint32_t q = rcv_lo + wt; q < rcv_hi; q += nwt) {
+          const unsigned long long g = a.rcv_sorted[2 * (size_t)q], r = a.rcv_sorted[2 * (size_t)q + 1];
           const double val = V[g - (unsigned long long)j0 * nth];
-          a.seis[r + (size_t)a.R * cnt] = val;
+          a.seis[r + (size_t)a.R * sample] = val;
           if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
         }
       }
-    }
-    // 3. stress (each thread reads and writes only its own stress elements; v is fixed)
-    {
-      double sr[kBatch], st[kBatch];
-#pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (es[k] >= 0) {
-          const int e = es[k];
-          sr[k] = SRP[e + nth];
-          sr[k] = fma(CSR[e], V[e + nth], sr[k]);  // north v(j + 1, i)
-          sr[k] = fma(CSR[nv + e], V[e], sr[k]);   // south v(j, i)
-          if (send_s[k]) put(send_up + 2 * (e - (nrow - 1) * nth), tag, sr[k]);
-        }
-        if (est[k] >= 0) {
-          const int e = est[k];
-          st[k] = STP[e];
-          st[k] = fma(CST[e], V[estW[k]], st[k]);           // west v(j, i)
-          st[k] = fma(CST[ns + e], V[estW[k] + 1], st[k]);  // east v(j, i + 1)
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (es[k] >= 0) SRP[es[k] + nth] = sr[k];
-        if (est[k] >= 0) STP[est[k]] = st[k];
+      // every read of this step's v and every stress row is done
+      if (split)
+        asm volatile("bar.sync 1, %0;" ::"r"(kThreads) : "memory");
+      else
+        __syncthreads();
+      if (it + 1 < a.nsteps) {
+        if (vi_force) velocity<true>(vi, V, SRP, STP, CV, nv, nth, src_p, a.ftab[it + 1]);
+        else velocity<false>(vi, V, SRP, STP, CV, nv, nth, -1, 0.0);
       }
     }
-    // 4. the halo srp row j0 - 1 from the band below
-    if (down)
-      for (uint32_t i = threadIdx.x; i < nth; i += kThreads) {
-        double x;
-        if (get(recv_below + 2 * i, tag, &x))
-          SRP[i] = x;
-        else
-          ok = false;
-      }
+    if (sampling && sample < a.seis_T) ++sample;
+    if (!split)
+      ok = receive(recv_above, recv_below, slot, tag, down_pts, up_pts, n_above, n_recv, srp_above, nth, nrow, SRP,
+                   STP, threadIdx.x, npt);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
       break;
     }
   }
-  // the band back to the state
+  // the band back to the state (its own rows only)
   for (uint32_t e = threadIdx.x; e < nrow * nth; e += kThreads) a.xv[(size_t)j0 * nth + e] = V[e];
   for (uint32_t e = threadIdx.x; e < nrow * nth; e += kThreads) {
     const uint32_t rl = e / nth, i = e - rl * nth, j = j0 + rl;
@@ -281,7 +418,8 @@ bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* rows, size_t* sm
   const uint32_t r = (nr + (uint32_t)sms - 1) / (uint32_t)sms;
   const uint32_t g = (nr + r - 1) / r;
   if (g < 2) return false;
-  if ((size_t)r * nth > (size_t)kBatch * kThreads) return false;  // a band is at most kBatch points a thread
+  if ((size_t)(r + 1) * nth > (size_t)kBatch * kThreads) return false;  // at most kBatch points a thread
+  if (3 * (size_t)nth > (size_t)kRecvMax * kThreads) return false;       // received points: under 3 nth
   const size_t bytes = smem_doubles(nth, r) * sizeof(double);
   if (bytes + 1024 > (size_t)optin) return false;
   if (cudaFuncSetAttribute(fom_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {

@@ -21,13 +21,13 @@ struct Args {
   unsigned long long src;
   int kind;
   double period, delay, dt;
-  const unsigned long long* rcv;
-  double* seis;  // [R x T]
+  const unsigned long long* rcv_sorted;  // [R][2]: (gid, receiver index) pairs in gid order
+  double* seis;                          // [R x T]
   double* ftab;  // [nsteps]: the forcing increment of each step (filled by launch)
   FomCtl* ctl;
-  // halo exchange words: [bands][nth][2] each, a (tag, half of a double) pair per word
-  unsigned long long* xdown;  // band b's lowest v row, read by band b - 1
-  unsigned long long* xup;    // band b's highest srp row, read by band b + 1
+  // halo exchange words, a (tag, half of a double) pair per point, two slots per band:
+  unsigned long long* xdown;  // [bands][2][2 nth - 1][2]: band b's lowest srp and stp rows, read by band b - 1
+  unsigned long long* xup;    // [bands][2][nth][2]: band b's highest srp row, read by band b + 1
   unsigned long long step0, nsteps;
   uint32_t tag0;  // tag of the launch's first step (>= 1); step it carries tag0 + it
   uint32_t nth, nr, rows, R, seis_freq, seis_T;
@@ -37,8 +37,9 @@ struct Args {
 // not fit one co-resident band per CTA on this device.
 bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* rows, size_t* smem);
 
-// Exchange words (unsigned long long) that `bands` bands of nth points need per direction.
-inline size_t exchange_words(uint32_t bands, uint32_t nth) { return (size_t)bands * nth * 2; }
+// Exchange words (unsigned long long) of each direction for `bands` bands of nth points.
+inline size_t down_words(uint32_t bands, uint32_t nth) { return (size_t)bands * 2 * (2 * (size_t)nth - 1) * 2; }
+inline size_t up_words(uint32_t bands, uint32_t nth) { return (size_t)bands * 2 * nth * 2; }
 
 // nsteps leapfrog steps of the rank-1 FOM in one cooperative launch on stream s.
 int launch(const Args& a, uint32_t bands, size_t smem, cudaStream_t s);

@@ -43,11 +43,12 @@ def generated(shaw, oracle, nth, nr):
     return m, om, dt
 
 
-def run(shaw, m, sched, src, rcv, dt, n, kind="ricker", period=None, delay=None, pieces=None, repeat=False):
+def run(shaw, m, sched, src, rcv, dt, n, kind="ricker", period=None, delay=None, pieces=None, repeat=False,
+        freq=1):
     f = shaw.Fom(m, 1, 1)
     f.set_schedule(sched)
     f.set_sources([src], kind, period, delay)
-    f.set_receivers(rcv, 1, n)
+    f.set_receivers(rcv, freq, n)
     for _ in range(2 if repeat else 1):
         if pieces:
             f.reset()
@@ -96,6 +97,12 @@ def test_persistent_runs_in_pieces_repeats_and_fixture(shaw, oracle):
     for x in (parts, again, two):
         assert np.array_equal(whole[0][0], x[0][0]) and np.array_equal(whole[0][1], x[0][1])
         assert np.array_equal(whole[1], x[1])
+    # sampling every third step, with pieces that start at every sampling phase
+    for pieces in ((1, 63, 64, 22), (2, 103, 45)):
+        a = run(shaw, m, shaw.SCHEDULE_PERSISTENT, *args, pieces=pieces, freq=3)
+        b = run(shaw, m, shaw.SCHEDULE_TWO_PASS, *args, pieces=pieces, freq=3)
+        assert np.array_equal(a[0][0], b[0][0]) and np.array_equal(a[0][1], b[0][1])
+        assert np.array_equal(a[1], b[1]) and np.max(np.abs(a[1])) > 0
 
 
 def test_persistent_schedule_errors(shaw, oracle):
