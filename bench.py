@@ -360,19 +360,27 @@ def extra_workloads(np, torch, shaw):
     b = forcing_vectors(k, [mesh.map_source(depth, 0.0)])[:, 0]
     rows = np.ascontiguousarray(basis["phi_v"][rcv, :k])
     res = {}
-    for prec in (shaw.FP64, shaw.MIXED_FP32):
+    # FP64 on its default launch (row bands over the SMs), FP64 on the 16-CTA cluster, mixed
+    for key, prec, sched in (("fp64", shaw.FP64, shaw.ROM_SCHEDULE_AUTO),
+                             ("fp64_cluster", shaw.FP64, shaw.ROM_SCHEDULE_CLUSTER),
+                             ("mixed", shaw.MIXED_FP32, shaw.ROM_SCHEDULE_AUTO)):
         r = shaw.Rom(av, as_, b, rank=1, precision=prec)
+        r.set_schedule(sched)
         r.set_signals("gaussDer", period, 180.0)
         r.set_receivers(rows, 1, n)
         r.reset()
         t = _timed(torch, r.stream, lambda: r.advance(dt, n))
         r.synchronize()
-        res[prec] = (t, r.seismogram(), r.get_state())
+        res[key] = (t, r.seismogram().copy(), r.get_state())
         r.close()
+    assert np.array_equal(res["fp64"][1], res["fp64_cluster"][1])  # the same row arithmetic
+    res[shaw.FP64], res[shaw.MIXED_FP32] = res["fp64"], res["mixed"]
     ref = oracle_lib.rom_run(av, as_, b.reshape(k, 1), n, dt, [2], [period], [180.0], freq_vp=1)
     ref_seis = np.einsum("rk,kt->rt", rows, ref["snaps_vp"][:, :, 0])[:, :, None]
     out["rom_rank1_k256"] = {"metric": "ROM forcing-steps/s", "steps": n,
                              "fp64": n / res[shaw.FP64][0], "mixed_fp32": n / res[shaw.MIXED_FP32][0],
+                             "fp64_launch": "row bands over the SMs, new rows gathered through L2 (the default)",
+                             "fp64_cluster": n / res["fp64_cluster"][0],
                              "speedup": res[shaw.FP64][0] / res[shaw.MIXED_FP32][0],
                              "seismogram_rel_err": _relerr(np, res[shaw.MIXED_FP32][1], res[shaw.FP64][1]),
                              "seismogram_max_abs": float(np.max(np.abs(res[shaw.FP64][1]))),

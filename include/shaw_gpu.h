@@ -253,6 +253,16 @@ int shaw_rom_set_receivers(shaw_rom_t h, const double* phi_rows, uint32_t num_re
                            uint64_t nsteps);
 int shaw_rom_run(shaw_rom_t h, double dt, uint64_t nsteps);
 int shaw_rom_reset(shaw_rom_t h);
+/* The launch of a rank-1 FP64 handle (bit-identical results either way):
+ * SHAW_ROM_SCHEDULE_CLUSTER one thread-block cluster of up to 16 CTAs, the new rows
+ * exchanged through distributed shared memory; SHAW_ROM_SCHEDULE_BANDS one cooperative
+ * launch of a few rows per CTA over up to every SM, the new rows gathered through L2 as
+ * tagged words (at most 1024 modes per dof).  AUTO (the default) takes the bands when
+ * they fit.  Other handles accept AUTO only. */
+#define SHAW_ROM_SCHEDULE_AUTO            0
+#define SHAW_ROM_SCHEDULE_CLUSTER         1
+#define SHAW_ROM_SCHEDULE_BANDS           2
+int shaw_rom_set_schedule(shaw_rom_t h, int schedule);
 int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps);
 int shaw_rom_synchronize(shaw_rom_t h);
 /* States out: xv kv x M, xs ks x M (LayoutLeft). */

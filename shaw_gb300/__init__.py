@@ -42,6 +42,7 @@ MATERIAL = {"unilayer": 0, "bilayer": 1, "prem": 2}
 # MIXED_TF32X3 is experimental: it does not meet the 1e-6 mixed-precision bar (see the C header).
 FP64, MIXED_TF32X3, MIXED_FP32, MIXED_OZAKI_BF16, OZAKI_FP64 = 0, 1, 3, 4, 5
 SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP, SCHEDULE_PERSISTENT = 0, 1, 2, 3
+ROM_SCHEDULE_AUTO, ROM_SCHEDULE_CLUSTER, ROM_SCHEDULE_BANDS = 0, 1, 2
 
 
 class ShawError(RuntimeError):
@@ -124,6 +125,7 @@ SIGNATURES = [
     ("shaw_rom_set_receivers", ctypes.c_int, [_vp, _dp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64]),
     ("shaw_rom_run", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     ("shaw_rom_reset", ctypes.c_int, [_vp]),
+    ("shaw_rom_set_schedule", ctypes.c_int, [_vp, ctypes.c_int]),
     ("shaw_rom_advance", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     ("shaw_rom_synchronize", ctypes.c_int, [_vp]),
     ("shaw_rom_get_state", ctypes.c_int, [_vp, _dp, _dp]),
@@ -557,6 +559,10 @@ class Rom:
 
     def reset(self):
         _check(lib().shaw_rom_reset(self.h))
+
+    def set_schedule(self, schedule):
+        """ROM_SCHEDULE_AUTO, ROM_SCHEDULE_CLUSTER or ROM_SCHEDULE_BANDS (see shaw_rom_set_schedule)."""
+        _check(lib().shaw_rom_set_schedule(self.h, schedule))
 
     def advance(self, dt, nsteps):
         _check(lib().shaw_rom_advance(self.h, dt, nsteps))

@@ -37,6 +37,7 @@
 #include <cstring>
 
 #include "fom_band.h"
+#include "l2_exchange.cuh"
 #include "shaw_internal.h"
 
 namespace shaw {
@@ -44,7 +45,6 @@ namespace band {
 
 constexpr uint32_t kThreads = 512;
 constexpr int kBatch = 2;                      // elements of a set per thread, processed side by side
-constexpr uint32_t kPollLimit = 1u << 22;      // polling rounds before a wait gives up (about a second)
 
 // Doubles of shared memory a CTA with `rows` rows needs.
 inline size_t smem_doubles(uint32_t nth, uint32_t rows) {
@@ -54,15 +54,6 @@ inline size_t smem_doubles(uint32_t nth, uint32_t rows) {
 
 namespace {
 
-// One point of a halo row: two words (tag | high half, tag | low half), one 16-byte store.
-// The vector access is two 8-byte accesses, each single-copy atomic; each is validated alone.
-__device__ __forceinline__ void put(unsigned long long* w, uint32_t tag, double v) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-  const unsigned long long t = (unsigned long long)tag << 32;
-  asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(w), "l"(t | (u >> 32)),
-               "l"(t | (u & 0xffffffffull))
-               : "memory");
-}
 // The forcing increments of the steps of a launch: ftab[s] = (dt rhoInv[src]) f(t) at
 // t = (step0 + s) dt, rounded as KokkosBlas::mult(1, x, dt, rhoInv, f) forms them, so the
 // kernel adds each with one FP64 add (the same roundings as the half-step kernels).
@@ -115,7 +106,7 @@ __device__ __forceinline__ bool receive(const unsigned long long* recv_above, co
                                         uint32_t n_above, uint32_t n_recv, bool srp_above, uint32_t nth,
                                         uint32_t nrow, double* SRP, double* STP, uint32_t t, uint32_t nt) {
   const unsigned long long* src[kRecvMax];
-  double* dst[kRecvMax];
+  double* dst[kRecvMax];  // (both filled for the pending points only)
   uint32_t pending = 0;
 #pragma unroll
   for (int k = 0; k < kRecvMax; ++k) {
@@ -134,20 +125,7 @@ __device__ __forceinline__ bool receive(const unsigned long long* recv_above, co
       dst[k] = SRP + pb;
     }
   }
-  for (uint32_t round = 0; pending && round < kPollLimit; ++round) {
-    unsigned long long hi[kRecvMax], lo[kRecvMax];
-#pragma unroll
-    for (int k = 0; k < kRecvMax; ++k)
-      if (pending & (1u << k))
-        asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(hi[k]), "=l"(lo[k]) : "l"(src[k]) : "memory");
-#pragma unroll
-    for (int k = 0; k < kRecvMax; ++k)
-      if ((pending & (1u << k)) && (uint32_t)(hi[k] >> 32) == tag && (uint32_t)(lo[k] >> 32) == tag) {
-        *dst[k] = __longlong_as_double((long long)((hi[k] << 32) | (lo[k] & 0xffffffffull)));
-        pending &= ~(1u << k);
-      }
-  }
-  return pending == 0;
+  return l2x::poll<kRecvMax>(src, dst, pending, tag);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
@@ -339,8 +317,8 @@ __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
           y = fma(CST[ns + e], V[e + 1], y);  // east v(j0, i + 1)
           STP[e] = y;
         }
-        if (m & 2) put(su + 2 * (m >> 3), tag, y);
-        if (m & 4) put(sd + 2 * (m >> 3), tag, y);
+        if (m & 2) l2x::put(su + 2 * (m >> 3), tag, y);
+        if (m & 4) l2x::put(sd + 2 * (m >> 3), tag, y);
       }
     }
     // 3. while the rows travel: the other stp rows, the receivers, the next interior velocity

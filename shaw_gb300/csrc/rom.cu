@@ -28,6 +28,7 @@
 #include <string>
 #include <vector>
 
+#include "l2_exchange.cuh"
 #include "rom_oz.h"
 #include "rom_tc.h"
 #include "shaw_internal.h"
@@ -37,11 +38,11 @@ namespace cg = cooperative_groups;
 namespace {
 
 constexpr int kRomThreads = 256;
-constexpr int kRomWarps = kRomThreads / 32;
 // rank-1 cluster kernel: 16 warps, so that at k = 256 over 16 CTAs every warp owns one
 // velocity row and one stress row (no serial rows per warp on the latency-bound path)
 constexpr int kR1Threads = 512;
 constexpr int kR1Warps = kR1Threads / 32;
+constexpr uint64_t kR1MaxSteps = 1 << 16;  // leapfrog steps per rank-1 launch
 
 // ---- double-float (hi + lo FP32) arithmetic ------------------------------------
 struct df {
@@ -104,6 +105,11 @@ struct RomArgs {
   double* hist;                 // kv x (samples of this launch): XV on the seismogram's sample steps
   unsigned long long hist_t0;   // sample index of hist's first column
   unsigned int* error;          // set when an exchange wait runs out
+  // band kernel (FP64): each CTA's mailbox of tagged words, [CTA][2 slots][kv][2] and
+  // [CTA][2 slots][ks][2]
+  unsigned long long* xw_v;
+  unsigned long long* xw_s;
+  uint32_t tag0;  // tag of the launch's first step (>= 1); step it carries tag0 + it
 };
 
 // Dynamic shared memory of the rank-1 kernel, in elements of T (double or df):
@@ -211,6 +217,23 @@ struct Arith<true> {
   __device__ static void store_sample(double* p, T x) { *reinterpret_cast<df*>(p) = x; }
 };
 
+// The observers' sample steps, counted instead of divided (a 64-bit division per step and
+// thread sat on the latency-bound loop): at step n, `due` when n is a multiple of freq,
+// with `index` = n / freq - 1 - base.  Start with the launch's first step step0 + 1.
+struct SampleClock {
+  uint32_t freq, phase;
+  unsigned long long next;  // index of the next sample
+  __device__ SampleClock(uint32_t f, unsigned long long step0, unsigned long long base)
+      : freq(f), phase(f ? (uint32_t)(step0 % f) : 0), next(f ? step0 / f - base : 0) {}
+  // advance to the next step; true (and the sample index in *idx) on a sample step
+  __device__ __forceinline__ bool tick(unsigned long long* idx) {
+    if (!freq || ++phase != freq) return false;
+    phase = 0;
+    *idx = next++;
+    return true;
+  }
+};
+
 // One persistent launch for nsteps ROM rank-1 leapfrog steps (one cluster).
 template <bool MIXED>
 __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a) {
@@ -250,17 +273,17 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   cluster.sync();
 
   const T dtT = A::load(a.dt);
+  SampleClock clk_v(a.fvp, a.step0, 0), clk_s(a.fsp, a.step0, 0), clk_h(a.hist ? a.fseis : 0, a.step0, a.hist_t0);
   for (unsigned long long it = 0; it < a.nsteps; ++it) {
-    const unsigned long long n = a.step0 + it + 1;
     // rom_run_rank_one.hpp:118 fValDt = f(t_{n-1}) * dt, from the table filled before the launch
     // (RankOneForcing keeps the whole signal time series too: forcing_rank_one.hpp:169-178)
     const T fdt = static_cast<const T*>(a.fdt_t)[it];
     // sample steps of the observers, decided once per step
-    const bool snap_v = a.fvp && n % a.fvp == 0, snap_s = a.fsp && n % a.fsp == 0;
+    unsigned long long iv = 0, is = 0, ih = 0;
+    const bool snap_v = clk_v.tick(&iv), snap_s = clk_s.tick(&is);
     // the ROM seismogram S = PhiVp[gid_r, :] XV (main_reconstruct_seismo.cc:157-185) is one
     // GEMM kernel after the launch over the XV of the sample steps, kept here in hist
-    double* const hcol = a.hist && a.fseis && n % a.fseis == 0
-                             ? a.hist + (size_t)a.kv * (n / a.fseis - 1 - a.hist_t0) : nullptr;
+    double* const hcol = clk_h.tick(&ih) ? a.hist + (size_t)a.kv * ih : nullptr;
     const uint32_t cur = (uint32_t)(it & 1), nxt = cur ^ 1u, par = (uint32_t)((it >> 1) & 1);
     const T* const xvc = xvb + (size_t)cur * a.kv;
     const T* const xsc = xsb + (size_t)cur * a.ks;
@@ -275,7 +298,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
         x = A::axpy(x, fdt, bv[r - v0]);
         st_async8(peer_addr(smem_addr(xv + r), lane), bits8(x), peer_addr(smem_addr(&xbar[nxt]), lane));
         if (lane == 0 && snap_v)
-          a.snap_vp[r + (size_t)a.kv * (n / a.fvp - 1)] = A::value(x);
+          a.snap_vp[r + (size_t)a.kv * iv] = A::value(x);
         if (lane == 0 && hcol) A::store_sample(hcol + r, x);
       }
     }
@@ -292,7 +315,7 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
         const T x = A::update(xsc[r], y, dtT);
         st_async8(peer_addr(smem_addr(xs + r), lane), bits8(x), peer_addr(smem_addr(&xbar[2 + nxt]), lane));
         if (lane == 0 && snap_s)
-          a.snap_sp[r + (size_t)a.ks * (n / a.fsp - 1)] = A::value(x);
+          a.snap_sp[r + (size_t)a.ks * is] = A::value(x);
       }
     }
     ok = xbar_wait(&xbar[2 + nxt], par);
@@ -307,6 +330,111 @@ __global__ void __launch_bounds__(kR1Threads) rom_rank1_cluster_kernel(RomArgs a
   for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1Threads) a.xs[r] = A::value(xsf[r]);
   // no CTA leaves while a peer may still deliver rows into its shared memory
   cluster.sync();
+}
+
+// ---- FP64 rank 1 over many SMs: one cooperative launch of row bands ----------------
+//
+// The cluster kernel above keeps its 16 CTAs' FP64 pipes busy (a row dot is 8 dependent
+// FMAs and 5 shuffle adds per lane, ~64 cycles per warp FP64 instruction on a sub-
+// partition of GB300's narrow FP64 pipe).  Here a cooperative grid of up to one CTA per
+// SM runs the same steps with a few rows per CTA: CTA c owns velocity rows [c rv, ...)
+// and stress rows [c rs, ...), one warp per row (so four rows run on the four sub-
+// partitions side by side), and keeps full copies of both states.  After each half-step
+// every CTA writes its new rows as tagged words into every CTA's own mailbox and
+// gathers its mailbox through L2 (l2_exchange.cuh).  Private mailboxes keep the polls of
+// different CTAs on different lines: with one shared copy, every CTA polled the same
+// few lines and the writers' stores queued behind the polls (7.0 us per step at k = 256
+// against 5.7 for the cluster).  Two slots per state by step parity: a CTA overwrites
+// a slot of step n only after it has gathered step n - 1, which every CTA published after
+// it had gathered step n - 2 from that slot.  The row arithmetic (Arith<false>: the same warp
+// dot, update and forcing) is the cluster kernel's, so the results are bit-identical.
+// A row's own old value is read before the row is published, so the gather that
+// overwrites it cannot run ahead of that read; other rows of the state being gathered are
+// not read in that half-step.  Every wait is bounded (error bit 1 velocity, 2 stress).
+constexpr int kR1BandThreads = 256;
+constexpr int kR1BandWarps = kR1BandThreads / 32;
+constexpr int kR1BandRecv = 4;  // gathered points per thread: k <= 1024
+
+__device__ __forceinline__ bool gather_state(double* x, const unsigned long long* w, uint32_t k, uint32_t tag) {
+  const unsigned long long* src[kR1BandRecv];
+  double* dst[kR1BandRecv];
+  uint32_t pending = 0;
+#pragma unroll
+  for (int j = 0; j < kR1BandRecv; ++j) {
+    const uint32_t q = threadIdx.x + j * kR1BandThreads;
+    src[j] = nullptr;
+    dst[j] = nullptr;
+    if (q < k) {
+      src[j] = w + 2 * (size_t)q;
+      dst[j] = x + q;
+      pending |= 1u << j;
+    }
+  }
+  return shaw::l2x::poll<kR1BandRecv>(src, dst, pending, tag);
+}
+
+__global__ void __launch_bounds__(kR1BandThreads, 1) rom_rank1_band_kernel(RomArgs a) {
+  using A = Arith<false>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* const xv = reinterpret_cast<double*>(smem_raw);  // [kv]
+  double* const xs = xv + a.kv;                            // [ks]
+  double* const Av = xs + a.ks;                            // rows_v x ks
+  double* const As = Av + (size_t)a.rows_v * a.ks;         // rows_s x kv
+  double* const bv = As + (size_t)a.rows_s * a.kv;         // rows_v
+  const uint32_t c = blockIdx.x;
+  const uint32_t v0 = min(a.kv, c * a.rows_v), v1 = min(a.kv, v0 + a.rows_v);
+  const uint32_t s0 = min(a.ks, c * a.rows_s), s1 = min(a.ks, s0 + a.rows_s);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  for (uint32_t k = threadIdx.x; k < a.kv; k += kR1BandThreads) xv[k] = a.xv[k];
+  for (uint32_t k = threadIdx.x; k < a.ks; k += kR1BandThreads) xs[k] = a.xs[k];
+  for (size_t e = threadIdx.x; e < (size_t)(v1 - v0) * a.ks; e += kR1BandThreads) Av[e] = a.Av[(size_t)v0 * a.ks + e];
+  for (size_t e = threadIdx.x; e < (size_t)(s1 - s0) * a.kv; e += kR1BandThreads) As[e] = a.As[(size_t)s0 * a.kv + e];
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1BandThreads) bv[r - v0] = a.b[r];
+  __syncthreads();
+
+  const double dt = a.dt;
+  SampleClock clk_v(a.fvp, a.step0, 0), clk_s(a.fsp, a.step0, 0), clk_h(a.hist ? a.fseis : 0, a.step0, a.hist_t0);
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    const uint32_t tag = a.tag0 + (uint32_t)it;
+    const size_t slot = (size_t)(it & 1);
+    const double fdt = static_cast<const double*>(a.fdt_t)[it];  // rom_run_rank_one.hpp:118 fValDt
+    unsigned long long iv = 0, is = 0, ih = 0;
+    const bool snap_v = clk_v.tick(&iv), snap_s = clk_s.tick(&is);
+    double* const hcol = clk_h.tick(&ih) ? a.hist + (size_t)a.kv * ih : nullptr;
+    // 1. velocity rows of this CTA, written into every CTA's mailbox as they are formed
+    //    (every lane holds the row's sum and forms the same new value)
+    const uint32_t G = gridDim.x;
+    for (uint32_t r = v0 + warp; r < v1; r += kR1BandWarps) {
+      const double y = A::dot(Av + (size_t)(r - v0) * a.ks, xs, a.ks, lane);
+      double x = A::update(xv[r], y, dt);
+      x = A::axpy(x, fdt, bv[r - v0]);
+      for (uint32_t c = lane; c < G; c += 32) shaw::l2x::put(a.xw_v + ((2 * (size_t)c + slot) * a.kv + r) * 2, tag, x);
+      if (lane == 0) {
+        if (snap_v) a.snap_vp[r + (size_t)a.kv * iv] = x;
+        if (hcol) hcol[r] = x;
+      }
+    }
+    bool ok = gather_state(xv, a.xw_v + (2 * (size_t)blockIdx.x + slot) * a.kv * 2, a.kv, tag);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(a.error, 1u);
+      break;
+    }
+    // 2. stress rows of this CTA
+    for (uint32_t r = s0 + warp; r < s1; r += kR1BandWarps) {
+      const double y = A::dot(As + (size_t)(r - s0) * a.kv, xv, a.kv, lane);
+      const double x = A::update(xs[r], y, dt);
+      for (uint32_t c = lane; c < G; c += 32) shaw::l2x::put(a.xw_s + ((2 * (size_t)c + slot) * a.ks + r) * 2, tag, x);
+      if (lane == 0 && snap_s) a.snap_sp[r + (size_t)a.ks * is] = x;
+    }
+    ok = gather_state(xs, a.xw_s + (2 * (size_t)blockIdx.x + slot) * a.ks * 2, a.ks, tag);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(a.error, 2u);
+      break;
+    }
+  }
+  for (uint32_t r = v0 + threadIdx.x; r < v1; r += kR1BandThreads) a.xv[r] = xv[r];
+  for (uint32_t r = s0 + threadIdx.x; r < s1; r += kR1BandThreads) a.xs[r] = xs[r];
 }
 
 // FP64 -> FP32 hi + lo; in and out may be the same array (each element is read before
@@ -396,9 +524,14 @@ struct shaw_rom_s {
   double* hist = nullptr;  // rank-1: XV on the sample steps of a launch (seismogram GEMM input)
   size_t hist_cap = 0;
   unsigned int* r1_err = nullptr;  // rank-1 kernel: an exchange wait ran out
-  // rank-1 cluster launch shape
+  // rank-1 launch shape: cluster (rom_rank1_cluster_kernel) or bands (rom_rank1_band_kernel)
   uint32_t cluster = 1, rows_v = 0, rows_s = 0;
   size_t smem = 0;
+  bool band = false, band_ok = false, cluster_ok = false;  // band: the launch in use
+  uint32_t band_n = 0, band_rv = 0, band_rs = 0;
+  size_t band_smem = 0;
+  unsigned long long* xw = nullptr;  // band mailboxes: [CTA][2][kv][2] then [CTA][2][ks][2]
+  uint32_t band_tag = 0;             // last tag used in xw (0: cleared)
   uint64_t step = 0;
   uint64_t launches = 0;
 };
@@ -407,13 +540,55 @@ namespace {
 
 using RH = shaw_rom_s;
 
+// FP64 rank 1 on row bands: a few rows per CTA (one warp each), one CTA per SM at most;
+// every state gathered by 256 threads of at most four points.
+bool rank1_band_plan(RH* h, int sms, size_t budget) {
+  const uint64_t k = std::max(h->kv, h->ks);
+  if (k > (uint64_t)kR1BandRecv * kR1BandThreads || k < 2) return false;
+  // rows per CTA: measured at k = 128 .. 1024 (steps of 2000 with a 181-receiver seismogram),
+  // 4 rows per CTA up to k = 256 and 8 beyond were fastest: fewer CTAs write fewer mailboxes
+  // and stay on one die, more rows per CTA queue more warps on the FP64 pipe
+  uint64_t rpc = std::max<uint64_t>(4, (k + 63) / 64);
+  uint32_t g = 0, rv = 0, rs = 0;
+  size_t bytes = 0;
+  for (;; rpc = (rpc + 1) / 2) {
+    g = (uint32_t)std::max<uint64_t>(2, (k + rpc - 1) / rpc);
+    rv = (uint32_t)((h->kv + g - 1) / g);
+    rs = (uint32_t)((h->ks + g - 1) / g);
+    bytes = sizeof(double) * ((size_t)h->kv + h->ks + (size_t)rv * h->ks + (size_t)rs * h->kv + rv);
+    if (bytes <= budget || rpc == 1) break;
+  }
+  if (bytes > budget || g > (uint32_t)sms) return false;
+  if (cudaFuncSetAttribute(rom_rank1_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rom_rank1_band_kernel, kR1BandThreads, bytes) !=
+          cudaSuccess ||
+      (uint64_t)per_sm * sms < g) {
+    cudaGetLastError();
+    return false;
+  }
+  h->band_ok = true;
+  h->band_n = g;
+  h->band_rv = rv;
+  h->band_rs = rs;
+  h->band_smem = bytes;
+  return true;
+}
+
 template <bool MIXED>
 int rank1_configure(RH* h) {
   using T = typename Arith<MIXED>::T;
-  int dev = 0, maxOptin = 0;
+  int dev = 0, maxOptin = 0, sms = 0;
   SHAW_CUDA(cudaGetDevice(&dev));
   SHAW_CUDA(cudaDeviceGetAttribute(&maxOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  SHAW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const size_t budget = (size_t)maxOptin;
+  // FP64: row bands over the GPU when they fit (the default), else the cluster
+  if (!MIXED) h->band = rank1_band_plan(h, sms, budget);
   for (uint32_t c : {1u, 2u, 4u, 8u, 16u}) {
     const uint32_t rv = (uint32_t)((h->kv + c - 1) / c), rs = (uint32_t)((h->ks + c - 1) / c);
     const size_t bytes = rank1_smem_bytes<T>((uint32_t)h->kv, (uint32_t)h->ks, rv, rs);
@@ -423,9 +598,11 @@ int rank1_configure(RH* h) {
       // to 16 CTAs (the cluster exchange costs less than the extra rows per CTA)
       if (rv > 16 && c < 16) continue;
       h->cluster = c; h->rows_v = rv; h->rows_s = rs; h->smem = bytes;
+      h->cluster_ok = true;
       return SHAW_OK;
     }
   }
+  if (h->band_ok) return SHAW_OK;
   return shaw::fail(SHAW_ERR_UNSUPPORTED, "reduced operators too large for the on-chip rank-1 ROM kernel");
 }
 
@@ -475,6 +652,36 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
     a.hist_t0 = t0;
     a.fseis = (uint32_t)h->fseis;
   }
+  if (!MIXED && h->band) {
+    const size_t words = 4 * (size_t)h->band_n * ((size_t)h->kv + h->ks);  // a mailbox per CTA
+    if (!h->xw) {
+      SHAW_CUDA(cudaMalloc(&h->xw, words * sizeof(unsigned long long)));
+      SHAW_CUDA(cudaMemsetAsync(h->xw, 0, words * sizeof(unsigned long long), h->stream));
+      h->band_tag = 0;
+    }
+    if ((uint64_t)h->band_tag + nsteps >= 0xffffffffull) {  // tags would wrap: clear the words
+      SHAW_CUDA(cudaMemsetAsync(h->xw, 0, words * sizeof(unsigned long long), h->stream));
+      h->band_tag = 0;
+    }
+    a.xw_v = h->xw;
+    a.xw_s = h->xw + 4 * (size_t)h->band_n * h->kv;
+    a.tag0 = h->band_tag + 1;
+    a.rows_v = h->band_rv;
+    a.rows_s = h->band_rs;
+    cudaLaunchConfig_t cfg;
+    std::memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(h->band_n);
+    cfg.blockDim = dim3(kR1BandThreads);
+    cfg.dynamicSmemBytes = h->band_smem;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;  // every band co-resident, or the launch fails
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SHAW_CUDA(cudaLaunchKernelEx(&cfg, rom_rank1_band_kernel, a));
+    h->band_tag += (uint32_t)nsteps;
+  } else {
   auto kern = rom_rank1_cluster_kernel<MIXED>;
   SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem));
   if (h->cluster > 8) SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -492,6 +699,7 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+  }
   h->launches++;
   if (a.hist) {
     const size_t cnt = (size_t)h->kv * (t1 - t0);
@@ -625,7 +833,7 @@ void shaw_rom_destroy(shaw_rom_t h) {
     if (h->host_sp) cudaHostUnregister(h->host_sp);
   }
   void* bufs[] = {h->Av, h->As, h->b, h->xv, h->xs, h->kind, h->period, h->delay,
-                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->hist, h->r1_err};
+                  h->snap_vp, h->snap_sp, h->phi_rcv, h->seis, h->fdt, h->hist, h->r1_err, h->xw};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -737,6 +945,25 @@ int shaw_rom_reset(shaw_rom_t h) {
   return SHAW_OK;
 }
 
+int shaw_rom_set_schedule(shaw_rom_t h, int schedule) {
+  if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
+  if (schedule < SHAW_ROM_SCHEDULE_AUTO || schedule > SHAW_ROM_SCHEDULE_BANDS)
+    return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown ROM schedule");
+  if (schedule == SHAW_ROM_SCHEDULE_AUTO) {
+    if (h->rank == 1 && h->precision == SHAW_FP64) h->band = h->band_ok;
+    return SHAW_OK;
+  }
+  if (h->rank != 1 || h->precision != SHAW_FP64)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "ROM schedules other than AUTO apply to rank-1 FP64 handles");
+  if (schedule == SHAW_ROM_SCHEDULE_BANDS && !h->band_ok)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the row-band schedule needs at most 1024 modes per dof");
+  if (schedule == SHAW_ROM_SCHEDULE_CLUSTER && !h->cluster_ok)
+    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the reduced operators do not fit the cluster kernel");
+  SHAW_CUDA(cudaStreamSynchronize(h->stream));
+  h->band = schedule == SHAW_ROM_SCHEDULE_BANDS;
+  return SHAW_OK;
+}
+
 int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
   if (!(dt > 0.0) || !std::isfinite(dt)) return shaw::fail(SHAW_ERR_INVALID_ARG, "dt must be > 0");
@@ -747,10 +974,14 @@ int shaw_rom_advance(shaw_rom_t h, double dt, uint64_t nsteps) {
     return shaw::fail(SHAW_ERR_INVALID_ARG, "advancing past the step count the snapshots were sized for");
   if (nsteps == 0) return SHAW_OK;
   int rc = SHAW_OK;
-  if (h->rank == 1) {
-    rc = h->precision == SHAW_FP64 ? rank1_launch<false>(h, dt, nsteps) : rank1_launch<true>(h, dt, nsteps);
-    if (rc) return rc;
-    h->step += nsteps;
+  if (h->rank == 1) {  // launches of at most kR1MaxSteps steps (bounded forcing table and history)
+    for (uint64_t done = 0; done < nsteps;) {
+      const uint64_t k = std::min<uint64_t>(kR1MaxSteps, nsteps - done);
+      rc = h->precision == SHAW_FP64 ? rank1_launch<false>(h, dt, k) : rank1_launch<true>(h, dt, k);
+      if (rc) return rc;
+      h->step += k;
+      done += k;
+    }
     return SHAW_OK;
   }
   if (h->tc || h->oz) {
@@ -781,7 +1012,7 @@ int shaw_rom_synchronize(shaw_rom_t h) {
     unsigned int err = 0;
     SHAW_CUDA(cudaMemcpy(&err, h->r1_err, sizeof(err), cudaMemcpyDeviceToHost));
     if (err)
-      return shaw::fail(SHAW_ERR_CUDA, "rank-1 ROM kernel: a cluster exchange wait ran out (code " +
+      return shaw::fail(SHAW_ERR_CUDA, "rank-1 ROM kernel: a row exchange wait ran out (code " +
                                            std::to_string(err) + ")");
   }
   if (h->rank == 1 && h->fvp) {

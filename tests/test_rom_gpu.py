@@ -350,3 +350,80 @@ def test_rank2_ozaki_fp64_advance_in_pieces(shaw):
     part = r.get_state()
     assert np.array_equal(whole[0], part[0]) and np.array_equal(whole[1], part[1])
     r.close()
+
+
+def _bounded_pair(kv, ks, seed):
+    """Av (kv x ks) with As = -Av^T (ks x kv): a symplectic, bounded rank-1 leapfrog at dt 0.5."""
+    rng = np.random.default_rng(seed)
+    av = rng.standard_normal((kv, ks)) * (0.5 / np.sqrt(max(kv, ks)))
+    return av, -av.T.copy(), rng.standard_normal(kv) * 1e-3, rng.standard_normal((7, kv)) / np.sqrt(kv)
+
+
+@pytest.mark.parametrize("kv,ks", [(32, 32), (256, 256), (200, 256), (513, 384)])
+def test_rank1_bands_equal_cluster(shaw, kv, ks):
+    """The row-band launch (the FP64 default) and the cluster launch run the same row
+    arithmetic, so states, snapshots and seismograms agree bit for bit, also when the run
+    is advanced in uneven pieces (each piece a launch with new exchange tags)."""
+    av, as_, b, rows = _bounded_pair(kv, ks, kv + ks)
+    n = 400
+    out = {}
+    for sched in (shaw.ROM_SCHEDULE_CLUSTER, shaw.ROM_SCHEDULE_BANDS):
+        r = shaw.Rom(av, as_, b, rank=1)
+        r.set_schedule(sched)
+        r.set_signals("ricker", 40.0, 10.0)
+        r.set_snapshots(4, 4, n)
+        r.set_receivers(rows, 2, n)
+        r.run(0.5, n)
+        whole = (r.get_state(), tuple(x.copy() for x in r.snapshots()), r.seismogram().copy())
+        r.reset()
+        for m in (1, 150, 249):
+            r.advance(0.5, m)
+        r.synchronize()
+        parts = (r.get_state(), tuple(x.copy() for x in r.snapshots()), r.seismogram().copy())
+        r.close()
+        for x, y in zip(whole[0] + whole[1] + (whole[2],), parts[0] + parts[1] + (parts[2],)):
+            assert np.array_equal(x, y)
+        out[sched] = whole
+    a, c = out[shaw.ROM_SCHEDULE_BANDS], out[shaw.ROM_SCHEDULE_CLUSTER]
+    for x, y in zip(a[0] + a[1] + (a[2],), c[0] + c[1] + (c[2],)):
+        assert np.array_equal(x, y)
+    assert np.max(np.abs(a[2])) > 0
+
+
+def test_rank1_bands_1024_modes_match_oracle(shaw, oracle):
+    """1024 modes per dof: the operators no longer fit a 16-CTA cluster; the row bands run
+    them (one CTA per SM, seven rows each on 152 SMs) within 1e-12 of the oracle."""
+    k, n, dt = 1024, 300, 0.5
+    av, as_, b, rows = _bounded_pair(k, k, 99)
+    r = shaw.Rom(av, as_, b, rank=1)
+    r.set_signals("gaussDer", 30.0, 20.0)
+    r.set_snapshots(10, 10, n)
+    r.run(dt, n)
+    ref = oracle.rom_run(av, as_, b.reshape(-1, 1), n, dt, [2], [30.0], [20.0], 10, 10)
+    xv, xs = r.get_state()
+    assert relerr(xv, ref["final_vp"]) <= 1e-12 and relerr(xs, ref["final_sp"]) <= 1e-12
+    svp, ssp = r.snapshots()
+    assert relerr(svp, ref["snaps_vp"]) <= 1e-12 and relerr(ssp, ref["snaps_sp"]) <= 1e-12
+    with pytest.raises(shaw.ShawError) as e:
+        r.set_schedule(shaw.ROM_SCHEDULE_CLUSTER)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    r.close()
+
+
+def test_rom_schedule_errors(shaw):
+    av, as_, b, _ = _bounded_pair(64, 64, 3)
+    r = shaw.Rom(av, as_, b, rank=1, precision=shaw.MIXED_FP32)
+    r.set_schedule(shaw.ROM_SCHEDULE_AUTO)
+    for sched in (shaw.ROM_SCHEDULE_CLUSTER, shaw.ROM_SCHEDULE_BANDS):
+        with pytest.raises(shaw.ShawError) as e:
+            r.set_schedule(sched)
+        assert e.value.code == shaw.ERR_UNSUPPORTED
+    r.close()
+    r = shaw.Rom(av, as_, np.column_stack([b, b]), rank=2)
+    with pytest.raises(shaw.ShawError) as e:
+        r.set_schedule(shaw.ROM_SCHEDULE_BANDS)
+    assert e.value.code == shaw.ERR_UNSUPPORTED
+    with pytest.raises(shaw.ShawError) as e:
+        r.set_schedule(7)
+    assert e.value.code == shaw.ERR_INVALID_ARG
+    r.close()
