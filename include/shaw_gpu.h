@@ -172,13 +172,6 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
 #define SHAW_FOM_SCHEDULE_AUTO            0
 #define SHAW_FOM_SCHEDULE_TWO_PASS        1
 #define SHAW_FOM_SCHEDULE_SWEEP           2
-#define SHAW_FOM_SCHEDULE_SWEEP_SPLIT     4  /* FP64, forcing columns a multiple of 64: the
-                                              * single sweep with the forcing columns split
-                                              * between the FP64 pipe (FMAs) and the integer
-                                              * pipes (each update v + sum c x formed exactly
-                                              * in 64-bit integers from the significands'
-                                              * products and rounded once: within 0.5 ulp +
-                                              * 2^-56 of exact, not bit-identical to FMAs). */
 #define SHAW_FOM_SCHEDULE_PERSISTENT      3  /* rank 1, FP64, small grids: all the steps of a
                                               * call in one cooperative launch (one CTA per SM,
                                               * each a band of r rows in shared memory, halo

@@ -41,7 +41,7 @@ SIGNAL = {"ricker": 0, "sinusoid": 1, "gaussDer": 2}
 MATERIAL = {"unilayer": 0, "bilayer": 1, "prem": 2}
 # MIXED_TF32X3 is experimental: it does not meet the 1e-6 mixed-precision bar (see the C header).
 FP64, MIXED_TF32X3, MIXED_FP32, MIXED_OZAKI_BF16, OZAKI_FP64 = 0, 1, 3, 4, 5
-SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP, SCHEDULE_PERSISTENT, SCHEDULE_SWEEP_SPLIT = 0, 1, 2, 3, 4
+SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP, SCHEDULE_PERSISTENT = 0, 1, 2, 3
 ROM_SCHEDULE_AUTO, ROM_SCHEDULE_CLUSTER, ROM_SCHEDULE_BANDS = 0, 1, 2
 
 
@@ -353,8 +353,7 @@ class Fom:
         _check(lib().shaw_fom_set_state(self.h, _p(vp, _dp), _p(sp, _dp)))
 
     def set_schedule(self, schedule):
-        """SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP, SCHEDULE_PERSISTENT or SCHEDULE_SWEEP_SPLIT
-        (see shaw_fom_set_schedule)."""
+        """SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_SWEEP or SCHEDULE_PERSISTENT (see shaw_fom_set_schedule)."""
         _check(lib().shaw_fom_set_schedule(self.h, schedule))
 
     @property

@@ -548,7 +548,7 @@ int ensure_folded(H* h, double dt) {
   }
   h->launches += 2;
   if (h->sweep) {
-    if (h->form != sweep::kF32) {
+    if (h->form == sweep::kF64) {
       fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->cvp_raw, (double*)h->cv4, dt, h->nvp, 4, 0);
       fom_fold_aos_kernel<double><<<1024, 256, 0, h->stream>>>(h->csp_raw, (double*)h->cs2, dt, h->nsp, 2, 1);
     } else {
@@ -1304,12 +1304,10 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp) {
 
 int shaw_fom_set_schedule(shaw_fom_t h, int schedule) {
   if (!h) return shaw::fail(SHAW_ERR_INVALID_ARG, "null handle");
-  if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_SWEEP_SPLIT)
+  if (schedule < SHAW_FOM_SCHEDULE_AUTO || schedule > SHAW_FOM_SCHEDULE_PERSISTENT)
     return shaw::fail(SHAW_ERR_INVALID_ARG, "unknown FOM schedule");
   if (schedule == SHAW_FOM_SCHEDULE_SWEEP && !h->sweep_ok)
     return shaw::fail(SHAW_ERR_UNSUPPORTED, "the single sweep needs a multiple of 32 forcing columns");
-  if (schedule == SHAW_FOM_SCHEDULE_SWEEP_SPLIT && (!h->sweep_ok || h->precision != SHAW_FP64 || h->M % 64 != 0))
-    return shaw::fail(SHAW_ERR_UNSUPPORTED, "the split sweep needs an FP64 handle with a multiple of 64 forcing columns");
   if (schedule == SHAW_FOM_SCHEDULE_PERSISTENT && !h->band_ok)
     return shaw::fail(SHAW_ERR_UNSUPPORTED,
                       "the persistent schedule needs a rank-1 FP64 handle on a grid of at least two r rows "
@@ -1317,13 +1315,7 @@ int shaw_fom_set_schedule(shaw_fom_t h, int schedule) {
   SHAW_CUDA(cudaStreamSynchronize(h->stream));
   drop_graphs(h);
   h->folded_dt = std::nan("");  // fold the stencil values of the new form on the next step
-  h->sweep = schedule == SHAW_FOM_SCHEDULE_AUTO ? auto_sweep(h)
-                                                : (schedule == SHAW_FOM_SCHEDULE_SWEEP ||
-                                                   schedule == SHAW_FOM_SCHEDULE_SWEEP_SPLIT);
-  if (h->sweep_ok)
-    h->form = h->precision == SHAW_MIXED_FP32                   ? sweep::kF32
-              : schedule == SHAW_FOM_SCHEDULE_SWEEP_SPLIT ? sweep::kF64Split
-                                                           : sweep::kF64;
+  h->sweep = schedule == SHAW_FOM_SCHEDULE_AUTO ? auto_sweep(h) : schedule == SHAW_FOM_SCHEDULE_SWEEP;
   h->use_band = schedule == SHAW_FOM_SCHEDULE_AUTO ? h->band_ok : schedule == SHAW_FOM_SCHEDULE_PERSISTENT;
   return SHAW_OK;
 }

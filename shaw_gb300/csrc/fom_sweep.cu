@@ -33,7 +33,6 @@
 // Every wait is bounded: a wait that runs out sets ctl->error bit 1 and the CTA stops
 // issuing copies; before it exits it waits (bounded again) for the copies it issued.
 #include "fom_sweep.h"
-#include "fdot.cuh"
 
 #include <cudaTypedefs.h>
 
@@ -65,13 +64,6 @@ struct FT<kF64> {
   using V = double;   // v_new as kept for the stress half-step
 };
 template <>
-struct FT<kF64Split> {
-  using S = double;
-  using CV = double;
-  using CS = double;
-  using V = double;
-};
-template <>
 struct FT<kF32> {
   using S = float;
   using CV = float;
@@ -87,52 +79,28 @@ struct Arith;
 template <>
 struct Arith<kF64> {
   __device__ static double vel(double v, double cN, double sN, double cS, double sS, double cW, double sW, double cE,
-                               double sE, int) {
+                               double sE) {
     v = fma(cN, sN, v);
     v = fma(cS, sS, v);
     v = fma(cW, sW, v);
     return fma(cE, sE, v);
   }
-  __device__ static double str(double s, double cA, double vA, double cB, double vB, int) {
+  __device__ static double str(double s, double cA, double vA, double cB, double vB) {
     s = fma(cA, vA, s);
     return fma(cB, vB, s);
-  }
-};
-
-// Even columns on the FP64 pipe (the FMA chain), odd columns on the integer pipes (a fused
-// dot rounded once; the FMA chain again where it reports a non-finite input or a result
-// outside the normal range).  The column index is a constant of the unrolled column loop.
-template <>
-struct Arith<kF64Split> {
-  __device__ static double vel(double v, double cN, double sN, double cS, double sS, double cW, double sW, double cE,
-                               double sE, int c) {
-    if (c & 1) {
-      bool bad = false;
-      const double r = fd::vel(v, cN, sN, cS, sS, cW, sW, cE, sE, &bad);
-      if (!bad) return r;
-    }
-    return Arith<kF64>::vel(v, cN, sN, cS, sS, cW, sW, cE, sE, c);
-  }
-  __device__ static double str(double s, double cA, double vA, double cB, double vB, int c) {
-    if (c & 1) {
-      bool bad = false;
-      const double r = fd::str(s, cA, vA, cB, vB, &bad);
-      if (!bad) return r;
-    }
-    return Arith<kF64>::str(s, cA, vA, cB, vB, c);
   }
 };
 
 template <>
 struct Arith<kF32> {
   __device__ static float vel(float v, float cN, float sN, float cS, float sS, float cW, float sW, float cE,
-                              float sE, int) {
+                              float sE) {
     v = fmaf(cN, sN, v);
     v = fmaf(cS, sS, v);
     v = fmaf(cW, sW, v);
     return fmaf(cE, sE, v);
   }
-  __device__ static float str(float s, float cA, float vA, float cB, float vB, int) {
+  __device__ static float str(float s, float cA, float vA, float cB, float vB) {
     s = fmaf(cA, vA, s);
     return fmaf(cB, vB, s);
   }
@@ -419,7 +387,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
             const S oN = last ? oS : rawN.x[c];
             const S oW = have_e ? eW[c] : rawW.x[c];
             const S oE = rawE.x[c];
-            v.x[c] = A::vel(v.x[c], cN, oN, cS, oS, cW, oW, cE, oE, c);
+            v.x[c] = A::vel(v.x[c], cN, oN, cS, oS, cW, oW, cE, oE);
             carry[q][c] = oN;
             eW[c] = oE;
           }
@@ -455,7 +423,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
           const CS cA = csq[srp_off(li)][0], cB = csq[srp_off(li)][1];
           const VV a = vn[li * VS], bb = vo[li * VS];
 #pragma unroll
-          for (int c = 0; c < VEC; ++c) sg.x[c] = A::str(sg.x[c], cA, a.x[c], cB, bb.x[c], c);
+          for (int c = 0; c < VEC; ++c) sg.x[c] = A::str(sg.x[c], cA, a.x[c], cB, bb.x[c]);
           stv<S, VEC>(xs_new + g * M + col, sg);
         }
         if (i + 1 < nth) {  // stp(rq, i)
@@ -463,7 +431,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
           const CS cA = csq[stp_off((int)li, false)][0], cB = csq[stp_off((int)li, false)][1];
           const VV a = vo[li * VS], bb = vo[(li + 1) * VS];
 #pragma unroll
-          for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c], c);
+          for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c]);
           stv<S, VEC>(xs_new + (g + 1) * M + col, su);
         }
       }
@@ -483,7 +451,7 @@ __global__ void __launch_bounds__(kBlock, 2) fom_sweep_kernel(const __grid_const
         const CS cA = csc[stp_off((int)li, true)][0], cB = csc[stp_off((int)li, true)][1];
         const VV a = vn[li * VS], bb = vn[(li + 1) * VS];
 #pragma unroll
-        for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c], c);
+        for (int c = 0; c < VEC; ++c) su.x[c] = A::str(su.x[c], cA, a.x[c], cB, bb.x[c]);
         stv<S, VEC>(xs_new + g * M + col, su);
       }
     }
@@ -591,9 +559,6 @@ int launch(Form f, const CUtensorMap& tv, const CUtensorMap& ts, const Params& p
     case kF64:
       return p.vec == 2 ? launch_t<kF64, 2>(tv, ts, p, k_local, host_step, s, pdl)
                         : launch_t<kF64, 1>(tv, ts, p, k_local, host_step, s, pdl);
-    case kF64Split:  // two columns per lane (the handle checks M % 64 == 0)
-      if (p.vec != 2) return shaw::fail(SHAW_ERR_UNSUPPORTED, "the split sweep needs two columns per lane");
-      return launch_t<kF64Split, 2>(tv, ts, p, k_local, host_step, s, pdl);
     default:
       return p.vec == 4   ? launch_t<kF32, 4>(tv, ts, p, k_local, host_step, s, pdl)
              : p.vec == 2 ? launch_t<kF32, 2>(tv, ts, p, k_local, host_step, s, pdl)
@@ -604,7 +569,7 @@ int launch(Form f, const CUtensorMap& tv, const CUtensorMap& ts, const Params& p
 int launch_gather(Form f, const Params& p, const void* xv, unsigned long long step, cudaStream_t s) {
   if (!p.R || !p.seis_freq) return SHAW_OK;
   const uint32_t blocks = (p.R * p.M + 255) / 256;
-  if (f == kF32) fom_gather_kernel<kF32><<<blocks, 256, 0, s>>>(p, xv, step);  // FP64 state otherwise
+  if (f == kF32) fom_gather_kernel<kF32><<<blocks, 256, 0, s>>>(p, xv, step);
   else fom_gather_kernel<kF64><<<blocks, 256, 0, s>>>(p, xv, step);
   SHAW_CUDA(cudaGetLastError());
   return SHAW_OK;

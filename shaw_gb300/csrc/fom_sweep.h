@@ -18,10 +18,8 @@ struct FomCtl {
 namespace sweep {
 
 // Arithmetic of one sweep: FP64 state and FP64 FMAs (kF64, the two-pass kernels'
-// arithmetic in one sweep), FP32 state and FP32 FMAs (kF32), or FP64 state with the
-// forcing columns split between the FP64 pipe (FMAs, even columns) and the integer pipes
-// (fused dots rounded once, fdot.cuh; odd columns) -- kF64Split, two columns per lane.
-enum Form { kF64 = 0, kF32 = 1, kF64Split = 2 };
+// arithmetic in one sweep) or FP32 state and FP32 FMAs (kF32).
+enum Form { kF64 = 0, kF32 = 1 };
 
 constexpr uint32_t kTI = 16;               // vp points per strip (theta)
 constexpr uint32_t kTM = 32;               // forcing columns per tile at one column per lane

@@ -4,9 +4,6 @@ state buffers) against the oracle and against the two half-step kernels.
   * SHAW_FP64: 1e-12 relative to the oracle (max |gpu - oracle| / max |oracle| per array).
   * SHAW_FP64 and SHAW_MIXED_FP32: the same FMAs in the same order as the two half-step
     kernels, so the states and seismograms are bit-identical to theirs.
-  * SHAW_FOM_SCHEDULE_SWEEP_SPLIT (FP64): even forcing columns on the FMA chain (bit-identical
-    to the half-step kernels), odd columns as integer fused dots rounded once (1e-12 from the
-    oracle, also where the seismogram is nothing but tiny precursors).
 Grids cover partial theta strips (nth not a multiple of 16, a strip holding only the
 axis point), several r segments, a segment starting on the surface row, sources on the
 axis, the CMB and the surface, corner receivers, runs in pieces with odd step counts
@@ -53,8 +50,8 @@ GRIDS = [(51, 21), (17, 40), (100, 201), (37, 33)]
 
 
 @pytest.mark.parametrize("nth,nr", GRIDS)
-@pytest.mark.parametrize("sched,M", [("sweep", 32), ("sweep", 64), ("split", 64), ("split", 128)])
-def test_sweep_fp64_matches_oracle(shaw, oracle, nth, nr, sched, M):
+@pytest.mark.parametrize("M", [32, 64])
+def test_sweep_fp64_matches_oracle(shaw, oracle, nth, nr, M):
     m, om, dt = grids(shaw, oracle, nth, nr)
     n = 150
     gids = sources(m, M, nth + nr)
@@ -64,7 +61,7 @@ def test_sweep_fp64_matches_oracle(shaw, oracle, nth, nr, sched, M):
     delays = list(rng.uniform(0.0, 20.0 * dt, M))
     rcv = [0, nth - 1, (nr - 1) * nth, m.nvp - 1] + gids[8:16]
     f = shaw.Fom(m, 2, M)
-    f.set_schedule(shaw.SCHEDULE_SWEEP if sched == "sweep" else shaw.SCHEDULE_SWEEP_SPLIT)
+    f.set_schedule(shaw.SCHEDULE_SWEEP)
     f.set_sources(gids, kinds, periods, delays)
     f.set_receivers(rcv, 1, n)
     f.run(dt, n)
@@ -143,57 +140,6 @@ def test_sweep_pieces_graphs_and_snapshots(shaw, oracle):
     f.close()
 
 
-@pytest.mark.parametrize("nth,nr", [(100, 201), (37, 33)])
-def test_split_sweep_even_columns_bitwise_odd_close(shaw, oracle, nth, nr):
-    """The split form's even columns run the two-pass kernels' FMA chain (bit-identical);
-    its odd columns are fused dots, within 1e-13 of the FMA chain over 140 steps."""
-    m, _, dt = grids(shaw, oracle, nth, nr)
-    M, n = 64, 140
-    gids = sources(m, M, 11 * nth)
-    periods = np.random.default_rng(nth).uniform(0.5, 3.0, M) * 40 * dt
-    rcv = [0, nth - 1, (nr - 1) * nth + 1, m.nvp - 1] + gids[:6]
-    out = []
-    for sched in (shaw.SCHEDULE_TWO_PASS, shaw.SCHEDULE_SWEEP_SPLIT):
-        f = shaw.Fom(m, 2, M)
-        f.set_schedule(sched)
-        f.set_sources(gids, "ricker", periods, 10 * dt)
-        f.set_receivers(rcv, 1, n)
-        f.run(dt, n)
-        out.append((f.get_state(), f.seismogram()))
-        f.close()
-    (a, sa), (b, sb) = out
-    for x, y in ((a[0], b[0]), (a[1], b[1]), (sa, sb)):
-        assert np.array_equal(x[..., 0::2], y[..., 0::2])
-        assert relerr(y[..., 1::2], x[..., 1::2]) <= 1e-13
-        assert not np.array_equal(x[..., 1::2], y[..., 1::2])  # the integer path did run
-    assert np.max(np.abs(sa)) > 0
-
-
-def test_split_sweep_tiny_seismogram(shaw, oracle):
-    """Sources near the CMB, receivers on the surface, few steps: the receivers see only
-    numerical precursors many orders of magnitude below the state's maximum.  Each fused
-    dot keeps FP64's relative precision, so even that seismogram meets 1e-12 against the
-    oracle (a fixed-point or FP32-pair form does not)."""
-    m, om, dt = grids(shaw, oracle, 100, 201)
-    M, n = 64, 260  # the stencil reaches one row further per step: the surface after ~200
-    rng = np.random.default_rng(5)
-    gids = [int(j) * 100 + int(i) for j, i in zip(rng.integers(1, 4, M), rng.integers(1, 99, M))]
-    periods = list(rng.uniform(0.5, 3.0, M) * 40 * dt)
-    rcv = [200 * 100 + i for i in range(0, 100, 3)]
-    f = shaw.Fom(m, 2, M)
-    f.set_schedule(shaw.SCHEDULE_SWEEP_SPLIT)
-    f.set_sources(gids, "ricker", periods, 5 * dt)
-    f.set_receivers(rcv, 1, n)
-    f.run(dt, n)
-    ref = om.fom_run(2, n, dt, gids, [0] * M, periods, [5 * dt] * M, rcv, 1, 0, 0)
-    vp, sp = f.get_state()
-    seis = f.seismogram()
-    assert 0 < np.max(np.abs(ref["seis"])) < 1e-30 * np.max(np.abs(ref["final_vp"]))
-    assert relerr(seis, ref["seis"]) <= RTOL
-    assert relerr(vp, ref["final_vp"]) <= RTOL and relerr(sp, ref["final_sp"]) <= RTOL
-    f.close()
-
-
 def test_sweep_schedule_errors(shaw, oracle):
     m, _, _ = grids(shaw, oracle, 51, 21)
     f = shaw.Fom(m, 2, 12)  # 12 columns: the two half-step kernels only
@@ -201,17 +147,8 @@ def test_sweep_schedule_errors(shaw, oracle):
         f.set_schedule(shaw.SCHEDULE_SWEEP)
     assert e.value.code == shaw.ERR_UNSUPPORTED
     with pytest.raises(shaw.ShawError) as e:
-        f.set_schedule(shaw.SCHEDULE_SWEEP_SPLIT)
-    assert e.value.code == shaw.ERR_UNSUPPORTED
-    with pytest.raises(shaw.ShawError) as e:
         f.set_schedule(7)
     assert e.value.code == shaw.ERR_INVALID_ARG
     f.set_schedule(shaw.SCHEDULE_TWO_PASS)
     f.set_schedule(shaw.SCHEDULE_AUTO)
     f.close()
-    for M, prec in ((32, shaw.FP64), (64, shaw.MIXED_FP32)):  # split: FP64 and 64-column multiples
-        g = shaw.Fom(m, 2, M, precision=prec)
-        with pytest.raises(shaw.ShawError) as e:
-            g.set_schedule(shaw.SCHEDULE_SWEEP_SPLIT)
-        assert e.value.code == shaw.ERR_UNSUPPORTED
-        g.close()
