@@ -155,7 +155,6 @@ int shaw_fom_get_seismogram(shaw_fom_t h, double* out);
 /* Copy the states out / in: vp nvp x M, sp nsp x M (LayoutLeft). */
 int shaw_fom_get_state(shaw_fom_t h, double* vp, double* sp);
 int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
-/* The handle's cudaStream_t, for callers that time with CUDA events. */
 /* Schedule of the FOM leapfrog (no counterpart in the reference, which always runs
  * its two CRS products per step, fom_update_kernels.hpp:60-181).
  *   SHAW_FOM_SCHEDULE_TWO_PASS: the two half-step kernels (in place).
@@ -163,23 +162,24 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
  *     reads and writes every state value once per step (16 B per FP64 DOF-update, 8 B per
  *     FP32 one) and alternates between two state buffers.  Same FMAs in the same order as
  *     the two-pass kernels: bit-identical results.
- *   SHAW_FOM_SCHEDULE_AUTO (the default): the faster of the two for the handle's precision
- *     on GB300: the sweep for SHAW_MIXED_FP32 (HBM-bound, when the column count allows
- *     it), the two-pass kernels for SHAW_FP64 (both schedules are bound by the FP64 pipe
- *     there, and the two-pass kernels keep it busier).
- * SHAW_FOM_SCHEDULE_SWEEP returns SHAW_ERR_UNSUPPORTED when the column count does not
- * allow it.  Synchronizes the handle's stream. */
+ *   SHAW_FOM_SCHEDULE_PERSISTENT: rank 1, FP64, small grids: all the steps of a call in
+ *     one cooperative launch (one CTA per SM, each a band of r rows in shared memory, halo
+ *     rows exchanged through L2 as tagged words); bit-identical to the two-pass kernels;
+ *     runs with snapshots keep the two-pass kernels.
+ *   SHAW_FOM_SCHEDULE_AUTO (the default): the fastest for the handle on GB300: the
+ *     persistent launch for rank-1 FP64 handles whose grid fits (at least two r rows,
+ *     (rows per band + 1) x nth <= 1024 points), the sweep for SHAW_MIXED_FP32 (HBM-bound,
+ *     when the column count allows it), otherwise the two-pass kernels (for FP64 both
+ *     the sweep and the two-pass kernels are bound by the FP64 pipe, and the two-pass
+ *     kernels keep it busier).
+ * SHAW_FOM_SCHEDULE_SWEEP and SHAW_FOM_SCHEDULE_PERSISTENT return SHAW_ERR_UNSUPPORTED
+ * when the handle does not allow them.  Synchronizes the handle's stream. */
 #define SHAW_FOM_SCHEDULE_AUTO            0
 #define SHAW_FOM_SCHEDULE_TWO_PASS        1
 #define SHAW_FOM_SCHEDULE_SWEEP           2
-#define SHAW_FOM_SCHEDULE_PERSISTENT      3  /* rank 1, FP64, small grids: all the steps of a
-                                              * call in one cooperative launch (one CTA per SM,
-                                              * each a band of r rows in shared memory, halo
-                                              * rows exchanged through L2 as tagged words);
-                                              * bit-identical to the two-pass kernels; not with
-                                              * snapshots.  AUTO takes it for rank-1 FP64
-                                              * handles whose grid fits. */
+#define SHAW_FOM_SCHEDULE_PERSISTENT      3
 int shaw_fom_set_schedule(shaw_fom_t h, int schedule);
+/* The handle's cudaStream_t, for callers that time with CUDA events. */
 void* shaw_fom_stream(shaw_fom_t h);
 /* Kernels this handle has launched since creation (graph replays count each node). */
 uint64_t shaw_fom_kernel_launches(shaw_fom_t h);
