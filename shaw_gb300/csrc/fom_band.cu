@@ -100,7 +100,7 @@ __device__ __forceinline__ void velocity(const VelSet& e, double* V, const doubl
 // first the message from above (srp(j1) when it exists, then stp(j1, .)), then srp(j0 - 1)
 // from below.  Each round issues the loads of all the thread's pending points before it
 // checks any, so their round trips overlap.
-constexpr int kRecvMax = 4;
+constexpr int kRecvMax = 3;  // received points per thread: 3 nth - 1 <= 3 kThreads for nth <= 512
 __device__ __forceinline__ bool receive(const unsigned long long* recv_above, const unsigned long long* recv_below,
                                         uint32_t slot, uint32_t tag, size_t down_pts, size_t up_pts,
                                         uint32_t n_above, uint32_t n_recv, bool srp_above, uint32_t nth,
