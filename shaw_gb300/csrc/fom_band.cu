@@ -419,6 +419,8 @@ bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* rows, size_t* sm
 int launch(const Args& a, uint32_t bands, size_t smem, cudaStream_t s) {
   fom_band_forcing_kernel<<<(unsigned)((a.nsteps + 255) / 256), 256, 0, s>>>(a);
   SHAW_CUDA(cudaGetLastError());
+  // per launch: another handle's plan may have set the kernel's limit for a smaller grid
+  SHAW_CUDA(cudaFuncSetAttribute(fom_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(bands);

@@ -668,6 +668,9 @@ int rank1_launch(RH* h, double dt, uint64_t nsteps) {
     a.tag0 = h->band_tag + 1;
     a.rows_v = h->band_rv;
     a.rows_s = h->band_rs;
+    // per launch: another handle's plan may have set the kernel's limit for fewer modes
+    SHAW_CUDA(cudaFuncSetAttribute(rom_rank1_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)h->band_smem));
     cudaLaunchConfig_t cfg;
     std::memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3(h->band_n);

@@ -125,3 +125,31 @@ def test_persistent_schedule_errors(shaw, oracle):
         h.set_schedule(shaw.SCHEDULE_PERSISTENT)
     assert e.value.code == shaw.ERR_UNSUPPORTED
     h.close()
+
+
+def test_persistent_handles_of_different_sizes(shaw, oracle):
+    """A handle planned for a wide grid (76 KB of shared memory per band) still launches
+    after a handle for a narrow grid (24 KB) was planned: the kernel's shared-memory limit
+    is set at every launch.  Both equal the two half-step kernels bit for bit."""
+    runs = {}
+    handles = []
+    for nth, nr in ((500, 21), (101, 201)):
+        m, _, dt = generated(shaw, oracle, nth, nr)
+        f = shaw.Fom(m, 1, 1)
+        f.set_schedule(shaw.SCHEDULE_PERSISTENT)
+        f.set_sources([(nr // 2) * nth + nth // 2], "ricker", 40 * dt, 10 * dt)
+        f.set_receivers([0, (nr - 1) * nth + 3], 1, 120)
+        handles.append((nth, nr, m, dt, f))
+    for nth, nr, m, dt, f in handles:  # the wide grid runs last-planned-second
+        f.run(dt, 120)
+        runs[(nth, nr)] = (f.get_state(), f.seismogram())
+        f.close()
+    for nth, nr, m, dt, _ in handles:
+        g = shaw.Fom(m, 1, 1)
+        g.set_schedule(shaw.SCHEDULE_TWO_PASS)
+        g.set_sources([(nr // 2) * nth + nth // 2], "ricker", 40 * dt, 10 * dt)
+        g.set_receivers([0, (nr - 1) * nth + 3], 1, 120)
+        g.run(dt, 120)
+        (a, sa), b, sb = runs[(nth, nr)], g.get_state(), g.seismogram()
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(sa, sb)
+        g.close()

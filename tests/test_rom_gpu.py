@@ -427,3 +427,24 @@ def test_rom_schedule_errors(shaw):
         r.set_schedule(7)
     assert e.value.code == shaw.ERR_INVALID_ARG
     r.close()
+
+
+def test_rank1_bands_handles_of_different_sizes(shaw):
+    """A 1024-mode band handle (its kernel's shared memory far above a 64-mode handle's)
+    still launches after the smaller handle was planned, and equals a run of its own."""
+    big = _bounded_pair(1024, 1024, 21)
+    small = _bounded_pair(64, 64, 22)
+    rb = shaw.Rom(big[0], big[1], big[2], rank=1)
+    rs = shaw.Rom(small[0], small[1], small[2], rank=1)
+    for r in (rb, rs):
+        r.set_signals("ricker", 40.0, 10.0)
+        r.run(0.5, 100)
+    xb = rb.get_state()
+    rb.close()
+    rs.close()
+    r = shaw.Rom(big[0], big[1], big[2], rank=1)
+    r.set_signals("ricker", 40.0, 10.0)
+    r.run(0.5, 100)
+    x = r.get_state()
+    assert np.array_equal(x[0], xb[0]) and np.array_equal(x[1], xb[1])
+    r.close()
