@@ -307,10 +307,11 @@ int shaw_rom_batch_set_tiling(shaw_rom_batch_t h, uint32_t width, int paired);
 /* Diagnostic of failure detection: every wait of the persistent kernels is bounded and
  * reports a timeout instead of hanging.  One small launch waits, with the same helpers,
  * on an mbarrier phase that nothing completes and on a global counter that nothing
- * increments, each for `polls` polls; *status receives the error bits they set (64 and
- * 128, the codes the ROM kernels report).  The device stays usable afterwards.
- * polls must be in 1 .. 16777216 (2^24, the kernels' own wait limit), else
- * SHAW_ERR_INVALID_ARG. */
+ * increments, each for `polls` polls, and on a tagged exchange word that nothing writes
+ * (the row exchange of the band kernels) for min(polls, 2^22) rounds; *status receives
+ * the bits they set (64, 128 -- the codes the ROM kernels report -- and 256).  The device
+ * stays usable afterwards.  polls must be in 1 .. 16777216 (2^24, the kernels' own wait
+ * limit), else SHAW_ERR_INVALID_ARG. */
 int shaw_selftest_bounded_waits(uint64_t polls, uint32_t* status);
 /* Reduced-state snapshots of instance i: kv x (nsteps/freq_vp) x M and
  * ks x (nsteps/freq_sp) x M LayoutLeft host arrays, filled by _synchronize. */

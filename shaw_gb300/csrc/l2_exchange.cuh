@@ -28,11 +28,11 @@ __device__ __forceinline__ void put(unsigned long long* w, uint32_t tag, double 
 
 // Bounded wait for the points src[k] (k with bit k of `pending` set) tagged `tag`, each
 // stored to *dst[k] as it arrives.  Every round issues the loads of all pending points
-// before it checks any, so their round trips overlap.  False when the limit ran out.
+// before it checks any, so their round trips overlap.  False when `limit` rounds ran out.
 template <int N>
 __device__ __forceinline__ bool poll(const unsigned long long* const (&src)[N], double* const (&dst)[N],
-                                     uint32_t pending, uint32_t tag) {
-  for (uint32_t round = 0; pending && round < kPollLimit; ++round) {
+                                     uint32_t pending, uint32_t tag, uint32_t limit = kPollLimit) {
+  for (uint32_t round = 0; pending && round < limit; ++round) {
     unsigned long long hi[N], lo[N];
 #pragma unroll
     for (int k = 0; k < N; ++k)

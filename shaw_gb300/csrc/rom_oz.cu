@@ -50,6 +50,7 @@
 #include <vector>
 
 #include "rom_oz.h"
+#include "l2_exchange.cuh"
 #include "shaw_internal.h"
 #include "tc_ptx.cuh"
 
@@ -1367,7 +1368,8 @@ __global__ void __launch_bounds__(kThreads, 1) rom_rank2_ozaki_kernel(OzArgs a) 
 // that nothing completes (the wait of gates, stages and accumulators) and a global counter
 // that nothing increments (the wait on the peer of a paired tile).  Each must give up after
 // `polls` polls; status gets the error bits the kernel uses for them (64, 128).
-__global__ void oz_wait_selftest_kernel(unsigned long long polls, const unsigned int* ctr, unsigned int* status) {
+__global__ void oz_wait_selftest_kernel(unsigned long long polls, const unsigned int* ctr,
+                                        const unsigned long long* word, unsigned int* status) {
   __shared__ uint64_t bar;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
@@ -1378,6 +1380,12 @@ __global__ void oz_wait_selftest_kernel(unsigned long long polls, const unsigned
     unsigned int s = 0u;
     if (!mbar_wait_n(&bar, 0u, polls)) s |= 64u;      // phase 0: nobody arrives
     if (!poll_counter(ctr, 1u, polls)) s |= 128u;     // the counter stays 0
+    // the band kernels' row exchange: a tagged word that nobody writes (it stays 0, tag 1)
+    double x = 0.0;
+    const unsigned long long* const src[1] = {word};
+    double* const dst[1] = {&x};
+    const uint32_t lim = (uint32_t)(polls < shaw::l2x::kPollLimit ? polls : shaw::l2x::kPollLimit);
+    if (!shaw::l2x::poll<1>(src, dst, 1u, 1u, lim)) s |= 256u;
     *status = s;
   }
 }
@@ -1921,11 +1929,11 @@ std::string describe(const Batch* p) {
 uint32_t num_ctas(const Batch* p) { return p->ctas; }
 
 int wait_selftest(unsigned long long polls, unsigned int* status) {
-  unsigned int* d = nullptr;
-  SHAW_CUDA(cudaMalloc(&d, 2 * sizeof(unsigned int)));
-  cudaError_t rc = cudaMemset(d, 0, 2 * sizeof(unsigned int));
+  unsigned int* d = nullptr;  // [0] the counter, [1] the status, [4..7] the tagged word pair
+  SHAW_CUDA(cudaMalloc(&d, 8 * sizeof(unsigned int)));
+  cudaError_t rc = cudaMemset(d, 0, 8 * sizeof(unsigned int));
   if (rc == cudaSuccess) {
-    oz_wait_selftest_kernel<<<1, 32>>>(polls, d, d + 1);
+    oz_wait_selftest_kernel<<<1, 32>>>(polls, d, reinterpret_cast<const unsigned long long*>(d + 4), d + 1);
     rc = cudaGetLastError();
   }
   if (rc == cudaSuccess) rc = cudaDeviceSynchronize();

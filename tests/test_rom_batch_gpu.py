@@ -203,14 +203,15 @@ def test_batch_ozaki_paired_tiles_bitwise(shaw, width):
 
 
 def test_bounded_waits_report_timeouts(shaw):
-    """Failure detection without a fault: the persistent ROM kernels' waits are bounded.
-    A wait on an mbarrier phase that nothing completes and one on a counter that nothing
-    increments each give up after the poll limit and report it (error bits 64 and 128,
-    as the kernels do), and the device stays usable: a tensor-core batch runs right after
-    and matches the FP64 batch."""
+    """Failure detection without a fault: the persistent kernels' waits are bounded.
+    A wait on an mbarrier phase that nothing completes, one on a counter that nothing
+    increments and one on a tagged exchange word that nothing writes (the band kernels'
+    row exchange) each give up after the poll limit and report it (bits 64, 128, 256), and
+    the device stays usable: a tensor-core batch runs right after and matches the FP64
+    batch."""
     st = ctypes.c_uint32(0)
     assert shaw.lib().shaw_selftest_bounded_waits(1 << 14, ctypes.byref(st)) == 0
-    assert st.value == 64 | 128
+    assert st.value == 64 | 128 | 256
     assert shaw.lib().shaw_selftest_bounded_waits(0, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
     # beyond the kernels' own wait limit (2^24 polls): refused before any launch
     assert shaw.lib().shaw_selftest_bounded_waits((1 << 24) + 1, ctypes.byref(st)) == shaw.ERR_INVALID_ARG
