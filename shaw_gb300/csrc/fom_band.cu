@@ -20,15 +20,14 @@
 //   3. while those rows travel: sigma of the other stp rows, the receivers of the band,
 //      and v of the interior rows for the NEXT step (they read only this band's rows);
 //   4. wait for srp(j1) and stp(j1, .) from band b + 1 and srp(j0 - 1) from band b - 1.
-// Rows travel through L2 as self-validating 8-byte words: each carries 32 bits of the
-// double and a 32-bit tag naming the step, so a reader polls the data itself; no flag,
-// fence or second round trip follows the data.  Each 8-byte word is written and read by
-// single-copy-atomic accesses, so a word is never seen half old and half new.  Tags grow
-// monotonically over the life of the buffers (the host clears them before the 32-bit tag
-// would wrap), so a word left by an earlier step or launch never matches.  Each direction
-// has two slots, by step parity: band b writes its rows of step n + 2 into the slot of step
-// n only after it has received the neighbour's rows of step n + 1, which that neighbour
-// sends after it has read b's rows of step n.
+// When the step-3 work fits the warps left over, 3 and 4 run side by side: the first
+// warps (one lane per received point) poll from the moment their rows are sent, the others
+// do the step-3 work, and the two groups meet at a named barrier before v is overwritten.
+// Rows travel through L2 as tagged words (l2_exchange.cuh), the tag naming the step; the
+// host clears the words before the 32-bit tag would wrap.  Each direction has two slots,
+// by step parity: band b writes its rows of step n + 2 into the slot of step n only after
+// it has received the neighbour's rows of step n + 1, which that neighbour sends after it
+// has read b's rows of step n.
 // Results are bit-identical to the two half-step kernels.  Every wait is bounded: a wait
 // that runs out sets ctl->error bit 1 and the CTA leaves the loop; its neighbours' waits
 // then run out in turn, so the launch always ends.
