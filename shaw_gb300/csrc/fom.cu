@@ -436,11 +436,11 @@ struct shaw_fom_s {
   int sms = 0;
   // rank-1 persistent band path (small FP64 grids): bands, rows per band, shared memory
   bool band_ok = false, use_band = false;
-  uint32_t band_n = 0, band_rows = 0;
+  uint32_t band_n = 0, band_rows = 0, band_cols = 0;  // band width (rows or columns), column bands
   size_t band_smem = 0;
   double* ftab = nullptr;                 // [kBandSteps] forcing increments of one band launch
   unsigned long long* xwords = nullptr;   // halo exchange words, down then up
-  unsigned long long* rcv_sorted = nullptr;  // [R][2] (gid, receiver) pairs in gid order
+  unsigned long long* rcv_sorted = nullptr;  // [R][2] (key, receiver) pairs in key order (band ranges)
   uint32_t band_tag = 0;                  // last tag used in xwords (0: cleared)
   uint64_t src0 = 0;  // the rank-1 source: gid, kind, period, delay
   int kind0 = 0;
@@ -925,8 +925,8 @@ int shaw_fom_create(const shaw_fom_operator_desc* d, int rank, uint32_t M, int p
     h->sweep = auto_sweep(h);
   }
   if (rank == 1 && precision == SHAW_FP64)
-    h->band_ok = h->use_band =
-        shaw::band::plan((uint32_t)h->nth, (uint32_t)h->nr, &h->band_n, &h->band_rows, &h->band_smem);
+    h->band_ok = h->use_band = shaw::band::plan((uint32_t)h->nth, (uint32_t)h->nr, &h->band_n, &h->band_rows,
+                                                &h->band_cols, &h->band_smem);
   SHAW_TRY(cudaStreamSynchronize(h->stream));
 #undef SHAW_TRY
   *out = h;
@@ -1000,13 +1000,17 @@ int shaw_fom_set_receivers(shaw_fom_t h, const uint64_t* gid, uint32_t R, uint64
   SHAW_CUDA(cudaMalloc(&h->rcv, R * sizeof(unsigned long long)));
   SHAW_CUDA(cudaMalloc(&h->seis, (size_t)R * T * h->M * sizeof(double)));
   SHAW_CUDA(cudaMemcpyAsync(h->rcv, gid, R * sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
-  if (h->band_ok) {  // (gid, receiver) pairs in gid order: each row band reads a contiguous range
+  if (h->band_ok) {  // (key, receiver) pairs in key order: each band reads a contiguous range
+    // key: the gid (row-major) for row bands, i nr + j (column-major) for column bands
+    auto key = [&](uint64_t g) -> unsigned long long {
+      return h->band_cols ? (unsigned long long)(g % h->nth) * h->nr + g / h->nth : (unsigned long long)g;
+    };
     std::vector<unsigned long long> pairs(2 * (size_t)R);
     std::vector<uint32_t> order(R);
     for (uint32_t r = 0; r < R; ++r) order[r] = r;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return gid[x] < gid[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return key(gid[x]) < key(gid[y]); });
     for (uint32_t q = 0; q < R; ++q) {
-      pairs[2 * (size_t)q] = gid[order[q]];
+      pairs[2 * (size_t)q] = key(gid[order[q]]);
       pairs[2 * (size_t)q + 1] = order[q];
     }
     SHAW_CUDA(cudaMalloc(&h->rcv_sorted, 2 * (size_t)R * sizeof(unsigned long long)));
@@ -1110,11 +1114,13 @@ int shaw_fom_advance(shaw_fom_t h, double dt, uint64_t nsteps) {
     c.nth = (uint32_t)h->nth;
     c.nr = (uint32_t)h->nr;
     c.rows = h->band_rows;
+    c.cols = h->band_cols;
     c.R = h->R;
     c.seis_freq = (uint32_t)h->seis_freq;
     c.seis_T = (uint32_t)h->seis_T;
-    const size_t dw = shaw::band::down_words(h->band_n, (uint32_t)h->nth);
-    const size_t words = dw + shaw::band::up_words(h->band_n, (uint32_t)h->nth);
+    const uint32_t L = h->band_cols ? (uint32_t)h->nr : (uint32_t)h->nth;  // points of a band's edge line
+    const size_t dw = shaw::band::down_words(h->band_n, L);
+    const size_t words = dw + shaw::band::up_words(h->band_n, L);
     if (!h->ftab) {
       SHAW_CUDA(cudaMalloc(&h->ftab, kBandSteps * sizeof(double)));
       SHAW_CUDA(cudaMalloc(&h->xwords, words * sizeof(unsigned long long)));

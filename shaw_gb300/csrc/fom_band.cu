@@ -382,36 +382,392 @@ __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
   }
 }
 
+
+// ---- the same leapfrog on column bands (grids wider than tall) ------------------------
+//
+// CTA b owns theta columns i0 .. i1 - 1 for every r row: its v columns plus v(., i1), its
+// srp columns plus srp(., i1), its stp columns plus stp(., i0 - 1) and stp(., i1), and the
+// folded stencil values of all of them; the shared arrays are column-major (stride nr for
+// v and stp, nr - 1 for srp).  The roles of the row bands swap: the edge velocity columns
+// are i0 (reading the received stp(., i0 - 1)) and i1 (computed here from the received
+// srp(., i1) and stp(., i1) -- band b + 1 computes the same values); band b sends srp(., i0)
+// and stp(., i0) to band b - 1 and stp(., i1 - 1) to band b + 1.  Same step order, roles,
+// slots and bounded waits as the row kernel; bit-identical to the half-step kernels.
+
+// Column-band velocity set: p = c nr + j (column c = i - i0) and m: bit 0 interior theta
+// point, bit 1 N is srp(j) (else srp(j - 1)), bit 2 S is srp(j - 1) (else srp(j)), bits 3..
+// = c.  srp(j, i) is SRP[p - c], srp(j - 1, i) is SRP[p - c - 1]; stp(j, i - 1) is STP[p]
+// and stp(j, i) is STP[p + nr].
+template <bool FORCE>
+__device__ __forceinline__ void velocity_cols(const VelSet& e, double* V, const double* SRP, const double* STP,
+                                              const double* CV, uint32_t nv, uint32_t nr, int src_p, double fdt) {
+#pragma unroll
+  for (int k = 0; k < kBatch; ++k) {
+    if (e.p[k] < 0) continue;
+    const int p = e.p[k], m = e.m[k], c = m >> 3;
+    double v = V[p];
+    if (m & 1) {
+      v = fma(CV[p], SRP[(m & 2) ? p - c : p - c - 1], v);           // N
+      v = fma(CV[nv + p], SRP[(m & 4) ? p - c - 1 : p - c], v);      // S
+      v = fma(CV[2 * nv + p], STP[p], v);                           // W
+      v = fma(CV[3 * nv + p], STP[p + (int)nr], v);                 // E
+    }
+    if (FORCE && p == src_p) v = __dadd_rn(v, fdt);  // after the FMAs, as the half-step kernel
+    V[p] = v;
+  }
+}
+
+// Received points of a column band: first the message from the right (srp(., i1), nr - 1
+// points, then stp(., i1), nr points, when it exists), then stp(., i0 - 1) from the left.
+__device__ __forceinline__ bool receive_cols(const unsigned long long* recv_right, const unsigned long long* recv_left,
+                                             uint32_t slot, uint32_t tag, size_t left_pts, size_t right_pts,
+                                             uint32_t n_right, uint32_t n_recv, uint32_t nr, uint32_t ncol,
+                                             double* SRP, double* STP, uint32_t t, uint32_t nt) {
+  const unsigned long long* src[kRecvMax];
+  double* dst[kRecvMax];
+  uint32_t pending = 0;
+#pragma unroll
+  for (int k = 0; k < kRecvMax; ++k) {
+    const uint32_t q = t + k * nt;
+    src[k] = nullptr;
+    dst[k] = nullptr;
+    if (q >= n_recv) continue;
+    pending |= 1u << k;
+    if (q < n_right) {  // the right band's left message: srp(., i1) then stp(., i1)
+      src[k] = recv_right + (size_t)slot * left_pts * 2 + 2 * q;
+      dst[k] = q < nr - 1 ? SRP + (size_t)ncol * (nr - 1) + q : STP + (size_t)(ncol + 1) * nr + (q - (nr - 1));
+    } else {  // the left band's right message: stp(., i0 - 1)
+      const uint32_t pb = q - n_right;
+      src[k] = recv_left + (size_t)slot * right_pts * 2 + 2 * pb;
+      dst[k] = STP + pb;
+    }
+  }
+  return l2x::poll<kRecvMax>(src, dst, pending, tag);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) fom_bandc_kernel(const Args a) {
+  const uint32_t b = blockIdx.x;
+  const uint32_t nth = a.nth, nr = a.nr, cw = a.rows;  // cw: columns per band
+  const uint32_t i0 = b * cw, i1 = min(nth, i0 + cw), ncol = i1 - i0;  // plan: every band owns columns
+  const bool right = i1 < nth;  // a band on the right: v(., i1) computed here, srp(., i1), stp(., i1) from it
+  const bool left = i0 > 0;     // a band on the left: stp(., i0 - 1) from it
+  const bool stp_right = i1 + 1 < nth;  // stp(., i1) exists
+  const uint32_t vcols = ncol + (right ? 1 : 0);
+  const uint32_t sp_row = 2 * nth - 1, ns1 = nr - 1;
+  const size_t nvp = (size_t)nth * nr, nsp = (size_t)(nr - 1) * nth + (size_t)nr * (nth - 1);
+  extern __shared__ __align__(16) double sm[];
+  double* const V = sm;                                   // (cw + 1) x nr: columns i0 .. i1
+  double* const SRP = V + (size_t)(cw + 1) * nr;          // (cw + 1) x (nr - 1): columns i0 .. i1
+  double* const STP = SRP + (size_t)(cw + 1) * ns1;       // (cw + 2) x nr: columns i0 - 1 .. i1
+  double* const CV = STP + (size_t)(cw + 2) * nr;         // 4 x (cw + 1) x nr: columns i0 .. i1
+  double* const CSR = CV + (size_t)4 * (cw + 1) * nr;     // 2 x cw x (nr - 1): own srp columns
+  double* const CST = CSR + (size_t)2 * cw * ns1;         // 2 x cw x nr: own stp columns
+  const uint32_t nv = (cw + 1) * nr, nsr = cw * ns1, nst = cw * nr;
+  // messages: left = srp(., i0) then stp(., i0) (2 nr - 1 points), right = stp(., i1 - 1) (nr)
+  const size_t left_pts = 2 * (size_t)nr - 1, right_pts = nr;
+  unsigned long long* const send_left = a.xdown + (size_t)b * 2 * left_pts * 2;  // + slot * left_pts * 2
+  unsigned long long* const send_right = a.xup + (size_t)b * 2 * right_pts * 2;
+  const unsigned long long* const recv_right = right ? a.xdown + (size_t)(b + 1) * 2 * left_pts * 2 : nullptr;
+  const unsigned long long* const recv_left = left ? a.xup + (size_t)(b - 1) * 2 * right_pts * 2 : nullptr;
+  auto stp_q = [&](uint32_t j, uint32_t i) -> size_t {  // stp(j, i) in the sp state
+    return (j + 1 < nr) ? (size_t)j * sp_row + 2 * i + 1 : (size_t)j * sp_row + i;
+  };
+
+  // the band, its halos and its stencil values
+  for (uint32_t e = threadIdx.x; e < vcols * nr; e += kThreads) {
+    const uint32_t c = e / nr, j = e - c * nr;
+    const size_t p = (size_t)j * nth + i0 + c;
+    V[e] = a.xv[p];
+    for (int q = 0; q < 4; ++q) CV[q * nv + e] = a.cvp[q * nvp + p];
+  }
+  for (uint32_t e = threadIdx.x; e < vcols * ns1; e += kThreads) {
+    const uint32_t c = e / ns1, j = e - c * ns1;
+    const size_t q = (size_t)j * sp_row + 2 * (i0 + c);
+    SRP[e] = a.xs[q];
+    if (c < ncol) {
+      CSR[e] = a.csp[q];
+      CSR[nsr + e] = a.csp[nsp + q];
+    }
+  }
+  for (uint32_t e = threadIdx.x; e < (ncol + 2) * nr; e += kThreads) {
+    const uint32_t c = e / nr, j = e - c * nr;
+    const int i = (int)i0 - 1 + (int)c;  // stp column
+    if (i >= 0 && i + 1 < (int)nth && i <= (int)i1) STP[e] = a.xs[stp_q(j, (uint32_t)i)];
+    if (c >= 1 && c <= ncol && i + 1 < (int)nth) {  // own stp column c - 1
+      const size_t q = stp_q(j, (uint32_t)i);
+      CST[e - nr] = a.csp[q];
+      CST[nst + e - nr] = a.csp[nsp + q];
+    }
+  }
+
+  // Roles, as in the row kernel.  Received: srp(., i1) (nr - 1) and stp(., i1) (nr, when it
+  // exists) from the right, stp(., i0 - 1) (nr) from the left.
+  const uint32_t n_edge_cols = (left ? 1 : 0) + (right ? 1 : 0);
+  const uint32_t n_int_cols = vcols - n_edge_cols;
+  const uint32_t c_first_int = left ? 1 : 0;
+  const bool stp_left_msg = left && i0 + 1 < nth;           // stp(., i0) exists and goes left
+  const uint32_t n_s2_srp = (ncol - (left ? 1 : 0)) * ns1;  // srp columns not sent
+  // stp columns sent: 0 (to the left, when it exists) and ncol - 1 (to the right)
+  const bool c0_sent = stp_left_msg, clast_sent = right;  // (ncol - 1 == 0 is one column, sent both ways)
+  const uint32_t last_stp_col = right ? ncol : ncol - 1;  // own stp columns [0, last_stp_col): stp(., i) for i <= nth - 2
+  const uint32_t n_right = right ? ns1 + (stp_right ? nr : 0) : 0;
+  const uint32_t n_recv = n_right + (left ? nr : 0);
+  const uint32_t poll_threads = min(kThreads, 32 * ((n_recv + 31) / 32));
+  const uint32_t work_threads = kThreads - poll_threads;
+  // unsent stress elements: srp of columns c_first_int .. ncol - 1, stp of the columns that
+  // are not sent
+  uint32_t n_s2_stp = 0;
+  for (uint32_t c = 0; c < last_stp_col; ++c)
+    if (!((c == 0 && c0_sent) || (c + 1 == ncol && clast_sent))) n_s2_stp += nr;
+  const uint32_t n_s2 = n_s2_srp + n_s2_stp;
+  const bool split = work_threads > 0 && n_s2 <= kBatch * work_threads && n_int_cols * nr <= kBatch * work_threads;
+  const bool poller = !split || threadIdx.x < poll_threads;
+  const bool worker = !split || threadIdx.x >= poll_threads;
+  const uint32_t wt = split ? threadIdx.x - poll_threads : threadIdx.x;
+  const uint32_t nwt = split ? work_threads : kThreads;
+  const uint32_t npt = split ? poll_threads : kThreads;
+
+  VelSet ve, vi;
+  int src_p = -1;
+  {
+    const unsigned long long js = a.src / nth, is = a.src - js * nth;
+    if (is >= i0 && is < i0 + vcols) src_p = (int)((is - i0) * nr + js);
+  }
+  bool ve_src = false, vi_src = false;
+#pragma unroll
+  for (int k = 0; k < kBatch; ++k) {
+#pragma unroll
+    for (int set = 0; set < 2; ++set) {
+      VelSet& vs = set ? vi : ve;
+      const uint32_t ncols_set = set ? n_int_cols : n_edge_cols;
+      const uint32_t e = set ? (worker ? wt + k * nwt : ~0u) : threadIdx.x + k * kThreads;
+      vs.p[k] = -1;
+      vs.m[k] = 0;
+      if (e < ncols_set * nr) {
+        const uint32_t r = e / nr, j = e - r * nr;
+        const uint32_t c = set ? c_first_int + r : ((left && r == 0) ? 0 : ncol);  // the column
+        const uint32_t i = i0 + c, pt = c * nr + j;
+        vs.p[k] = (int)pt;
+        vs.m[k] = (i != 0 && i + 1 != nth ? 1 : 0) | (j + 1 < nr ? 2 : 0) | (j > 0 ? 4 : 0) | (int)(c << 3);
+        if ((int)pt == src_p) (set ? vi_src : ve_src) = true;
+      }
+    }
+  }
+  // Sent stress elements (all threads): s1t = target (SRP or STP place), s1v = the first v
+  // input (the second is s1v + 1 for srp, s1v + nr for stp), s1m: bit 0 srp, bit 1 to the
+  // right, bit 2 to the left, bits 3.. = the message point.  Unsent ones (workers): s2t,
+  // s2v, s2m likewise (bit 0 srp).  Coefficients: CSR[t] / CST[t - nr] for srp / stp.
+  const uint32_t n_s1_srp = left ? ns1 : 0;
+  const uint32_t n_s1_stp = ((c0_sent ? 1u : 0u) + ((clast_sent && !(ncol == 1 && c0_sent)) ? 1u : 0u)) * nr;
+  const uint32_t n_s1 = n_s1_srp + n_s1_stp;
+  int s1t[kBatch], s1v[kBatch], s1m[kBatch], s2t[kBatch], s2v[kBatch], s2m[kBatch];
+#pragma unroll
+  for (int k = 0; k < kBatch; ++k) {
+    const uint32_t e = threadIdx.x + k * kThreads;
+    s1t[k] = s2t[k] = -1;
+    s1v[k] = s1m[k] = s2v[k] = s2m[k] = 0;
+    if (e < n_s1_srp) {  // srp(j, i0), to the left
+      const uint32_t j = e;
+      s1t[k] = (int)j;
+      s1v[k] = (int)j;  // v(j, i0) at V[j]; v(j + 1, i0) follows
+      s1m[k] = 1 | 4 | (int)(j << 3);
+    } else if (e < n_s1) {  // stp(j, i0) (left and/or right) or stp(j, i1 - 1) (right)
+      const uint32_t f = e - n_s1_srp, which = f / nr, j = f - which * nr;
+      const uint32_t c = (which == 0 && c0_sent) ? 0 : ncol - 1;
+      s1t[k] = (int)((c + 1) * nr + j);
+      s1v[k] = (int)(c * nr + j);
+      const bool to_left = c == 0 && c0_sent, to_right = c + 1 == ncol && clast_sent;
+      const uint32_t lp = (uint32_t)ns1 + j;  // the left message's stp points follow its srp points
+      s1m[k] = (to_right ? 2 : 0) | (to_left ? 4 : 0) | (int)((to_left ? lp : j) << 3);
+      if (to_left && to_right) s1m[k] |= (int)(1u << 30);  // right point = j (low bits carry lp)
+    }
+    const uint32_t e2 = worker ? wt + k * nwt : ~0u;
+    if (e2 < n_s2_srp) {
+      const uint32_t c = c_first_int + e2 / ns1, j = e2 % ns1;
+      s2t[k] = (int)(c * ns1 + j);
+      s2v[k] = (int)(c * nr + j);
+      s2m[k] = 1;
+    } else if (e2 < n_s2) {
+      uint32_t f = e2 - n_s2_srp, c = 0;
+      for (; c < last_stp_col; ++c) {  // the f-th unsent stp element
+        if ((c == 0 && c0_sent) || (c + 1 == ncol && clast_sent)) continue;
+        if (f < nr) break;
+        f -= nr;
+      }
+      s2t[k] = (int)((c + 1) * nr + f);
+      s2v[k] = (int)(c * nr + f);
+      s2m[k] = 0;
+    }
+  }
+  const bool ve_force = __any_sync(0xffffffffu, ve_src), vi_force = __any_sync(0xffffffffu, vi_src);
+
+  // receivers: a range of the list in column-major key order (key = i nr + j = V place + i0 nr)
+  __shared__ uint32_t s_rcv[2];
+  if (threadIdx.x < 2) {
+    const unsigned long long key = (unsigned long long)(threadIdx.x ? i1 : i0) * nr;
+    uint32_t lo = 0, hi = a.R;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (a.rcv_sorted[2 * (size_t)mid] < key) lo = mid + 1; else hi = mid;
+    }
+    s_rcv[threadIdx.x] = lo;
+  }
+  uint32_t phase = a.seis_freq ? (uint32_t)(a.step0 % a.seis_freq) : 0;
+  uint32_t sample = 0;
+  if (a.seis_freq) {
+    const unsigned long long s0 = a.step0 / a.seis_freq;
+    sample = s0 < a.seis_T ? (uint32_t)s0 : a.seis_T;
+  }
+  __syncthreads();
+  const uint32_t rcv_lo = s_rcv[0], rcv_hi = s_rcv[1];
+
+  auto stress = [&](int t, int v0, int m) -> double {  // one element, the stress kernel's FMAs
+    if (m & 1) {  // srp(j, i): north v(j + 1, i), south v(j, i)
+      double y = SRP[t];
+      y = fma(CSR[t], V[v0 + 1], y);
+      y = fma(CSR[nsr + t], V[v0], y);
+      SRP[t] = y;
+      return y;
+    }
+    double y = STP[t];  // stp(j, i): west v(j, i), east v(j, i + 1)
+    y = fma(CST[t - (int)nr], V[v0], y);
+    y = fma(CST[nst + t - (int)nr], V[v0 + (int)nr], y);
+    STP[t] = y;
+    return y;
+  };
+
+  if (a.nsteps > 0) {
+    if (vi_force) velocity_cols<true>(vi, V, SRP, STP, CV, nv, nr, src_p, a.ftab[0]);
+    else velocity_cols<false>(vi, V, SRP, STP, CV, nv, nr, -1, 0.0);
+  }
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    const uint32_t tag = a.tag0 + (uint32_t)it;
+    const uint32_t slot = (uint32_t)(it & 1);
+    if (ve_force) velocity_cols<true>(ve, V, SRP, STP, CV, nv, nr, src_p, a.ftab[it]);
+    else velocity_cols<false>(ve, V, SRP, STP, CV, nv, nr, -1, 0.0);
+    __syncthreads();
+    {
+      unsigned long long* const sl = send_left + (size_t)slot * left_pts * 2;
+      unsigned long long* const sr = send_right + (size_t)slot * right_pts * 2;
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) {
+        if (s1t[k] < 0) continue;
+        const int m = s1m[k];
+        const double y = stress(s1t[k], s1v[k], m);
+        const int pt = (m >> 3) & ((1 << 27) - 1);
+        if (m & 4) l2x::put(sl + 2 * pt, tag, y);
+        if (m & 2) l2x::put(sr + 2 * ((m & (1 << 30)) ? pt - (int)ns1 : pt), tag, y);
+      }
+    }
+    const bool sampling = a.seis_freq && ++phase == a.seis_freq;
+    if (sampling) phase = 0;
+    bool ok = true;
+    if (split && poller) {
+      asm volatile("bar.arrive 1, %0;" ::"r"(kThreads) : "memory");
+      ok = receive_cols(recv_right, recv_left, slot, tag, left_pts, right_pts, n_right, n_recv, nr, ncol, SRP, STP,
+                        threadIdx.x, npt);
+    }
+    if (worker) {
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k)
+        if (s2t[k] >= 0) stress(s2t[k], s2v[k], s2m[k]);
+      if (sampling && sample < a.seis_T) {
+        for (uint32_t q = rcv_lo + wt; q < rcv_hi; q += nwt) {
+          const unsigned long long g = a.rcv_sorted[2 * (size_t)q], r = a.rcv_sorted[2 * (size_t)q + 1];
+          const double val = V[g - (unsigned long long)i0 * nr];
+          a.seis[r + (size_t)a.R * sample] = val;
+          if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
+        }
+      }
+      if (split)
+        asm volatile("bar.sync 1, %0;" ::"r"(kThreads) : "memory");
+      else
+        __syncthreads();
+      if (it + 1 < a.nsteps) {
+        if (vi_force) velocity_cols<true>(vi, V, SRP, STP, CV, nv, nr, src_p, a.ftab[it + 1]);
+        else velocity_cols<false>(vi, V, SRP, STP, CV, nv, nr, -1, 0.0);
+      }
+    }
+    if (sampling && sample < a.seis_T) ++sample;
+    if (!split)
+      ok = receive_cols(recv_right, recv_left, slot, tag, left_pts, right_pts, n_right, n_recv, nr, ncol, SRP, STP,
+                        threadIdx.x, npt);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
+      break;
+    }
+  }
+  // the band back to the state (its own columns only)
+  for (uint32_t e = threadIdx.x; e < ncol * nr; e += kThreads) {
+    const uint32_t c = e / nr, j = e - c * nr;
+    a.xv[(size_t)j * nth + i0 + c] = V[e];
+  }
+  for (uint32_t e = threadIdx.x; e < ncol * ns1; e += kThreads) {
+    const uint32_t c = e / ns1, j = e - c * ns1;
+    a.xs[(size_t)j * sp_row + 2 * (i0 + c)] = SRP[e];
+  }
+  for (uint32_t e = threadIdx.x; e < last_stp_col * nr; e += kThreads) {
+    const uint32_t c = e / nr, j = e - c * nr;
+    a.xs[stp_q(j, i0 + c)] = STP[e + nr];
+  }
+}
 }  // namespace
 
-bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* rows, size_t* smem) {
+// Doubles of shared memory a column band of cw theta columns needs.
+inline size_t smem_doubles_cols(uint32_t nr, uint32_t cw) {
+  return (size_t)(cw + 1) * nr + (size_t)(cw + 1) * (nr - 1) + (size_t)(cw + 2) * nr + (size_t)4 * (cw + 1) * nr +
+         (size_t)2 * cw * (nr - 1) + (size_t)2 * cw * nr;
+}
+
+namespace {
+
+// Whether kern fits `need` co-resident CTAs with `bytes` of shared memory each.
+bool fits(void (*kern)(Args), size_t bytes, int sms, int optin, uint32_t need) {
+  if (bytes + 1024 > (size_t)optin) return false;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, bytes) != cudaSuccess ||
+      (size_t)per_sm * sms < need) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+bool plan(uint32_t nth, uint32_t nr, uint32_t* bands, uint32_t* width, uint32_t* cols, size_t* smem) {
   if (nth < 3 || nr < 2) return false;
   int dev = 0, sms = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return false;
-  // the fewest rows per band with one band per SM; the grid needs at least two bands
-  const uint32_t r = (nr + (uint32_t)sms - 1) / (uint32_t)sms;
-  const uint32_t g = (nr + r - 1) / r;
-  if (g < 2) return false;
-  if ((size_t)(r + 1) * nth > (size_t)kBatch * kThreads) return false;  // at most kBatch points a thread
-  if (3 * (size_t)nth > (size_t)kRecvMax * kThreads) return false;       // received points: under 3 nth
-  const size_t bytes = smem_doubles(nth, r) * sizeof(double);
-  if (bytes + 1024 > (size_t)optin) return false;
-  if (cudaFuncSetAttribute(fom_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
+  // the narrowest bands with one band per SM; at least two bands.  Cost: the points between
+  // receiving and sending (edge velocity rows plus the stress rows sent), per band.
+  const uint32_t r = (nr + (uint32_t)sms - 1) / (uint32_t)sms, gr = (nr + r - 1) / r;
+  const uint32_t w = (nth + (uint32_t)sms - 1) / (uint32_t)sms, gc = (nth + w - 1) / w;
+  const size_t br = smem_doubles(nth, r) * sizeof(double), bc = smem_doubles_cols(nr, w) * sizeof(double);
+  const bool row_ok = gr >= 2 && (size_t)(r + 1) * nth <= (size_t)kBatch * kThreads &&
+                      3 * (size_t)nth <= (size_t)kRecvMax * kThreads && fits(fom_band_kernel, br, sms, optin, gr);
+  const bool col_ok = gc >= 2 && (size_t)(w + 1) * nr <= (size_t)kBatch * kThreads &&
+                      3 * (size_t)nr <= (size_t)kRecvMax * kThreads && fits(fom_bandc_kernel, bc, sms, optin, gc);
+  const size_t cost_r = (size_t)(r + 3) * nth, cost_c = (size_t)(w >= 2 ? 5 : 4) * nr;
+  if (col_ok && (!row_ok || cost_c < cost_r)) {
+    *bands = gc;
+    *width = w;
+    *cols = 1;
+    *smem = bc;
+    return true;
   }
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fom_band_kernel, kThreads, bytes) != cudaSuccess ||
-      (size_t)per_sm * sms < g) {
-    cudaGetLastError();
-    return false;
-  }
-  *bands = g;
-  *rows = r;
-  *smem = bytes;
+  if (!row_ok) return false;
+  *bands = gr;
+  *width = r;
+  *cols = 0;
+  *smem = br;
   return true;
 }
 
@@ -419,7 +775,8 @@ int launch(const Args& a, uint32_t bands, size_t smem, cudaStream_t s) {
   fom_band_forcing_kernel<<<(unsigned)((a.nsteps + 255) / 256), 256, 0, s>>>(a);
   SHAW_CUDA(cudaGetLastError());
   // per launch: another handle's plan may have set the kernel's limit for a smaller grid
-  SHAW_CUDA(cudaFuncSetAttribute(fom_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  void (*kern)(Args) = a.cols ? fom_bandc_kernel : fom_band_kernel;
+  SHAW_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg;
   std::memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(bands);
@@ -431,7 +788,7 @@ int launch(const Args& a, uint32_t bands, size_t smem, cudaStream_t s) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  SHAW_CUDA(cudaLaunchKernelEx(&cfg, fom_band_kernel, a));
+  SHAW_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
   return SHAW_OK;
 }
 

@@ -1,5 +1,7 @@
 """The rank-1 FOM as one persistent cooperative launch (SHAW_FOM_SCHEDULE_PERSISTENT, the
-default for rank-1 FP64 handles on grids whose row bands fit one CTA per SM).
+default for rank-1 FP64 handles on grids whose bands fit one CTA per SM): row bands, or
+column bands on grids wider than tall (201 x 101, 51 x 21, 7 x 5, 500 x 21, the 21 x 51
+fixture).
 
 The band kernel runs the two half-step kernels' FMAs in the same order, so its states
 and seismograms must equal theirs bit for bit; it is also held to the oracle (1e-12
@@ -117,8 +119,9 @@ def test_persistent_schedule_errors(shaw, oracle):
         g.set_schedule(shaw.SCHEDULE_PERSISTENT)
     assert e.value.code == shaw.ERR_UNSUPPORTED
     g.close()
-    # a band wider than 1024 points (four per thread) keeps the two half-step kernels
-    wide = shaw.Mesh.generate(1100, 3)
+    # bands of more than 1024 points either way (row bands of 4 x 1100, column bands of
+    # 8 x 600 points plus a halo line) keep the two half-step kernels
+    wide = shaw.Mesh.generate(1100, 600)
     wide.set_material("unilayer", MATERIAL)
     h = shaw.Fom(wide, 1, 1)
     with pytest.raises(shaw.ShawError) as e:
