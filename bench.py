@@ -321,7 +321,7 @@ def fom_rank1_config1(np, torch, shaw, nth, nr, n=2000):
     ref = om.fom_run(1, n, dt, [src], [2], [60.0], [180.0], rcv, 1, 0, 0)
     return {"metric": "FOM DOF-updates/s", "value": (mesh.nvp + mesh.nsp) * n / t, "steps": n,
             "us_per_step": t / n * 1e6, "launches": launches,
-            "schedule": "persistent (one cooperative launch of row bands; the default for rank-1 FP64)",
+            "schedule": "persistent (one cooperative launch of row or column bands; the default for rank-1 FP64)",
             "two_pass_us_per_step": t2 / n * 1e6,
             "max_rel_err_vs_oracle": {"seismogram": _relerr(np, seis, ref["seis"]),
                                       "state_vp": _relerr(np, vp, ref["final_vp"]),

@@ -163,12 +163,13 @@ int shaw_fom_set_state(shaw_fom_t h, const double* vp, const double* sp);
  *     FP32 one) and alternates between two state buffers.  Same FMAs in the same order as
  *     the two-pass kernels: bit-identical results.
  *   SHAW_FOM_SCHEDULE_PERSISTENT: rank 1, FP64, small grids: all the steps of a call in
- *     one cooperative launch (one CTA per SM, each a band of r rows in shared memory, halo
- *     rows exchanged through L2 as tagged words); bit-identical to the two-pass kernels;
- *     runs with snapshots keep the two-pass kernels.
+ *     one cooperative launch (one CTA per SM, each a band of r rows -- or of theta
+ *     columns, on grids wider than tall -- in shared memory, halo lines exchanged through
+ *     L2 as tagged words); bit-identical to the two-pass kernels; runs with snapshots keep
+ *     the two-pass kernels.
  *   SHAW_FOM_SCHEDULE_AUTO (the default): the fastest for the handle on GB300: the
- *     persistent launch for rank-1 FP64 handles whose grid fits (at least two r rows,
- *     (rows per band + 1) x nth <= 1024 points), the sweep for SHAW_MIXED_FP32 (HBM-bound,
+ *     persistent launch for rank-1 FP64 handles whose grid fits (at least two bands of at
+ *     most 1024 points with the halo line), the sweep for SHAW_MIXED_FP32 (HBM-bound,
  *     when the column count allows it), otherwise the two-pass kernels (for FP64 both
  *     the sweep and the two-pass kernels are bound by the FP64 pipe, and the two-pass
  *     kernels keep it busier).
