@@ -50,7 +50,7 @@ def parse():
                    choices=["ozaki", "ozaki-fp64", "tf32x3", "fp64", "rank1-fp64", "rank1-mixed"],
                    help="only run the rank-2 ROM (k=512, M=4096) or the rank-1 ROM (k=256, 181 receivers) "
                         "for --steps steps, for profiler captures")
-    p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32", "rank1"],
+    p.add_argument("--profile-fom", default=None, choices=["fp64", "fp32", "rank1", "rank1-wide"],
                    help="only run the FOM on the 1000x2000 grid with --forcings columns for --steps steps")
     p.add_argument("--schedule", default="auto", choices=["auto", "two-pass", "sweep", "persistent"],
                    help="FOM schedule of --profile-fom")
@@ -875,10 +875,11 @@ def main():
         r.run(0.5, args.steps)
         print(json.dumps({"profile_rom": args.profile_rom, "steps": args.steps, "launches": r.kernel_launches}))
         r.close()
-    elif args.profile_fom == "rank1":
+    elif args.profile_fom in ("rank1", "rank1-wide"):
         import shaw_gb300 as shaw
         shaw.build()
-        mesh = shaw.Mesh.generate(101, 201)  # config 1: rank 1, 181 surface receivers
+        # config 1: rank 1, 181 surface receivers, on 101 theta x 201 r or the fixture's 201 x 101
+        mesh = shaw.Mesh.generate(*((101, 201) if args.profile_fom == "rank1" else (201, 101)))
         mesh.set_material("unilayer", MATERIAL)
         dt = 0.25 * min(mesh.info[5], mesh.info[4] * mesh.info[2]) / (2.0 ** 0.5 * 7300.0)
         f = shaw.Fom(mesh, 1, 1)
@@ -887,7 +888,7 @@ def main():
         f.set_sources([mesh.map_source(640.0, 0.0)], "gaussDer", 60.0, 180.0)
         f.set_receivers([mesh.map_receiver(float(a)) for a in range(181)], 1, args.steps)
         f.run(dt, args.steps)
-        print(json.dumps({"profile_fom": "rank1", "steps": args.steps, "launches": f.kernel_launches}))
+        print(json.dumps({"profile_fom": args.profile_fom, "steps": args.steps, "launches": f.kernel_launches}))
     elif args.profile_fom:
         import numpy as np
         import shaw_gb300 as shaw
