@@ -127,6 +127,86 @@ __device__ __forceinline__ bool receive(const unsigned long long* recv_above, co
   return l2x::poll<kRecvMax>(src, dst, pending, tag);
 }
 
+// The time loop shared by the row and the column band kernels (steps 1-4 above, the roles,
+// the barriers and the bounded waits).  The orientation's work comes in as callables:
+// vel_edge(it) / vel_int(it) the velocity of the edge / interior lines of step it,
+// send(tag, slot) the stress of the lines a neighbour waits for (each put as it is formed),
+// unsent() the stress of the other lines, recv(slot, tag, t, nt) the halo lines (points t,
+// t + nt, ...).  V is the band's velocity; the band's receivers have keys in [key0, key1)
+// of the key-ordered list, each at V[key - key0].
+template <class VelE, class VelI, class Send, class Unsent, class Recv>
+__device__ __forceinline__ void band_steps(const Args& a, const double* V, unsigned long long key0,
+                                           unsigned long long key1, bool split, bool poller, bool worker, uint32_t wt,
+                                           uint32_t nwt, uint32_t npt, VelE vel_edge, VelI vel_int, Send send,
+                                           Unsent unsent, Recv recv) {
+  // the receivers: a range of the list; the sampling phase and the sample count before the
+  // launch's first step (step step0 + 1)
+  __shared__ uint32_t s_rcv[2];
+  if (threadIdx.x < 2) {
+    const unsigned long long key = threadIdx.x ? key1 : key0;
+    uint32_t lo = 0, hi = a.R;  // first entry with key >= key
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (a.rcv_sorted[2 * (size_t)mid] < key) lo = mid + 1; else hi = mid;
+    }
+    s_rcv[threadIdx.x] = lo;
+  }
+  uint32_t phase = a.seis_freq ? (uint32_t)(a.step0 % a.seis_freq) : 0;
+  uint32_t sample = 0;  // clamped at seis_T: samples past the seismogram's length are dropped
+  if (a.seis_freq) {
+    const unsigned long long s0 = a.step0 / a.seis_freq;
+    sample = s0 < a.seis_T ? (uint32_t)s0 : a.seis_T;
+  }
+  __syncthreads();
+  const uint32_t rcv_lo = s_rcv[0], rcv_hi = s_rcv[1];
+
+  if (a.nsteps > 0) vel_int(0ull);  // the interior lines of the first step
+  for (unsigned long long it = 0; it < a.nsteps; ++it) {
+    const uint32_t tag = a.tag0 + (uint32_t)it;
+    const uint32_t slot = (uint32_t)(it & 1);
+    // 1. velocity of the edge lines (each thread reads and writes only its own v elements)
+    vel_edge(it);
+    __syncthreads();
+    // 2. stress of the lines a neighbour waits for; each goes out as soon as it is formed
+    //    (each thread reads and writes only its own stress elements; v is fixed)
+    send(tag, slot);
+    // 3. while the lines travel: the other stress lines, the receivers, the next interior
+    //    velocity (workers); 4. the halo lines (pollers).  Work and polls touch different
+    //    lines: the polls write only the halo lines.
+    const bool sampling = a.seis_freq && ++phase == a.seis_freq;
+    if (sampling) phase = 0;
+    bool ok = true;
+    if (split && poller) {
+      asm volatile("bar.arrive 1, %0;" ::"r"(kThreads) : "memory");  // this thread's reads of v are done
+      ok = recv(slot, tag, threadIdx.x, npt);
+    }
+    if (worker) {
+      unsent();
+      // the receivers of the band (Seismogram::storeVelocitySignalAtReceivers)
+      if (sampling && sample < a.seis_T) {
+        for (uint32_t q = rcv_lo + wt; q < rcv_hi; q += nwt) {
+          const unsigned long long g = a.rcv_sorted[2 * (size_t)q], r = a.rcv_sorted[2 * (size_t)q + 1];
+          const double val = V[g - key0];
+          a.seis[r + (size_t)a.R * sample] = val;
+          if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
+        }
+      }
+      // every read of this step's v and every stress line is done
+      if (split)
+        asm volatile("bar.sync 1, %0;" ::"r"(kThreads) : "memory");
+      else
+        __syncthreads();
+      if (it + 1 < a.nsteps) vel_int(it + 1);
+    }
+    if (sampling && sample < a.seis_T) ++sample;
+    if (!split) ok = recv(slot, tag, threadIdx.x, npt);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
+      break;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
   const uint32_t b = blockIdx.x;
   const uint32_t nth = a.nth, nr = a.nr, rows = a.rows;
@@ -262,113 +342,54 @@ __global__ void __launch_bounds__(kThreads, 1) fom_band_kernel(const Args a) {
   // the warps that hold the source run the forcing form of their velocity set
   const bool ve_force = __any_sync(0xffffffffu, ve_src), vi_force = __any_sync(0xffffffffu, vi_src);
 
-  // the band's receivers: a range of the gid-ordered list; the sampling phase and the
-  // sample count before the launch's first step (step step0 + 1)
-  __shared__ uint32_t s_rcv[2];
-  if (threadIdx.x < 2) {
-    const unsigned long long key = (unsigned long long)(threadIdx.x ? j1 : j0) * nth;
-    uint32_t lo = 0, hi = a.R;  // first entry with gid >= key
-    while (lo < hi) {
-      const uint32_t mid = lo + (hi - lo) / 2;
-      if (a.rcv_sorted[2 * (size_t)mid] < key) lo = mid + 1; else hi = mid;
-    }
-    s_rcv[threadIdx.x] = lo;
-  }
-  uint32_t phase = a.seis_freq ? (uint32_t)(a.step0 % a.seis_freq) : 0;
-  uint32_t sample = 0;  // clamped at seis_T: samples past the seismogram's length are dropped
-  if (a.seis_freq) {
-    const unsigned long long s0 = a.step0 / a.seis_freq;
-    sample = s0 < a.seis_T ? (uint32_t)s0 : a.seis_T;
-  }
-  __syncthreads();
-  const uint32_t rcv_lo = s_rcv[0], rcv_hi = s_rcv[1];
-
-  // the interior velocity rows of the first step
-  if (a.nsteps > 0) {
-    if (vi_force) velocity<true>(vi, V, SRP, STP, CV, nv, nth, src_p, a.ftab[0]);
-    else velocity<false>(vi, V, SRP, STP, CV, nv, nth, -1, 0.0);
-  }
-  for (unsigned long long it = 0; it < a.nsteps; ++it) {
-    const uint32_t tag = a.tag0 + (uint32_t)it;
-    const uint32_t slot = (uint32_t)(it & 1);
-    // 1. velocity of the edge rows (each thread reads and writes only its own v elements)
+  auto vel_edge = [&](unsigned long long it) {
     if (ve_force) velocity<true>(ve, V, SRP, STP, CV, nv, nth, src_p, a.ftab[it]);
     else velocity<false>(ve, V, SRP, STP, CV, nv, nth, -1, 0.0);
-    __syncthreads();
-    // 2. stress of the rows a neighbour waits for; each goes out as soon as it is computed
-    //    (each thread reads and writes only its own stress elements; v is fixed)
-    {
-      unsigned long long* const sd = send_down + (size_t)slot * down_pts * 2;
-      unsigned long long* const su = send_up + (size_t)slot * up_pts * 2;
+  };
+  auto vel_int = [&](unsigned long long it) {
+    if (vi_force) velocity<true>(vi, V, SRP, STP, CV, nv, nth, src_p, a.ftab[it]);
+    else velocity<false>(vi, V, SRP, STP, CV, nv, nth, -1, 0.0);
+  };
+  auto send = [&](uint32_t tag, uint32_t slot) {
+    unsigned long long* const sd = send_down + (size_t)slot * down_pts * 2;
+    unsigned long long* const su = send_up + (size_t)slot * up_pts * 2;
 #pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (s1a[k] < 0) continue;
-        const int e = s1a[k], m = s1m[k];
-        double y;
-        if (m & 1) {
-          y = SRP[e + nth];
-          y = fma(CSR[e], V[e + nth], y);  // north v(j + 1, i)
-          y = fma(CSR[nsr + e], V[e], y);  // south v(j, i)
-          SRP[e + nth] = y;
-        } else {
-          y = STP[e];
-          y = fma(CST[e], V[e], y);           // west v(j0, i)
-          y = fma(CST[ns + e], V[e + 1], y);  // east v(j0, i + 1)
-          STP[e] = y;
-        }
-        if (m & 2) l2x::put(su + 2 * (m >> 3), tag, y);
-        if (m & 4) l2x::put(sd + 2 * (m >> 3), tag, y);
-      }
-    }
-    // 3. while the rows travel: the other stp rows, the receivers, the next interior velocity
-    //    (workers); 4. srp(j1), stp(j1, .) from the band above and srp(j0 - 1) from below
-    //    (pollers).  Work and polls touch different rows: the polls write only the halo rows.
-    const bool sampling = a.seis_freq && ++phase == a.seis_freq;
-    if (sampling) phase = 0;
-    bool ok = true;
-    if (split && poller) {
-      asm volatile("bar.arrive 1, %0;" ::"r"(kThreads) : "memory");  // this thread's reads of v are done
-      ok = receive(recv_above, recv_below, slot, tag, down_pts, up_pts, n_above, n_recv, srp_above, nth, nrow,
-                   SRP, STP, threadIdx.x, npt);
-    }
-    if (worker) {
-#pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (s2a[k] < 0) continue;
-        const int e = s2a[k];
-        double y = STP[e];
-        y = fma(CST[e], V[s2w[k]], y);
-        y = fma(CST[ns + e], V[s2w[k] + 1], y);
+    for (int k = 0; k < kBatch; ++k) {
+      if (s1a[k] < 0) continue;
+      const int e = s1a[k], m = s1m[k];
+      double y;
+      if (m & 1) {
+        y = SRP[e + nth];
+        y = fma(CSR[e], V[e + nth], y);  // north v(j + 1, i)
+        y = fma(CSR[nsr + e], V[e], y);  // south v(j, i)
+        SRP[e + nth] = y;
+      } else {
+        y = STP[e];
+        y = fma(CST[e], V[e], y);           // west v(j0, i)
+        y = fma(CST[ns + e], V[e + 1], y);  // east v(j0, i + 1)
         STP[e] = y;
       }
-      // the receivers of the band (Seismogram::storeVelocitySignalAtReceivers)
-      if (sampling && sample < a.seis_T) {
-        for (uint32_t q = rcv_lo + wt; q < rcv_hi; q += nwt) {
-          const unsigned long long g = a.rcv_sorted[2 * (size_t)q], r = a.rcv_sorted[2 * (size_t)q + 1];
-          const double val = V[g - (unsigned long long)j0 * nth];
-          a.seis[r + (size_t)a.R * sample] = val;
-          if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
-        }
-      }
-      // every read of this step's v and every stress row is done
-      if (split)
-        asm volatile("bar.sync 1, %0;" ::"r"(kThreads) : "memory");
-      else
-        __syncthreads();
-      if (it + 1 < a.nsteps) {
-        if (vi_force) velocity<true>(vi, V, SRP, STP, CV, nv, nth, src_p, a.ftab[it + 1]);
-        else velocity<false>(vi, V, SRP, STP, CV, nv, nth, -1, 0.0);
-      }
+      if (m & 2) l2x::put(su + 2 * (m >> 3), tag, y);
+      if (m & 4) l2x::put(sd + 2 * (m >> 3), tag, y);
     }
-    if (sampling && sample < a.seis_T) ++sample;
-    if (!split)
-      ok = receive(recv_above, recv_below, slot, tag, down_pts, up_pts, n_above, n_recv, srp_above, nth, nrow, SRP,
-                   STP, threadIdx.x, npt);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
-      break;
+  };
+  auto unsent = [&]() {
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k) {
+      if (s2a[k] < 0) continue;
+      const int e = s2a[k];
+      double y = STP[e];
+      y = fma(CST[e], V[s2w[k]], y);
+      y = fma(CST[ns + e], V[s2w[k] + 1], y);
+      STP[e] = y;
     }
-  }
+  };
+  auto recv = [&](uint32_t slot, uint32_t tag, uint32_t t, uint32_t nt) {
+    return receive(recv_above, recv_below, slot, tag, down_pts, up_pts, n_above, n_recv, srp_above, nth, nrow, SRP,
+                   STP, t, nt);
+  };
+  band_steps(a, V, (unsigned long long)j0 * nth, (unsigned long long)j1 * nth, split, poller, worker, wt, nwt, npt,
+             vel_edge, vel_int, send, unsent, recv);
   // the band back to the state (its own rows only)
   for (uint32_t e = threadIdx.x; e < nrow * nth; e += kThreads) a.xv[(size_t)j0 * nth + e] = V[e];
   for (uint32_t e = threadIdx.x; e < nrow * nth; e += kThreads) {
@@ -601,26 +622,6 @@ __global__ void __launch_bounds__(kThreads, 1) fom_bandc_kernel(const Args a) {
   }
   const bool ve_force = __any_sync(0xffffffffu, ve_src), vi_force = __any_sync(0xffffffffu, vi_src);
 
-  // receivers: a range of the list in column-major key order (key = i nr + j = V place + i0 nr)
-  __shared__ uint32_t s_rcv[2];
-  if (threadIdx.x < 2) {
-    const unsigned long long key = (unsigned long long)(threadIdx.x ? i1 : i0) * nr;
-    uint32_t lo = 0, hi = a.R;
-    while (lo < hi) {
-      const uint32_t mid = lo + (hi - lo) / 2;
-      if (a.rcv_sorted[2 * (size_t)mid] < key) lo = mid + 1; else hi = mid;
-    }
-    s_rcv[threadIdx.x] = lo;
-  }
-  uint32_t phase = a.seis_freq ? (uint32_t)(a.step0 % a.seis_freq) : 0;
-  uint32_t sample = 0;
-  if (a.seis_freq) {
-    const unsigned long long s0 = a.step0 / a.seis_freq;
-    sample = s0 < a.seis_T ? (uint32_t)s0 : a.seis_T;
-  }
-  __syncthreads();
-  const uint32_t rcv_lo = s_rcv[0], rcv_hi = s_rcv[1];
-
   auto stress = [&](int t, int v0, int m) -> double {  // one element, the stress kernel's FMAs
     if (m & 1) {  // srp(j, i): north v(j + 1, i), south v(j, i)
       double y = SRP[t];
@@ -635,68 +636,39 @@ __global__ void __launch_bounds__(kThreads, 1) fom_bandc_kernel(const Args a) {
     STP[t] = y;
     return y;
   };
-
-  if (a.nsteps > 0) {
-    if (vi_force) velocity_cols<true>(vi, V, SRP, STP, CV, nv, nr, src_p, a.ftab[0]);
-    else velocity_cols<false>(vi, V, SRP, STP, CV, nv, nr, -1, 0.0);
-  }
-  for (unsigned long long it = 0; it < a.nsteps; ++it) {
-    const uint32_t tag = a.tag0 + (uint32_t)it;
-    const uint32_t slot = (uint32_t)(it & 1);
+  auto vel_edge = [&](unsigned long long it) {
     if (ve_force) velocity_cols<true>(ve, V, SRP, STP, CV, nv, nr, src_p, a.ftab[it]);
     else velocity_cols<false>(ve, V, SRP, STP, CV, nv, nr, -1, 0.0);
-    __syncthreads();
-    {
-      unsigned long long* const sl = send_left + (size_t)slot * left_pts * 2;
-      unsigned long long* const sr = send_right + (size_t)slot * right_pts * 2;
+  };
+  auto vel_int = [&](unsigned long long it) {
+    if (vi_force) velocity_cols<true>(vi, V, SRP, STP, CV, nv, nr, src_p, a.ftab[it]);
+    else velocity_cols<false>(vi, V, SRP, STP, CV, nv, nr, -1, 0.0);
+  };
+  auto send = [&](uint32_t tag, uint32_t slot) {
+    unsigned long long* const sl = send_left + (size_t)slot * left_pts * 2;
+    unsigned long long* const sr = send_right + (size_t)slot * right_pts * 2;
 #pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        if (s1t[k] < 0) continue;
-        const int m = s1m[k];
-        const double y = stress(s1t[k], s1v[k], m);
-        const int pt = (m >> 3) & ((1 << 27) - 1);
-        if (m & 4) l2x::put(sl + 2 * pt, tag, y);
-        if (m & 2) l2x::put(sr + 2 * ((m & (1 << 30)) ? pt - (int)ns1 : pt), tag, y);
-      }
+    for (int k = 0; k < kBatch; ++k) {
+      if (s1t[k] < 0) continue;
+      const int m = s1m[k];
+      const double y = stress(s1t[k], s1v[k], m);
+      const int pt = (m >> 3) & ((1 << 27) - 1);
+      if (m & 4) l2x::put(sl + 2 * pt, tag, y);
+      if (m & 2) l2x::put(sr + 2 * ((m & (1 << 30)) ? pt - (int)ns1 : pt), tag, y);
     }
-    const bool sampling = a.seis_freq && ++phase == a.seis_freq;
-    if (sampling) phase = 0;
-    bool ok = true;
-    if (split && poller) {
-      asm volatile("bar.arrive 1, %0;" ::"r"(kThreads) : "memory");
-      ok = receive_cols(recv_right, recv_left, slot, tag, left_pts, right_pts, n_right, n_recv, nr, ncol, SRP, STP,
-                        threadIdx.x, npt);
-    }
-    if (worker) {
+  };
+  auto unsent = [&]() {
 #pragma unroll
-      for (int k = 0; k < kBatch; ++k)
-        if (s2t[k] >= 0) stress(s2t[k], s2v[k], s2m[k]);
-      if (sampling && sample < a.seis_T) {
-        for (uint32_t q = rcv_lo + wt; q < rcv_hi; q += nwt) {
-          const unsigned long long g = a.rcv_sorted[2 * (size_t)q], r = a.rcv_sorted[2 * (size_t)q + 1];
-          const double val = V[g - (unsigned long long)i0 * nr];
-          a.seis[r + (size_t)a.R * sample] = val;
-          if (!isfinite(val)) atomicOr(&a.ctl->nonfinite, 1u);
-        }
-      }
-      if (split)
-        asm volatile("bar.sync 1, %0;" ::"r"(kThreads) : "memory");
-      else
-        __syncthreads();
-      if (it + 1 < a.nsteps) {
-        if (vi_force) velocity_cols<true>(vi, V, SRP, STP, CV, nv, nr, src_p, a.ftab[it + 1]);
-        else velocity_cols<false>(vi, V, SRP, STP, CV, nv, nr, -1, 0.0);
-      }
-    }
-    if (sampling && sample < a.seis_T) ++sample;
-    if (!split)
-      ok = receive_cols(recv_right, recv_left, slot, tag, left_pts, right_pts, n_right, n_recv, nr, ncol, SRP, STP,
-                        threadIdx.x, npt);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicOr(&a.ctl->error, 1u);
-      break;
-    }
-  }
+    for (int k = 0; k < kBatch; ++k)
+      if (s2t[k] >= 0) stress(s2t[k], s2v[k], s2m[k]);
+  };
+  auto recv = [&](uint32_t slot, uint32_t tag, uint32_t t, uint32_t nt) {
+    return receive_cols(recv_right, recv_left, slot, tag, left_pts, right_pts, n_right, n_recv, nr, ncol, SRP, STP,
+                        t, nt);
+  };
+  // receivers in column-major key order (key = i nr + j = V place + i0 nr)
+  band_steps(a, V, (unsigned long long)i0 * nr, (unsigned long long)i1 * nr, split, poller, worker, wt, nwt, npt,
+             vel_edge, vel_int, send, unsent, recv);
   // the band back to the state (its own columns only)
   for (uint32_t e = threadIdx.x; e < ncol * nr; e += kThreads) {
     const uint32_t c = e / nr, j = e - c * nr;
